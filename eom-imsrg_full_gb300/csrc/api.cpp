@@ -1,0 +1,504 @@
+// api.cpp -- the extern "C" entry points of include/imsrg_gpu.h and the host
+// side of the Magnus flow.
+//
+// The flow drivers restate IMSRG_MAGNUS.f90 (n-parzuchowski/EOM-IMSRG_FULL,
+// im-SRG/): MAGNUS_EXPAND (:622-693), BCH_EXPAND (:149-234), euler_step
+// (:756-766) and magnus_decouple (:15-128).  Operators stay resident on the
+// device; only the scalars that steer the series (norms, mbpt2, E0) are read
+// back.  The reference allocates fresh work operators in every BCH/MAGNUS call
+// (:164-174, :633-643); here they are allocated once per basis and reused, and
+// the INT1/AD/INT2 copies become two alternating buffers.
+#include <cmath>
+#include <cstring>
+#include <new>
+
+#include "internal.h"
+
+using imsrg::cuda_status;
+
+namespace {
+
+// Truncated Bernoulli coefficients of IMSRG_MAGNUS.f90:648, kept for parity.
+const double kMagnusCof[7] = {1.0, -0.5, .0833333333, 0.0, -0.00138888888, 0.0, 3.306878e-5};
+
+int check_op(const imsrg_op *op) { return (op && op->b && op->d) ? IMSRG_OK : IMSRG_ERR_INVALID; }
+
+int read_scalar(imsrg_basis *b, const double *d, double *out) {
+  IMSRG_CUDA_TRY(cudaMemcpyAsync(b->h_scal, d, sizeof(double), cudaMemcpyDeviceToHost, b->stream));
+  IMSRG_CUDA_TRY(cudaStreamSynchronize(b->stream));
+  *out = b->h_scal[0];
+  return IMSRG_OK;
+}
+
+int op_norm(imsrg_basis *b, const double *d, double *out) {
+  IMSRG_TRY(imsrg::launch_norm(b, d, b->scal));
+  return read_scalar(b, b->scal, out);
+}
+
+int copy_dev(imsrg_basis *b, const double *src, double *dst, long n) {
+  if (src == dst) return IMSRG_OK;
+  IMSRG_CUDA_TRY(cudaMemcpyAsync(dst, src, n * sizeof(double), cudaMemcpyDeviceToDevice, b->stream));
+  return IMSRG_OK;
+}
+
+// Work operators of the flow, created on first use: 0,1 alternating
+// commutator buffers, 2 the unevolved H, 3 the generator / dOmega.
+int tmp_op(imsrg_basis *b, int k, imsrg_op **out) {
+  while ((int)b->tmp_ops.size() <= k) {
+    imsrg_op *op = nullptr;
+    int s = imsrg_gpu_op_create(b, 1, &op);
+    if (s != IMSRG_OK) return s;
+    b->tmp_ops.push_back(op);
+  }
+  *out = b->tmp_ops[k];
+  return IMSRG_OK;
+}
+
+}  // namespace
+
+namespace imsrg {
+
+int commutator_dev(imsrg_basis *b, const double *L, int hL, const double *R, int hR, double *RES, int hRES,
+                   int precision, int with_e0) {
+  IMSRG_TRY(launch_cc_forward(b, L, hL, R, hR));
+  if (precision == IMSRG_PREC_FP64) {
+    IMSRG_TRY(launch_gemm_fp64(b, L, hL, R, hR));
+  } else if (precision == IMSRG_PREC_OZAKI) {
+    IMSRG_TRY(ozaki_gemm(b, L, hL, R, hR));
+  } else {
+    return IMSRG_ERR_INVALID;
+  }
+  IMSRG_TRY(launch_assemble_2body(b, L, hL, R, hR, RES, hRES));
+  IMSRG_TRY(launch_assemble_1body(b, L, hL, R, hR, RES, hRES, with_e0));
+  return IMSRG_OK;
+}
+
+}  // namespace imsrg
+
+extern "C" {
+
+const char *imsrg_gpu_strerror(int s) {
+  switch (s) {
+    case IMSRG_OK: return "ok";
+    case IMSRG_ERR_INVALID: return "invalid argument, shape or handle";
+    case IMSRG_ERR_CUDA: return "CUDA runtime error";
+    case IMSRG_ERR_OOM: return "device allocation failed";
+    case IMSRG_ERR_NOT_CONVERGED: return "BCH series did not converge in 39 terms (clipping BCH)";
+    case IMSRG_ERR_NONFINITE: return "non-finite value in a result";
+    case IMSRG_ERR_TIMEOUT: return "a bounded device wait gave up";
+    case IMSRG_ERR_MISMATCH: return "operators belong to different bases";
+    case IMSRG_ERR_NO_DEVICE: return "no usable CUDA device";
+    default: return "unknown status";
+  }
+}
+
+int imsrg_gpu_basis_create(int norb, const int *nn, const int *ll, const int *jj, const int *itzp, const int *con,
+                           imsrg_basis_t **out) {
+  if (!out || norb <= 0 || norb > 4096 || !nn || !ll || !jj || !itzp || !con) return IMSRG_ERR_INVALID;
+  *out = nullptr;
+  int nholes = 0;
+  for (int i = 0; i < norb; i++) {
+    if (jj[i] <= 0 || jj[i] % 2 != 1 || ll[i] < 0 || nn[i] < 0) return IMSRG_ERR_INVALID;
+    if (itzp[i] != 1 && itzp[i] != -1) return IMSRG_ERR_INVALID;
+    if (con[i] != 0 && con[i] != 1) return IMSRG_ERR_INVALID;
+    if (std::abs(2 * ll[i] - jj[i]) != 1) return IMSRG_ERR_INVALID;
+    nholes += con[i];
+  }
+  if (nholes == 0 || nholes == norb) return IMSRG_ERR_INVALID;
+  int ndev = 0;
+  cudaError_t ce = cudaGetDeviceCount(&ndev);
+  if (ce != cudaSuccess || ndev == 0) return IMSRG_ERR_NO_DEVICE;
+  imsrg_basis *b = new (std::nothrow) imsrg_basis();
+  if (!b) return IMSRG_ERR_OOM;
+  b->norb = norb;
+  b->nn.assign(nn, nn + norb);
+  b->ll.assign(ll, ll + norb);
+  b->jj.assign(jj, jj + norb);
+  b->itzp.assign(itzp, itzp + norb);
+  b->con.assign(con, con + norb);
+  int s = imsrg::build_basis(b);
+  if (s != IMSRG_OK) {
+    imsrg::free_basis_device(b);
+    delete b;
+    return s;
+  }
+  *out = b;
+  return IMSRG_OK;
+}
+
+int imsrg_gpu_basis_destroy(imsrg_basis_t *b) {
+  if (!b) return IMSRG_ERR_INVALID;
+  for (imsrg_op *op : b->tmp_ops) {
+    cudaFree(op->d);
+    delete op;
+  }
+  b->tmp_ops.clear();
+  imsrg::free_basis_device(b);
+  delete b;
+  return IMSRG_OK;
+}
+
+int imsrg_gpu_basis_info(const imsrg_basis_t *b, imsrg_basis_info_t *info) {
+  if (!b || !info) return IMSRG_ERR_INVALID;
+  info->norb = b->norb;
+  info->nholes = b->A;
+  info->nparts = b->P;
+  info->nblocks = b->nblocks;
+  info->jtotal_max = b->jtm;
+  info->ccblocks = b->ccblocks;
+  info->nfull = b->nfull;
+  info->neq = b->neq;
+  info->cc_total = b->cc_total;
+  info->wcc_total = b->wcc_total;
+  return IMSRG_OK;
+}
+
+int imsrg_gpu_block_dims(const imsrg_basis_t *b, int q, int *npp, int *nph, int *nhh) {
+  if (!b || q < 1 || q > b->nblocks) return IMSRG_ERR_INVALID;
+  if (npp) *npp = b->npp[q - 1];
+  if (nph) *nph = b->nph[q - 1];
+  if (nhh) *nhh = b->nhh[q - 1];
+  return IMSRG_OK;
+}
+
+int imsrg_gpu_synchronize(imsrg_basis_t *b) {
+  if (!b) return IMSRG_ERR_INVALID;
+  return cuda_status(cudaStreamSynchronize(b->stream));
+}
+
+int imsrg_gpu_launch_count(const imsrg_basis_t *b, long *count) {
+  if (!b || !count) return IMSRG_ERR_INVALID;
+  *count = b->launches;
+  return IMSRG_OK;
+}
+
+int imsrg_gpu_op_create(imsrg_basis_t *b, int herm, imsrg_op_t **out) {
+  if (!b || !out || (herm != 1 && herm != -1)) return IMSRG_ERR_INVALID;
+  *out = nullptr;
+  imsrg_op *op = new (std::nothrow) imsrg_op();
+  if (!op) return IMSRG_ERR_OOM;
+  op->b = b;
+  op->herm = herm;
+  cudaError_t ce = cudaMalloc(&op->d, b->nfull * sizeof(double));
+  if (ce != cudaSuccess) {
+    delete op;
+    return cuda_status(ce);
+  }
+  ce = cudaMemsetAsync(op->d, 0, b->nfull * sizeof(double), b->stream);
+  if (ce == cudaSuccess) ce = cudaStreamSynchronize(b->stream);
+  if (ce != cudaSuccess) {
+    cudaFree(op->d);
+    delete op;
+    return cuda_status(ce);
+  }
+  *out = op;
+  return IMSRG_OK;
+}
+
+int imsrg_gpu_op_destroy(imsrg_op_t *op) {
+  if (!op) return IMSRG_ERR_INVALID;
+  if (op->b) cudaStreamSynchronize(op->b->stream);
+  cudaFree(op->d);
+  delete op;
+  return IMSRG_OK;
+}
+
+int imsrg_gpu_op_set_herm(imsrg_op_t *op, int herm) {
+  IMSRG_TRY(check_op(op));
+  if (herm != 1 && herm != -1) return IMSRG_ERR_INVALID;
+  op->herm = herm;
+  return IMSRG_OK;
+}
+
+int imsrg_gpu_op_get_herm(const imsrg_op_t *op, int *herm) {
+  IMSRG_TRY(check_op(op));
+  if (!herm) return IMSRG_ERR_INVALID;
+  *herm = op->herm;
+  return IMSRG_OK;
+}
+
+int imsrg_gpu_op_device_ptr(imsrg_op_t *op, double **dptr) {
+  IMSRG_TRY(check_op(op));
+  if (!dptr) return IMSRG_ERR_INVALID;
+  *dptr = op->d;
+  return IMSRG_OK;
+}
+
+int imsrg_gpu_op_upload_flat(imsrg_op_t *op, const double *flat) {
+  IMSRG_TRY(check_op(op));
+  if (!flat) return IMSRG_ERR_INVALID;
+  imsrg_basis *b = op->b;
+  IMSRG_CUDA_TRY(cudaMemcpyAsync(op->d, flat, b->nfull * sizeof(double), cudaMemcpyHostToDevice, b->stream));
+  return cuda_status(cudaStreamSynchronize(b->stream));
+}
+
+int imsrg_gpu_op_download_flat(const imsrg_op_t *op, double *flat) {
+  IMSRG_TRY(check_op(op));
+  if (!flat) return IMSRG_ERR_INVALID;
+  imsrg_basis *b = op->b;
+  IMSRG_CUDA_TRY(cudaMemcpyAsync(flat, op->d, b->nfull * sizeof(double), cudaMemcpyDeviceToHost, b->stream));
+  return cuda_status(cudaStreamSynchronize(b->stream));
+}
+
+int imsrg_gpu_op_upload(imsrg_op_t *op, double e0, const double *fhh, const double *fph, const double *fpp,
+                        const double *const *gam) {
+  IMSRG_TRY(check_op(op));
+  imsrg_basis *b = op->b;
+  if ((b->A && !fhh) || (b->A * b->P && !fph) || (b->P && !fpp) || !gam) return IMSRG_ERR_INVALID;
+  IMSRG_CUDA_TRY(cudaStreamSynchronize(b->stream));  // h_stage may be in flight
+  double *h = b->h_stage;
+  h[0] = e0;
+  std::memcpy(h + b->off_fhh, fhh, (size_t)b->A * b->A * sizeof(double));
+  std::memcpy(h + b->off_fph, fph, (size_t)b->P * b->A * sizeof(double));
+  std::memcpy(h + b->off_fpp, fpp, (size_t)b->P * b->P * sizeof(double));
+  for (int k = 0; k < b->nblocks * 6; k++) {
+    size_t n = (size_t)b->gam_n1[k] * b->gam_n2[k];
+    if (n == 0) continue;
+    if (!gam[k]) return IMSRG_ERR_INVALID;
+    std::memcpy(h + b->gam_off[k], gam[k], n * sizeof(double));
+  }
+  IMSRG_CUDA_TRY(cudaMemcpyAsync(op->d, h, b->nfull * sizeof(double), cudaMemcpyHostToDevice, b->stream));
+  return cuda_status(cudaStreamSynchronize(b->stream));
+}
+
+int imsrg_gpu_op_download(const imsrg_op_t *op, double *e0, double *fhh, double *fph, double *fpp,
+                          double *const *gam) {
+  IMSRG_TRY(check_op(op));
+  imsrg_basis *b = op->b;
+  IMSRG_CUDA_TRY(cudaStreamSynchronize(b->stream));
+  double *h = b->h_stage;
+  IMSRG_CUDA_TRY(cudaMemcpyAsync(h, op->d, b->nfull * sizeof(double), cudaMemcpyDeviceToHost, b->stream));
+  IMSRG_CUDA_TRY(cudaStreamSynchronize(b->stream));
+  if (e0) *e0 = h[0];
+  if (fhh) std::memcpy(fhh, h + b->off_fhh, (size_t)b->A * b->A * sizeof(double));
+  if (fph) std::memcpy(fph, h + b->off_fph, (size_t)b->P * b->A * sizeof(double));
+  if (fpp) std::memcpy(fpp, h + b->off_fpp, (size_t)b->P * b->P * sizeof(double));
+  if (gam) {
+    for (int k = 0; k < b->nblocks * 6; k++) {
+      size_t n = (size_t)b->gam_n1[k] * b->gam_n2[k];
+      if (n == 0 || !gam[k]) continue;
+      std::memcpy(gam[k], h + b->gam_off[k], n * sizeof(double));
+    }
+  }
+  return IMSRG_OK;
+}
+
+int imsrg_gpu_op_upload_packed(imsrg_op_t *op, const double *packed) {
+  IMSRG_TRY(check_op(op));
+  if (!packed) return IMSRG_ERR_INVALID;
+  imsrg_basis *b = op->b;
+  IMSRG_CUDA_TRY(cudaMemcpyAsync(b->d_stage, packed, b->neq * sizeof(double), cudaMemcpyHostToDevice, b->stream));
+  IMSRG_TRY(imsrg::launch_unpack(b, b->d_stage, op->herm, op->d));
+  return cuda_status(cudaStreamSynchronize(b->stream));
+}
+
+int imsrg_gpu_op_download_packed(const imsrg_op_t *op, double *packed) {
+  IMSRG_TRY(check_op(op));
+  if (!packed) return IMSRG_ERR_INVALID;
+  imsrg_basis *b = op->b;
+  IMSRG_TRY(imsrg::launch_pack(b, op->d, b->d_stage));
+  IMSRG_CUDA_TRY(cudaMemcpyAsync(packed, b->d_stage, b->neq * sizeof(double), cudaMemcpyDeviceToHost, b->stream));
+  return cuda_status(cudaStreamSynchronize(b->stream));
+}
+
+int imsrg_gpu_op_copy(const imsrg_op_t *src, imsrg_op_t *dst) {
+  IMSRG_TRY(check_op(src));
+  IMSRG_TRY(check_op(dst));
+  if (src->b != dst->b) return IMSRG_ERR_MISMATCH;
+  dst->herm = src->herm;
+  return copy_dev(src->b, src->d, dst->d, src->b->nfull);
+}
+
+int imsrg_gpu_op_clear(imsrg_op_t *op) {
+  IMSRG_TRY(check_op(op));
+  IMSRG_CUDA_TRY(cudaMemsetAsync(op->d, 0, op->b->nfull * sizeof(double), op->b->stream));
+  return IMSRG_OK;
+}
+
+int imsrg_gpu_op_add(const imsrg_op_t *A, double ax, const imsrg_op_t *B, double bx, imsrg_op_t *C) {
+  IMSRG_TRY(check_op(A));
+  IMSRG_TRY(check_op(B));
+  IMSRG_TRY(check_op(C));
+  if (A->b != B->b || A->b != C->b) return IMSRG_ERR_MISMATCH;
+  return imsrg::launch_axpby(A->b, A->d, ax, B->d, bx, C->d);
+}
+
+int imsrg_gpu_op_norm(const imsrg_op_t *op, double *out) {
+  IMSRG_TRY(check_op(op));
+  if (!out) return IMSRG_ERR_INVALID;
+  return op_norm(op->b, op->d, out);
+}
+
+int imsrg_gpu_op_mbpt2(const imsrg_op_t *H, double *out) {
+  IMSRG_TRY(check_op(H));
+  if (!out) return IMSRG_ERR_INVALID;
+  imsrg_basis *b = H->b;
+  IMSRG_TRY(imsrg::launch_mbpt2(b, H->d, H->herm, b->scal));
+  return read_scalar(b, b->scal, out);
+}
+
+int imsrg_gpu_op_get_e0(const imsrg_op_t *op, double *e0) {
+  IMSRG_TRY(check_op(op));
+  if (!e0) return IMSRG_ERR_INVALID;
+  return read_scalar(op->b, op->d, e0);
+}
+
+int imsrg_gpu_commutator(const imsrg_op_t *L, const imsrg_op_t *R, imsrg_op_t *RES, int precision, int with_e0) {
+  IMSRG_TRY(check_op(L));
+  IMSRG_TRY(check_op(R));
+  IMSRG_TRY(check_op(RES));
+  if (L->b != R->b || L->b != RES->b) return IMSRG_ERR_MISMATCH;
+  if (RES == L || RES == R || RES->d == L->d || RES->d == R->d) return IMSRG_ERR_INVALID;
+  int hRES = -L->herm * R->herm;
+  RES->herm = hRES;
+  return imsrg::commutator_dev(L->b, L->d, L->herm, R->d, R->herm, RES->d, hRES, precision, with_e0 ? 1 : 0);
+}
+
+int imsrg_gpu_build_gs_white(const imsrg_op_t *H, imsrg_op_t *ETA) {
+  IMSRG_TRY(check_op(H));
+  IMSRG_TRY(check_op(ETA));
+  if (H->b != ETA->b) return IMSRG_ERR_MISMATCH;
+  if (H == ETA) return IMSRG_ERR_INVALID;
+  ETA->herm = -1;
+  return imsrg::launch_white(H->b, H->d, H->herm, ETA->d);
+}
+
+int imsrg_gpu_euler_step(imsrg_op_t *G, const imsrg_op_t *DG, double *s, double ds) {
+  IMSRG_TRY(check_op(G));
+  IMSRG_TRY(check_op(DG));
+  if (G->b != DG->b) return IMSRG_ERR_MISMATCH;
+  IMSRG_TRY(imsrg::launch_axpby(G->b, G->d, 1.0, DG->d, ds, G->d));
+  if (s) *s = *s + ds;
+  return IMSRG_OK;
+}
+
+int imsrg_gpu_magnus_expand(imsrg_op_t *DG, const imsrg_op_t *G, int precision, int *ncomm) {
+  IMSRG_TRY(check_op(DG));
+  IMSRG_TRY(check_op(G));
+  if (DG->b != G->b) return IMSRG_ERR_MISMATCH;
+  imsrg_basis *b = DG->b;
+  const double conv = 1e-6;
+  imsrg_op *X[2];
+  IMSRG_TRY(tmp_op(b, 0, &X[0]));
+  IMSRG_TRY(tmp_op(b, 1, &X[1]));
+  int nc = 0;
+  double advals[8] = {0};
+  // INT2 = DG; the E0 of INT2 never changes inside the loop (no 110/220)
+  IMSRG_TRY(copy_dev(b, DG->d, X[0]->d, b->nfull));
+  IMSRG_TRY(copy_dev(b, DG->d, X[1]->d, 1));
+  X[0]->herm = X[1]->herm = DG->herm;
+  IMSRG_TRY(op_norm(b, X[0]->d, &advals[1]));
+  double fullnorm = 0.0;
+  IMSRG_TRY(op_norm(b, G->d, &fullnorm));
+  if (fullnorm < 1e-9) {
+    if (ncomm) *ncomm = 0;
+    return IMSRG_OK;
+  }
+  int q = 1, cur = 0;
+  for (int i = 2; i <= 7; i++) {
+    double adnorm = advals[i - q];
+    q = (std::fabs(kMagnusCof[i - 1]) > 1e-6) ? 1 : 2;
+    if (std::fabs(adnorm / fullnorm) < conv) break;
+    imsrg_op *AD = X[cur], *INT2 = X[1 - cur];
+    int h = -G->herm * AD->herm;
+    INT2->herm = h;
+    IMSRG_TRY(imsrg::commutator_dev(b, G->d, G->herm, AD->d, AD->herm, INT2->d, h, precision, 0));
+    nc++;
+    IMSRG_TRY(imsrg::launch_axpby(b, DG->d, 1.0, INT2->d, kMagnusCof[i - 1], DG->d));
+    double nrm = 0.0;
+    IMSRG_TRY(op_norm(b, INT2->d, &nrm));
+    if (!std::isfinite(nrm)) return IMSRG_ERR_NONFINITE;
+    advals[i] = nrm * std::fabs(kMagnusCof[i - 1]);
+    cur = 1 - cur;
+  }
+  if (ncomm) *ncomm = nc;
+  return IMSRG_OK;
+}
+
+int imsrg_gpu_bch_expand(imsrg_op_t *HS, const imsrg_op_t *G, const imsrg_op_t *H, int precision, int *ncomm) {
+  IMSRG_TRY(check_op(HS));
+  IMSRG_TRY(check_op(G));
+  IMSRG_TRY(check_op(H));
+  if (HS->b != G->b || HS->b != H->b) return IMSRG_ERR_MISMATCH;
+  imsrg_basis *b = HS->b;
+  const double conv = 1e-6;
+  imsrg_op *X[2];
+  IMSRG_TRY(tmp_op(b, 0, &X[0]));
+  IMSRG_TRY(tmp_op(b, 1, &X[1]));
+  HS->herm = H->herm;
+  IMSRG_TRY(copy_dev(b, H->d, HS->d, b->nfull));
+  IMSRG_TRY(copy_dev(b, H->d, X[0]->d, b->nfull));
+  X[0]->herm = H->herm;
+  double coef = 1.0;
+  int nc = 0, cur = 0, iw;
+  for (iw = 2; iw <= 40; iw++) {
+    coef = coef / (iw - 1.0);
+    imsrg_op *AD = X[cur], *INT2 = X[1 - cur];
+    int h = -G->herm * AD->herm;
+    INT2->herm = h;
+    IMSRG_TRY(imsrg::commutator_dev(b, G->d, G->herm, AD->d, AD->herm, INT2->d, h, precision, 1));
+    nc++;
+    IMSRG_TRY(imsrg::launch_axpby(b, HS->d, 1.0, INT2->d, coef, HS->d));
+    double nrm = 0.0;
+    IMSRG_TRY(op_norm(b, INT2->d, &nrm));
+    if (!std::isfinite(nrm)) return IMSRG_ERR_NONFINITE;
+    cur = 1 - cur;
+    if (nrm * coef < conv) break;
+  }
+  if (ncomm) *ncomm = nc;
+  return (iw > 40) ? IMSRG_ERR_NOT_CONVERGED : IMSRG_OK;
+}
+
+int imsrg_gpu_magnus_decouple(imsrg_op_t *HS, imsrg_op_t *G, double s_max, double ds, int max_steps, int precision,
+                              double *trace, int *steps_out, int *ncomm) {
+  IMSRG_TRY(check_op(HS));
+  IMSRG_TRY(check_op(G));
+  if (HS->b != G->b) return IMSRG_ERR_MISMATCH;
+  if (ds <= 0.0 || max_steps < 0) return IMSRG_ERR_INVALID;
+  imsrg_basis *b = HS->b;
+  imsrg_op *H0, *DG;
+  IMSRG_TRY(tmp_op(b, 2, &H0));
+  IMSRG_TRY(tmp_op(b, 3, &DG));
+  IMSRG_CUDA_TRY(cudaMemsetAsync(G->d, 0, b->nfull * sizeof(double), b->stream));
+  IMSRG_CUDA_TRY(cudaMemsetAsync(DG->d, 0, b->nfull * sizeof(double), b->stream));
+  G->herm = -1;
+  DG->herm = -1;
+  IMSRG_TRY(imsrg::launch_white(b, HS->d, HS->herm, DG->d));
+  IMSRG_TRY(copy_dev(b, HS->d, H0->d, b->nfull));
+  H0->herm = HS->herm;
+  double s = 0.0, e0 = 0.0, emp2 = 0.0;
+  IMSRG_TRY(imsrg_gpu_op_mbpt2(HS, &emp2));
+  IMSRG_TRY(read_scalar(b, HS->d, &e0));
+  double crit = std::fabs(emp2);
+  if (trace) {
+    trace[0] = 0; trace[1] = s; trace[2] = e0; trace[3] = e0 + emp2; trace[4] = crit;
+  }
+  int steps = 0, nct = 0;
+  while (crit > 1e-6 && s < s_max - 1e-12 && steps < max_steps) {
+    steps++;
+    int nm = 0, nb = 0;
+    IMSRG_TRY(imsrg_gpu_magnus_expand(DG, G, precision, &nm));
+    IMSRG_TRY(imsrg_gpu_euler_step(G, DG, &s, ds));
+    int st = imsrg_gpu_bch_expand(HS, G, H0, precision, &nb);
+    nct += nm + nb;
+    if (st != IMSRG_OK) {
+      if (steps_out) *steps_out = steps;
+      if (ncomm) *ncomm = nct;
+      return st;
+    }
+    IMSRG_TRY(imsrg::launch_white(b, HS->d, HS->herm, DG->d));
+    IMSRG_TRY(imsrg_gpu_op_mbpt2(HS, &emp2));
+    IMSRG_TRY(read_scalar(b, HS->d, &e0));
+    if (!std::isfinite(e0) || !std::isfinite(emp2)) return IMSRG_ERR_NONFINITE;
+    crit = std::fabs(emp2);
+    if (trace) {
+      double *t = trace + 5 * steps;
+      t[0] = steps; t[1] = s; t[2] = e0; t[3] = e0 + emp2; t[4] = crit;
+    }
+  }
+  if (steps_out) *steps_out = steps;
+  if (ncomm) *ncomm = nct;
+  return IMSRG_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,453 @@
+// basis.cpp -- host construction of the basis tables and their device copies.
+//
+// Restates the layout routines of n-parzuchowski/EOM-IMSRG_FULL (im-SRG/):
+//   holes / particles, hb4 / pb4          basic_IMSRG.f90:380-398
+//   (2J,Tz,parity) blocks, qn, xmap       basic_IMSRG.f90:477-641
+//   jbas%states (same (l,j,tz) orbits)    basic_IMSRG.f90:302-340
+//   cross-coupled blocks, rmap/nbmap      cross_coupled.f90:61-177
+//   6j table                              basic_IMSRG.f90:2183-2288 (values from
+//                                         the Racah formula, anglib.f:285-377)
+//   vectorize order                       basic_IMSRG.f90:3794-3918
+// and lays them out as dense device tables (pair -> row, (block,i,j) -> CC
+// row) in place of the reference's linear searches.
+#include <cmath>
+#include <cstring>
+#include <algorithm>
+
+#include "internal.h"
+
+namespace imsrg {
+
+int cuda_status(cudaError_t e) {
+  if (e == cudaSuccess) return IMSRG_OK;
+  if (e == cudaErrorMemoryAllocation) return IMSRG_ERR_OOM;
+  if (e == cudaErrorNoDevice || e == cudaErrorInsufficientDriver) return IMSRG_ERR_NO_DEVICE;
+  return IMSRG_ERR_CUDA;
+}
+
+namespace {
+
+bool tri(int j1, int j2, int J) { return J <= j1 + j2 && J >= std::abs(j1 - j2); }
+
+// {a b c; d e f} with doubled arguments by the Racah single sum, long double.
+struct SixJ {
+  long double fact[256];
+  SixJ() {
+    fact[0] = 1.0L;
+    for (int i = 1; i < 256; i++) fact[i] = fact[i - 1] * (long double)i;
+  }
+  long double delta(int a, int b, int c) const {  // doubled
+    return std::sqrt(fact[(a + b - c) / 2] * fact[(a - b + c) / 2] * fact[(-a + b + c) / 2] /
+                     fact[(a + b + c) / 2 + 1]);
+  }
+  double operator()(int a, int b, int c, int d, int e, int f) const {
+    auto ok = [](int x, int y, int z) { return tri(x, y, z) && ((x + y + z) % 2 == 0); };
+    if (a < 0 || b < 0 || c < 0 || d < 0 || e < 0 || f < 0) return 0.0;
+    if (!(ok(a, b, c) && ok(a, e, f) && ok(d, b, f) && ok(d, e, c))) return 0.0;
+    int s1 = (a + b + c) / 2, s2 = (a + e + f) / 2, s3 = (d + b + f) / 2, s4 = (d + e + c) / 2;
+    int p1 = (a + b + d + e) / 2, p2 = (b + c + e + f) / 2, p3 = (c + a + f + d) / 2;
+    int tmin = std::max(std::max(s1, s2), std::max(s3, s4));
+    int tmax = std::min(std::min(p1, p2), p3);
+    long double sum = 0.0L;
+    for (int t = tmin; t <= tmax; t++) {
+      long double term = fact[t + 1] / (fact[t - s1] * fact[t - s2] * fact[t - s3] * fact[t - s4] *
+                                        fact[p1 - t] * fact[p2 - t] * fact[p3 - t]);
+      sum += (t % 2) ? -term : term;
+    }
+    return (double)(sum * delta(a, b, c) * delta(a, e, f) * delta(d, b, f) * delta(d, e, c));
+  }
+};
+
+template <typename T>
+int dev_upload(imsrg_basis *b, const std::vector<T> &h, const T **out) {
+  size_t n = std::max<size_t>(h.size(), 1) * sizeof(T);
+  void *p = nullptr;
+  IMSRG_CUDA_TRY(cudaMalloc(&p, n));
+  b->dev_allocs.push_back(p);
+  if (!h.empty()) IMSRG_CUDA_TRY(cudaMemcpy(p, h.data(), h.size() * sizeof(T), cudaMemcpyHostToDevice));
+  *out = (const T *)p;
+  return IMSRG_OK;
+}
+
+int dev_alloc(imsrg_basis *b, size_t bytes, void **out) {
+  void *p = nullptr;
+  IMSRG_CUDA_TRY(cudaMalloc(&p, std::max<size_t>(bytes, 16)));
+  IMSRG_CUDA_TRY(cudaMemset(p, 0, std::max<size_t>(bytes, 16)));
+  b->dev_allocs.push_back(p);
+  *out = p;
+  return IMSRG_OK;
+}
+
+// --- grouped GEMM problems of commutator_222_pp_hh (commutators.f90:596-766)
+// and of the WCC product of commutator_222_ph (:792-802).
+struct ProbBuilder {
+  std::vector<GemmProb> probs;
+  void add(int M, int N, int K, int c_dst, long c_off, int ldc, std::initializer_list<GemmTerm> terms) {
+    if (M <= 0 || N <= 0) return;
+    GemmProb p{};
+    p.M = M;
+    p.N = N;
+    p.K = K;
+    p.nterms = 0;
+    for (const GemmTerm &t : terms) p.t[p.nterms++] = t;
+    p.c_dst = c_dst;
+    p.c_off = c_off;
+    p.ldc = ldc;
+    probs.push_back(p);
+  }
+};
+
+GemmTerm term(int a, long aoff, int lda, int ta, int bsrc, long boff, int ldb, int tb, double coef, int hl = 0,
+              int hr = 0) {
+  GemmTerm t{};
+  t.a_src = a;
+  t.a_off = aoff;
+  t.lda = lda;
+  t.ta = ta;
+  t.b_src = bsrc;
+  t.b_off = boff;
+  t.ldb = ldb;
+  t.tb = tb;
+  t.coef = coef;
+  t.use_hl = hl;
+  t.use_hr = hr;
+  return t;
+}
+
+}  // namespace
+
+int build_basis(imsrg_basis *b) {
+  const int N = b->norb;
+  // holes / particles (find_holes, basic_IMSRG.f90:380-398)
+  std::vector<int> orbpos(N);
+  b->holes.clear();
+  b->parts.clear();
+  for (int i = 0; i < N; i++) {
+    if (b->con[i] == 1) {
+      orbpos[i] = (int)b->holes.size();
+      b->holes.push_back(i);
+    } else {
+      orbpos[i] = (int)b->parts.size();
+      b->parts.push_back(i);
+    }
+  }
+  b->A = (int)b->holes.size();
+  b->P = (int)b->parts.size();
+  b->jtm = *std::max_element(b->jj.begin(), b->jj.end());
+  const int jtm = b->jtm, nJ = jtm + 1, nj = (jtm + 1) / 2;
+  const int A = b->A, P = b->P;
+
+  // blocks (allocate_blocks, basic_IMSRG.f90:528-637)
+  b->nblocks = (jtm + 1) * 6;
+  b->npp.assign(b->nblocks, 0);
+  b->nph.assign(b->nblocks, 0);
+  b->nhh.assign(b->nblocks, 0);
+  b->qn.assign(b->nblocks * 3, {});
+  b->gam_off.assign(b->nblocks * 6, 0);
+  b->gam_n1.assign(b->nblocks * 6, 0);
+  b->gam_n2.assign(b->nblocks * 6, 0);
+  std::vector<int> pairrow((size_t)N * N * nJ, -1);
+  std::vector<int> blk_J2(b->nblocks);
+  b->off_fhh = 1;
+  b->off_fph = 1 + (long)A * A;
+  b->off_fpp = b->off_fph + (long)P * A;
+  long off = b->off_fpp + (long)P * P;
+  long neq = 1 + (long)A * A + (long)P * P + (long)P * A;
+  static const int sq[6] = {1, 0, 0, 1, 1, 0};
+  int q = 0;
+  for (int J2 = 0; J2 <= 2 * jtm; J2 += 2)
+    for (int Tz = -1; Tz <= 1; Tz++)
+      for (int Par = 0; Par <= 1; Par++, q++) {
+        blk_J2[q] = J2;
+        int cnt[3] = {0, 0, 0};
+        for (int i = 0; i < N; i++)
+          for (int j = i; j < N; j++) {
+            if (Tz != (b->itzp[i] + b->itzp[j]) / 2) continue;
+            if (Par != (b->ll[i] + b->ll[j]) % 2) continue;
+            if (!tri(b->jj[i], b->jj[j], J2)) continue;
+            int c = b->con[i] + b->con[j];
+            pairrow[((size_t)i * N + j) * nJ + J2 / 2] = cnt[c]++;
+            b->qn[q * 3 + c].push_back(i);
+            b->qn[q * 3 + c].push_back(j);
+          }
+        b->npp[q] = cnt[0];
+        b->nph[q] = cnt[1];
+        b->nhh[q] = cnt[2];
+        int d1[6] = {cnt[0], cnt[0], cnt[0], cnt[1], cnt[2], cnt[1]};
+        int d2[6] = {cnt[0], cnt[1], cnt[2], cnt[1], cnt[2], cnt[2]};
+        for (int g = 0; g < 6; g++) {
+          b->gam_off[q * 6 + g] = off;
+          b->gam_n1[q * 6 + g] = d1[g];
+          b->gam_n2[q * 6 + g] = d2[g];
+          off += (long)d1[g] * d2[g];
+          neq += sq[g] ? (long)d1[g] * (d1[g] + 1) / 2 : (long)d1[g] * d2[g];
+        }
+      }
+  b->nfull = off;
+  b->neq = neq;
+
+  // orbits sharing (l, j, tz): jbas%states (basic_IMSRG.f90:302-340)
+  std::vector<int> ljt_start(N), ljt_count(N), ljt_list;
+  for (int a = 0; a < N; a++) {
+    ljt_start[a] = (int)ljt_list.size();
+    for (int i = 0; i < N; i++)
+      if (b->jj[i] == b->jj[a] && b->ll[i] == b->ll[a] && b->itzp[i] == b->itzp[a]) ljt_list.push_back(i);
+    ljt_count[a] = (int)ljt_list.size() - ljt_start[a];
+  }
+  std::vector<int> ph_pairs;
+  for (int a = 0; a < P; a++)
+    for (int i = 0; i < A; i++) {
+      int ak = b->parts[a], ik = b->holes[i];
+      if (b->jj[ak] == b->jj[ik] && b->ll[ak] == b->ll[ik] && b->itzp[ak] == b->itzp[ik]) {
+        ph_pairs.push_back(a);
+        ph_pairs.push_back(i);
+      }
+    }
+
+  // cross-coupled layout (allocate_CCMAT, cross_coupled.f90:110-175)
+  b->ccblocks = (jtm + 1) * 4;
+  b->cc_rlen.assign(b->ccblocks, 0);
+  b->cc_nph.assign(b->ccblocks, 0);
+  b->cc_J2.assign(b->ccblocks, 0);
+  b->cc_off.assign(b->ccblocks, 0);
+  b->wcc_off.assign(b->ccblocks, 0);
+  std::vector<int> cc_row((size_t)b->ccblocks * N * N, -1);
+  std::vector<int> cc_rowpair, cc_rowstart(b->ccblocks), cc_colpair, cc_colstart(b->ccblocks);
+  long coff = 0, woff = 0;
+  for (int q1 = 0; q1 < b->ccblocks; q1++) {
+    int JC = (q1 % (jtm + 1)) * 2;
+    int PAR = q1 / (2 * jtm + 2);
+    int TZ = (q1 % (2 * jtm + 2)) / (jtm + 1);
+    cc_rowstart[q1] = (int)cc_rowpair.size();
+    cc_colstart[q1] = (int)cc_colpair.size();
+    int r = 0, nb = 0;
+    for (int i = 0; i < N; i++)
+      for (int j = 0; j < N; j++) {
+        if (!tri(b->jj[i], b->jj[j], JC)) continue;
+        if ((b->ll[i] + b->ll[j]) % 2 != PAR) continue;
+        if (std::abs(b->itzp[i] - b->itzp[j]) / 2 != TZ) continue;
+        cc_row[((size_t)q1 * N + i) * N + j] = r++;
+        cc_rowpair.push_back(i * 65536 + j);
+        if (b->con[i] == 0 && b->con[j] == 1) {
+          cc_colpair.push_back(i * 65536 + j);
+          nb++;
+        }
+      }
+    b->cc_rlen[q1] = r;
+    b->cc_nph[q1] = nb;
+    b->cc_J2[q1] = JC;
+    b->cc_off[q1] = coff;
+    b->wcc_off[q1] = woff;
+    coff += (long)r * nb;
+    woff += (long)r * r;
+  }
+  b->cc_total = coff;
+  b->wcc_total = woff;
+
+  // 6j table: [j1h][j2h][j4h][j5h][J3][J6] for {j1 j2 J3; j4 j5 J6}
+  SixJ sj;
+  std::vector<double> six((size_t)nj * nj * nj * nj * nJ * nJ, 0.0);
+  for (int a = 0; a < nj; a++)
+    for (int c = 0; c < nj; c++)
+      for (int d = 0; d < nj; d++)
+        for (int e = 0; e < nj; e++)
+          for (int J3 = 0; J3 < nJ; J3++)
+            for (int J6 = 0; J6 < nJ; J6++)
+              six[((((size_t)a * nj + c) * nj + d) * nj + e) * nJ * nJ + J3 * nJ + J6] =
+                  sj(2 * a + 1, 2 * c + 1, 2 * J3, 2 * d + 1, 2 * e + 1, 2 * J6);
+
+  // GEMM problems of 222_pp_hh per block, then the WCC products
+  ProbBuilder pb;
+  for (int qb = 0; qb < b->nblocks; qb++) {
+    int np = b->npp[qb], nb = b->nph[qb], nh = b->nhh[qb];
+    auto G = [&](int g) { return b->gam_off[qb * 6 + g - 1]; };
+    // W1_pppp = L_pppp R_pppp
+    pb.add(np, np, np, SRC_W1, G(1), np, {term(SRC_L, G(1), np, 0, SRC_R, G(1), np, 0, 1.0)});
+    // W2_hhhh = L_hhhh R_hhhh
+    pb.add(nh, nh, nh, SRC_W2, G(5), nh, {term(SRC_L, G(5), nh, 0, SRC_R, G(5), nh, 0, 1.0)});
+    // W1_hhhh = herm_L L_pphh^T R_pphh
+    pb.add(nh, nh, np, SRC_W1, G(5), nh, {term(SRC_L, G(3), np, 1, SRC_R, G(3), np, 0, 1.0, 1, 0)});
+    // W2_pppp = herm_R L_pphh R_pphh^T
+    pb.add(np, np, nh, SRC_W2, G(1), np, {term(SRC_L, G(3), np, 0, SRC_R, G(3), np, 1, 1.0, 0, 1)});
+    // W1_pphh = L_pppp R_pphh - R_pppp L_pphh
+    pb.add(np, nh, np, SRC_W1, G(3), np,
+           {term(SRC_R, G(1), np, 0, SRC_L, G(3), np, 0, -1.0), term(SRC_L, G(1), np, 0, SRC_R, G(3), np, 0, 1.0)});
+    // W2_pphh = L_pphh R_hhhh - R_pphh L_hhhh
+    pb.add(np, nh, nh, SRC_W2, G(3), np,
+           {term(SRC_R, G(3), np, 0, SRC_L, G(5), nh, 0, -1.0), term(SRC_L, G(3), np, 0, SRC_R, G(5), nh, 0, 1.0)});
+    // W2_phph = herm_R L_phhh R_phhh^T
+    pb.add(nb, nb, nh, SRC_W2, G(4), nb, {term(SRC_L, G(6), nb, 0, SRC_R, G(6), nb, 1, 1.0, 0, 1)});
+    // W1_phph = herm_L L_ppph^T R_ppph
+    pb.add(nb, nb, np, SRC_W1, G(4), nb, {term(SRC_L, G(2), np, 1, SRC_R, G(2), np, 0, 1.0, 1, 0)});
+    // W2_phhh = L_phhh R_hhhh - R_phhh L_hhhh
+    pb.add(nb, nh, nh, SRC_W2, G(6), nb,
+           {term(SRC_R, G(6), nb, 0, SRC_L, G(5), nh, 0, -1.0), term(SRC_L, G(6), nb, 0, SRC_R, G(5), nh, 0, 1.0)});
+    // W1_ppph = L_pppp R_ppph - R_pppp L_ppph
+    pb.add(np, nb, np, SRC_W1, G(2), np,
+           {term(SRC_R, G(1), np, 0, SRC_L, G(2), np, 0, -1.0), term(SRC_L, G(1), np, 0, SRC_R, G(2), np, 0, 1.0)});
+    // W1_phhh = -herm_R R_ppph^T L_pphh + herm_L L_ppph^T R_pphh
+    pb.add(nb, nh, np, SRC_W1, G(6), nb,
+           {term(SRC_R, G(2), np, 1, SRC_L, G(3), np, 0, -1.0, 0, 1),
+            term(SRC_L, G(2), np, 1, SRC_R, G(3), np, 0, 1.0, 1, 0)});
+    // W2_ppph = herm_R L_pphh R_phhh^T - herm_L R_pphh L_phhh^T
+    pb.add(np, nb, nh, SRC_W2, G(2), np,
+           {term(SRC_R, G(3), np, 0, SRC_L, G(6), nb, 1, -1.0, 1, 0),
+            term(SRC_L, G(3), np, 0, SRC_R, G(6), nb, 1, 1.0, 0, 1)});
+  }
+  for (int q1 = 0; q1 < b->ccblocks; q1++) {
+    int r = b->cc_rlen[q1], nb = b->cc_nph[q1];
+    pb.add(r, r, nb, SRC_WCC, b->wcc_off[q1], r,
+           {term(SRC_LCC, b->cc_off[q1], r, 0, SRC_RCC, b->cc_off[q1], r, 1, 1.0)});
+  }
+  int tiles = 0;
+  for (GemmProb &p : pb.probs) {
+    p.tiles_m = (p.M + 63) / 64;
+    p.tiles = p.tiles_m * ((p.N + 63) / 64);
+    p.tile0 = tiles;
+    tiles += p.tiles;
+  }
+  b->probs = pb.probs;
+  b->nprobs = (int)pb.probs.size();
+  b->ntiles = tiles;
+
+  // norm chunks (mat_frob_norm weights: fph and non-square gam count twice)
+  std::vector<NormChunk> chunks;
+  auto add_seg = [&](long start, long len, int w) {
+    for (long s = 0; s < len; s += 4096) {
+      NormChunk c{start + s, (int)std::min<long>(4096, len - s), w};
+      chunks.push_back(c);
+    }
+  };
+  add_seg(b->off_fhh, (long)A * A, 1);
+  add_seg(b->off_fph, (long)P * A, 2);
+  add_seg(b->off_fpp, (long)P * P, 1);
+  for (int qb = 0; qb < b->nblocks; qb++)
+    for (int g = 0; g < 6; g++)
+      add_seg(b->gam_off[qb * 6 + g], (long)b->gam_n1[qb * 6 + g] * b->gam_n2[qb * 6 + g], sq[g] ? 1 : 2);
+  b->nchunks = (int)chunks.size();
+
+  // packed (vectorize) map
+  std::vector<long> psrc, pmir;
+  psrc.reserve(neq);
+  pmir.reserve(neq);
+  psrc.push_back(0);
+  pmir.push_back(-1);
+  for (long k = 0; k < (long)A * A; k++) { psrc.push_back(b->off_fhh + k); pmir.push_back(-1); }
+  for (long k = 0; k < (long)P * P; k++) { psrc.push_back(b->off_fpp + k); pmir.push_back(-1); }
+  for (long k = 0; k < (long)P * A; k++) { psrc.push_back(b->off_fph + k); pmir.push_back(-1); }
+  for (int qb = 0; qb < b->nblocks; qb++)
+    for (int g = 0; g < 6; g++) {
+      int n1 = b->gam_n1[qb * 6 + g], n2 = b->gam_n2[qb * 6 + g];
+      long o = b->gam_off[qb * 6 + g];
+      for (int i = 0; i < n2; i++)
+        for (int j = sq[g] ? i : 0; j < n1; j++) {
+          psrc.push_back(o + j + (long)i * n1);
+          pmir.push_back(sq[g] ? o + i + (long)j * n1 : -1);
+        }
+    }
+  if ((long)psrc.size() != neq) return IMSRG_ERR_INVALID;
+
+  // --- device copies
+  cudaError_t ce = cudaGetDevice(&b->device);
+  if (ce != cudaSuccess) return cuda_status(ce);
+  IMSRG_CUDA_TRY(cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking));
+  DevTables &T = b->T;
+  T.norb = N;
+  T.A = A;
+  T.P = P;
+  T.nblocks = b->nblocks;
+  T.jtm = jtm;
+  T.nJ = nJ;
+  T.nj = nj;
+  T.ccblocks = b->ccblocks;
+  T.off_fhh = b->off_fhh;
+  T.off_fph = b->off_fph;
+  T.off_fpp = b->off_fpp;
+  T.nfull = b->nfull;
+  T.cc_total = b->cc_total;
+  T.wcc_total = b->wcc_total;
+  std::vector<int4> orb(N);
+  for (int i = 0; i < N; i++) orb[i] = make_int4(b->jj[i], b->ll[i], b->itzp[i], b->con[i]);
+  std::vector<int> qn_flat, qn_start(b->nblocks * 3);
+  for (int k = 0; k < b->nblocks * 3; k++) {
+    qn_start[k] = (int)qn_flat.size();
+    qn_flat.insert(qn_flat.end(), b->qn[k].begin(), b->qn[k].end());
+  }
+  IMSRG_TRY(dev_upload(b, orb, &T.orb));
+  IMSRG_TRY(dev_upload(b, orbpos, &T.orbpos));
+  IMSRG_TRY(dev_upload(b, pairrow, &T.pairrow));
+  IMSRG_TRY(dev_upload(b, b->gam_off, &T.gam_off));
+  IMSRG_TRY(dev_upload(b, b->gam_n1, &T.gam_n1));
+  IMSRG_TRY(dev_upload(b, b->gam_n2, &T.gam_n2));
+  IMSRG_TRY(dev_upload(b, blk_J2, &T.blk_J2));
+  IMSRG_TRY(dev_upload(b, qn_flat, &T.qn));
+  IMSRG_TRY(dev_upload(b, qn_start, &T.qn_start));
+  IMSRG_TRY(dev_upload(b, six, &T.six));
+  IMSRG_TRY(dev_upload(b, ljt_start, &T.ljt_start));
+  IMSRG_TRY(dev_upload(b, ljt_count, &T.ljt_count));
+  IMSRG_TRY(dev_upload(b, ljt_list, &T.ljt_list));
+  IMSRG_TRY(dev_upload(b, cc_row, &T.cc_row));
+  IMSRG_TRY(dev_upload(b, b->cc_off, &T.cc_off));
+  IMSRG_TRY(dev_upload(b, b->wcc_off, &T.wcc_off));
+  IMSRG_TRY(dev_upload(b, b->cc_rlen, &T.cc_rlen));
+  IMSRG_TRY(dev_upload(b, b->cc_nph, &T.cc_nph));
+  IMSRG_TRY(dev_upload(b, b->cc_J2, &T.cc_J2));
+  IMSRG_TRY(dev_upload(b, cc_rowpair, &T.cc_rowpair));
+  IMSRG_TRY(dev_upload(b, cc_rowstart, &T.cc_rowstart));
+  IMSRG_TRY(dev_upload(b, cc_colpair, &T.cc_colpair));
+  IMSRG_TRY(dev_upload(b, cc_colstart, &T.cc_colstart));
+  IMSRG_TRY(dev_upload(b, ph_pairs, &T.ph_pairs));
+  IMSRG_TRY(dev_upload(b, b->holes, &T.hole_orb));
+  IMSRG_TRY(dev_upload(b, b->parts, &T.part_orb));
+  T.n_ph_pairs = (int)ph_pairs.size() / 2;
+  const GemmProb *dp = nullptr;
+  IMSRG_TRY(dev_upload(b, b->probs, &dp));
+  b->d_probs = (GemmProb *)dp;
+  const NormChunk *dc = nullptr;
+  IMSRG_TRY(dev_upload(b, chunks, &dc));
+  b->d_chunks = (NormChunk *)dc;
+  const long *d1 = nullptr, *d2 = nullptr;
+  IMSRG_TRY(dev_upload(b, psrc, &d1));
+  IMSRG_TRY(dev_upload(b, pmir, &d2));
+  b->d_pack_src = (long *)d1;
+  b->d_pack_mirror = (long *)d2;
+
+  void *p = nullptr;
+  IMSRG_TRY(dev_alloc(b, b->nfull * sizeof(double), &p));
+  b->w1 = (double *)p;
+  IMSRG_TRY(dev_alloc(b, b->nfull * sizeof(double), &p));
+  b->w2 = (double *)p;
+  IMSRG_TRY(dev_alloc(b, b->cc_total * sizeof(double), &p));
+  b->lcc = (double *)p;
+  IMSRG_TRY(dev_alloc(b, b->cc_total * sizeof(double), &p));
+  b->rcc = (double *)p;
+  IMSRG_TRY(dev_alloc(b, b->wcc_total * sizeof(double), &p));
+  b->wcc = (double *)p;
+  IMSRG_TRY(dev_alloc(b, (size_t)N * N * sizeof(double), &p));
+  b->mono = (double *)p;
+  IMSRG_TRY(dev_alloc(b, 64 * sizeof(double), &p));
+  b->scal = (double *)p;
+  b->partials_len = std::max(b->nchunks, b->nblocks) + 64;
+  IMSRG_TRY(dev_alloc(b, b->partials_len * sizeof(double), &p));
+  b->partials = (double *)p;
+  IMSRG_TRY(dev_alloc(b, std::max(b->nfull, b->neq) * sizeof(double), &p));
+  b->d_stage = (double *)p;
+  IMSRG_CUDA_TRY(cudaMallocHost(&b->h_scal, 64 * sizeof(double)));
+  IMSRG_CUDA_TRY(cudaMallocHost(&b->h_stage, std::max(b->nfull, b->neq) * sizeof(double)));
+  IMSRG_CUDA_TRY(cudaDeviceSynchronize());
+  return IMSRG_OK;
+}
+
+void free_basis_device(imsrg_basis *b) {
+  if (b->stream) cudaStreamSynchronize(b->stream);
+  ozaki_free(b);
+  for (void *p : b->dev_allocs) cudaFree(p);
+  b->dev_allocs.clear();
+  if (b->h_scal) cudaFreeHost(b->h_scal);
+  if (b->h_stage) cudaFreeHost(b->h_stage);
+  b->h_scal = b->h_stage = nullptr;
+  if (b->stream) cudaStreamDestroy(b->stream);
+  b->stream = nullptr;
+}
+
+}  // namespace imsrg

@@ -1,0 +1,107 @@
+// device.cuh -- device-side element access shared by the kernels.
+//
+// Device restatements of the reference accessors (n-parzuchowski/EOM-IMSRG_FULL,
+// im-SRG/basic_IMSRG.f90): f_elem (:1147-1177), v_elem (:1270-1385),
+// v_same (:2007-2028), sixj (:2509-2555).  v_same's COMMON-block cache becomes
+// an explicit VLoc value: a location is resolved once and read from several
+// operators.
+#pragma once
+
+#include "internal.h"
+
+namespace imsrg {
+
+__device__ __forceinline__ bool dtri(int j1, int j2, int J) { return J <= j1 + j2 && J >= abs(j1 - j2); }
+__device__ __forceinline__ double m1pow(int e) { return (e & 1) ? -1.0 : 1.0; }
+
+#define IMSRG_SQRT2 1.4142135623730951
+
+struct VLoc {
+  long idx;    // flat index, -1 when the element is structurally zero
+  double pre;  // phase and sqrt(2) normalisation
+  int trans;   // element read transposed: multiply by the operator's herm
+};
+
+__device__ __forceinline__ int pair_row(const DevTables &T, int a, int b, int J2) {
+  return T.pairrow[((long)a * T.norb + b) * T.nJ + (J2 >> 1)];
+}
+
+// Location of <ab;J|V|cd;J> (orbits 0-based, J2 doubled).
+__device__ __forceinline__ VLoc v_loc(const DevTables &T, int a, int b, int c, int d, int J2) {
+  VLoc r;
+  r.idx = -1;
+  r.pre = 0.0;
+  r.trans = 0;
+  int4 oa = T.orb[a], ob = T.orb[b], oc = T.orb[c], od = T.orb[d];
+  if (!(dtri(oa.x, ob.x, J2) && dtri(oc.x, od.x, J2))) return r;
+  int P = (oa.y + ob.y) & 1;
+  if (((oc.y + od.y) & 1) != P) return r;
+  int tz2 = oa.z + ob.z;
+  if (oc.z + od.z != tz2) return r;
+  int q = 3 * J2 + 2 * (tz2 / 2 + 1) + P;
+  int C1 = oa.w + ob.w + 1, C2 = oc.w + od.w + 1;
+  int qx = C1 * C2;
+  if (qx == 9) qx = 5;
+  double pre = 1.0;
+  int i1, i2;
+  if (a > b) {
+    i1 = pair_row(T, b, a, J2);
+    pre = m1pow(1 + (oa.x + ob.x - J2) / 2);
+  } else {
+    if (a == b) pre = pre * IMSRG_SQRT2;
+    i1 = pair_row(T, a, b, J2);
+  }
+  if (c > d) {
+    i2 = pair_row(T, d, c, J2);
+    pre = pre * m1pow(1 + (oc.x + od.x - J2) / 2);
+  } else {
+    if (c == d) pre = pre * IMSRG_SQRT2;
+    i2 = pair_row(T, c, d, J2);
+  }
+  int s = q * 6 + qx - 1;
+  if (C1 > C2) {
+    r.idx = T.gam_off[s] + i2 + (long)i1 * T.gam_n1[s];
+    r.trans = 1;
+  } else {
+    r.idx = T.gam_off[s] + i1 + (long)i2 * T.gam_n1[s];
+  }
+  r.pre = pre;
+  return r;
+}
+
+__device__ __forceinline__ double v_read(const double *op, int herm, const VLoc &l) {
+  if (l.idx < 0) return 0.0;
+  double x = op[l.idx];
+  if (l.trans) return x * herm * l.pre;
+  return x * l.pre;
+}
+
+__device__ __forceinline__ double v_elem(const DevTables &T, const double *op, int herm, int a, int b, int c, int d,
+                                         int J2) {
+  return v_read(op, herm, v_loc(T, a, b, c, d, J2));
+}
+
+__device__ __forceinline__ double f_elem(const DevTables &T, const double *op, int herm, int a, int b) {
+  int ca = T.orb[a].w, cb = T.orb[b].w;
+  int pa = T.orbpos[a], pb = T.orbpos[b];
+  int s = ca + cb;
+  if (s == 0) return op[T.off_fpp + pa + (long)pb * T.P];
+  if (s == 2) return op[T.off_fhh + pa + (long)pb * T.A];
+  if (ca > cb) return op[T.off_fph + pb + (long)pa * T.P] * herm;
+  return op[T.off_fph + pa + (long)pb * T.P];
+}
+
+// {j1 j2 J3; j4 j5 J6}: j1,j2,j4,j5 doubled half-integers, J3,J6 doubled integers.
+__device__ __forceinline__ double sixj(const DevTables &T, int j1, int j2, int J3, int j4, int j5, int J6) {
+  long idx = ((((long)(j1 >> 1) * T.nj + (j2 >> 1)) * T.nj + (j4 >> 1)) * T.nj + (j5 >> 1)) * T.nJ * T.nJ +
+             (J3 >> 1) * T.nJ + (J6 >> 1);
+  return T.six[idx];
+}
+
+__device__ __forceinline__ double warp_sum(double v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+}  // namespace imsrg

@@ -1,0 +1,180 @@
+// internal.h -- shared declarations of the imsrg_gpu library (not part of the ABI).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include "../../include/imsrg_gpu.h"
+
+namespace imsrg {
+
+// Device-resident basis tables, passed by value to every kernel.  Orbits are
+// 0-based here; angular momenta stay doubled as in the reference.
+struct DevTables {
+  int norb, A, P, nblocks, jtm, nJ, nj, ccblocks;
+  long off_fhh, off_fph, off_fpp, nfull;
+  const int4 *orb;         // x = jj, y = ll, z = itzp, w = con
+  const int *orbpos;       // position among holes (con=1) or particles (0-based)
+  const int *pairrow;      // [(a*norb+b)*nJ + J2/2], a<=b: row in its category, -1 if absent
+  const long *gam_off;     // [q*6+g] (g 0-based) flat offset
+  const int *gam_n1;       // [q*6+g]
+  const int *gam_n2;       // [q*6+g]
+  const int *blk_J2;       // [q]
+  const int *qn;           // pair lists: qn[qn_start[q*3+c] + 2*IX + k], 0-based orbits
+  const int *qn_start;     // [q*3+c], c = 0 pp, 1 ph, 2 hh
+  const double *six;       // dense 6j table, see sixj_index()
+  const int *ljt_start;    // [a]: start of orbits sharing (l,j,tz) with a
+  const int *ljt_count;    // [a]
+  const int *ljt_list;     // concatenated lists (0-based orbits, ascending)
+  const int *cc_row;       // [(q1*norb+i)*norb+j] row (0-based) or -1
+  const long *cc_off;      // [q1] offset of CCX(q1) (rlen x nph, column-major)
+  const long *wcc_off;     // [q1] offset of WCC(q1) (rlen x rlen)
+  const int *cc_rlen;      // [q1]
+  const int *cc_nph;       // [q1]
+  const int *cc_J2;        // [q1]
+  const int *cc_rowpair;   // [cc_rowstart[q1] + r] = a*65536 + b
+  const int *cc_rowstart;  // [q1]
+  const int *cc_colpair;   // [cc_colstart[q1] + c] = p*65536 + h
+  const int *cc_colstart;  // [q1]
+  const int *ph_pairs;     // (l,j,tz)-allowed (particle pos, hole pos) pairs: [2*k], [2*k+1]
+  int n_ph_pairs;
+  const int *hole_orb;     // [hole position] -> orbit
+  const int *part_orb;     // [particle position] -> orbit
+  long cc_total, wcc_total;
+};
+
+// One term alpha * op(A) * op(B) of a grouped GEMM problem.  Operand ids:
+// 0 L, 1 R, 2 W1, 3 W2, 4 LCC, 5 RCC, 6 WCC.
+struct GemmTerm {
+  int a_src, b_src;
+  int ta, tb;        // 1 = transposed
+  long a_off, b_off;
+  int lda, ldb;
+  double coef;
+  int use_hl, use_hr;  // multiply coef by herm(L) / herm(R)
+};
+
+struct GemmProb {
+  int M, N, K, nterms;
+  GemmTerm t[2];
+  int c_dst;
+  long c_off;
+  int ldc;
+  int tile0;    // first tile id of this problem
+  int tiles_m;  // tiles along M
+  int tiles;    // tiles of this problem
+};
+
+struct Operands {
+  const double *src[7];
+  double *dst[7];
+};
+
+enum { SRC_L = 0, SRC_R = 1, SRC_W1 = 2, SRC_W2 = 3, SRC_LCC = 4, SRC_RCC = 5, SRC_WCC = 6 };
+
+// Norm segments: chunks of the flat layout with weight 1 or 2.
+struct NormChunk {
+  long start;
+  int len;
+  int weight;
+};
+
+}  // namespace imsrg
+
+struct imsrg_op;
+
+struct imsrg_basis {
+  // host copies
+  int norb, A, P, nblocks, jtm, ccblocks;
+  std::vector<int> nn, ll, jj, itzp, con;
+  std::vector<int> holes, parts;  // 0-based orbit ids
+  std::vector<int> npp, nph, nhh; // per block
+  std::vector<long> gam_off;      // [q*6+g]
+  std::vector<int> gam_n1, gam_n2;
+  std::vector<std::vector<int>> qn;  // [q*3+c] pair list (0-based, 2 ints per pair)
+  std::vector<int> cc_rlen, cc_nph, cc_J2;
+  std::vector<long> cc_off, wcc_off;
+  long nfull = 0, neq = 0, cc_total = 0, wcc_total = 0;
+  long off_fhh = 1, off_fph = 0, off_fpp = 0;
+
+  // device
+  imsrg::DevTables T{};
+  std::vector<void *> dev_allocs;
+  cudaStream_t stream = nullptr;
+  int device = 0;
+  // commutator workspace
+  double *w1 = nullptr, *w2 = nullptr, *lcc = nullptr, *rcc = nullptr, *wcc = nullptr;
+  double *mono = nullptr;       // norb x norb monopole table of the White generator
+  double *scal = nullptr;       // small device scratch for reductions (E0, norms)
+  double *partials = nullptr;   // norm/mbpt2 partial sums
+  double *h_scal = nullptr;     // pinned host mirror of scal
+  int partials_len = 0;
+  // grouped GEMM problems
+  imsrg::GemmProb *d_probs = nullptr;
+  int nprobs = 0, ntiles = 0;
+  std::vector<imsrg::GemmProb> probs;
+  // norm chunks
+  imsrg::NormChunk *d_chunks = nullptr;
+  int nchunks = 0;
+  // packed layout map: packed index k -> flat index, and mirrored flat index (or -1)
+  long *d_pack_src = nullptr, *d_pack_mirror = nullptr;
+  // staging buffer (pinned) for Fortran-style uploads/downloads
+  double *h_stage = nullptr;
+  double *d_stage = nullptr;  // device staging for packed uploads
+  // flow temporaries (allocated on first use)
+  std::vector<imsrg_op *> tmp_ops;
+  long launches = 0;
+  // Ozaki split-precision engine state (allocated on first use)
+  void *ozaki = nullptr;
+};
+
+struct imsrg_op {
+  imsrg_basis *b;
+  double *d;  // nfull doubles on device
+  int herm;
+};
+
+namespace imsrg {
+
+int build_basis(imsrg_basis *b);            // host tables + device upload (basis.cpp)
+void free_basis_device(imsrg_basis *b);
+int cuda_status(cudaError_t e);
+
+// launchers (kernels_*.cu); all enqueue on b->stream and bump b->launches
+int launch_cc_forward(imsrg_basis *b, const double *L, int hL, const double *R, int hR);
+int launch_gemm_fp64(imsrg_basis *b, const double *L, int hL, const double *R, int hR);
+int launch_assemble_2body(imsrg_basis *b, const double *L, int hL, const double *R, int hR, double *RES, int hRES);
+int launch_assemble_1body(imsrg_basis *b, const double *L, int hL, const double *R, int hR, double *RES, int hRES,
+                          int with_e0);
+int launch_axpby(imsrg_basis *b, const double *A, double ax, const double *B, double bx, double *C);
+int launch_norm(imsrg_basis *b, const double *op, double *d_out);
+int launch_mbpt2(imsrg_basis *b, const double *H, int herm, double *d_out);
+int launch_white(imsrg_basis *b, const double *H, int hH, double *ETA);
+int launch_pack(imsrg_basis *b, const double *flat, double *packed);
+int launch_unpack(imsrg_basis *b, const double *packed, int herm, double *flat);
+int launch_check_finite(imsrg_basis *b, const double *op, int *d_flag);
+
+// Ozaki split-precision contraction engine (ozaki.cu)
+int ozaki_gemm(imsrg_basis *b, const double *L, int hL, const double *R, int hR);
+void ozaki_free(imsrg_basis *b);
+
+// one full commutator (api.cpp)
+int commutator_dev(imsrg_basis *b, const double *L, int hL, const double *R, int hR, double *RES, int hRES,
+                   int precision, int with_e0);
+
+}  // namespace imsrg
+
+#define IMSRG_CUDA_TRY(expr)                           \
+  do {                                                 \
+    cudaError_t _e = (expr);                           \
+    if (_e != cudaSuccess) return imsrg::cuda_status(_e); \
+  } while (0)
+
+#define IMSRG_TRY(expr)          \
+  do {                           \
+    int _s = (expr);             \
+    if (_s != IMSRG_OK) return _s; \
+  } while (0)

@@ -1,0 +1,228 @@
+// kernels_ops.cu -- operator arithmetic, norms, mbpt2, the White generator and
+// the packed-layout conversions, all on the basis stream.
+//
+// Reference routines (n-parzuchowski/EOM-IMSRG_FULL, im-SRG/):
+//   add_sq_op        basic_IMSRG.f90:3450-3478
+//   mat_frob_norm    basic_IMSRG.f90:3921-3952
+//   mbpt2            basic_IMSRG.f90:4030-4064
+//   build_gs_white   generators.f90:4-106 (twobody_monopole basic_IMSRG.f90:2031-2046)
+//   vectorize        basic_IMSRG.f90:3794-3854, repackage :3857-3918
+// Reductions use fixed-order partial sums (no atomics): results are
+// bit-reproducible.
+#include "device.cuh"
+
+namespace imsrg {
+
+namespace {
+
+__global__ void k_axpby(const double *__restrict__ A, double ax, const double *__restrict__ B, double bx,
+                        double *__restrict__ C, long n) {
+  long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  long stride = (long)gridDim.x * blockDim.x;
+  for (; i < n; i += stride) C[i] = A[i] * ax + B[i] * bx;
+}
+
+__device__ double block_sum_ops(double v, double *sh) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  if (lane == 0) sh[w] = v;
+  __syncthreads();
+  double r = 0.0;
+  if (threadIdx.x < 32) {
+    r = (lane < (int)(blockDim.x >> 5)) ? sh[lane] : 0.0;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) r += __shfl_xor_sync(0xffffffffu, r, o);
+  }
+  __syncthreads();
+  return r;
+}
+
+// sum of squares of one chunk, times its weight
+__global__ void __launch_bounds__(256) k_norm_partial(const double *__restrict__ op, const NormChunk *chunks,
+                                                      double *partials) {
+  __shared__ double sh[32];
+  NormChunk c = chunks[blockIdx.x];
+  double s = 0.0;
+  for (int i = threadIdx.x; i < c.len; i += blockDim.x) {
+    double x = op[c.start + i];
+    s = fma(x, x, s);
+  }
+  s = block_sum_ops(s, sh);
+  if (threadIdx.x == 0) partials[blockIdx.x] = s * c.weight;
+}
+
+__global__ void __launch_bounds__(256) k_final_sum(const double *partials, int n, double *out, int take_sqrt) {
+  __shared__ double sh[32];
+  double s = 0.0;
+  for (int i = threadIdx.x; i < n; i += blockDim.x) s += partials[i];
+  s = block_sum_ops(s, sh);
+  if (threadIdx.x == 0) *out = take_sqrt ? sqrt(s) : s;
+}
+
+// mbpt2: one CTA per block q; partial = (2J+1) * sum Gamma_pphh^2 / eden
+__global__ void __launch_bounds__(256) k_mbpt2_partial(DevTables T, const double *__restrict__ H, int herm,
+                                                       double *partials) {
+  __shared__ double sh[32];
+  int q = blockIdx.x;
+  int np = T.gam_n1[q * 6 + 2], nh = T.gam_n2[q * 6 + 2];
+  long o = T.gam_off[q * 6 + 2];
+  const int *qp = T.qn + T.qn_start[q * 3 + 0];
+  const int *qh = T.qn + T.qn_start[q * 3 + 2];
+  double s = 0.0;
+  for (int k = threadIdx.x; k < np * nh; k += blockDim.x) {
+    int II = k % np, JJ = k / np;
+    int i = qp[2 * II], j = qp[2 * II + 1], kk = qh[2 * JJ], l = qh[2 * JJ + 1];
+    double fi = f_elem(T, H, herm, i, i), fj = f_elem(T, H, herm, j, j);
+    double fk = f_elem(T, H, herm, kk, kk), fl = f_elem(T, H, herm, l, l);
+    double eden = fk + fl - fi - fj;
+    double x = H[o + k];
+    s += x * x / eden;
+  }
+  s = block_sum_ops(s, sh);
+  if (threadIdx.x == 0) partials[q] = (T.blk_J2[q] + 1.0) * s;
+}
+
+// twobody_monopole(a, b) for every ordered orbit pair
+__global__ void k_monopole(DevTables T, const double *__restrict__ H, int herm, double *mono) {
+  int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= T.norb * T.norb) return;
+  int a = t / T.norb, b = t % T.norb;
+  int ja = T.orb[a].x, jb = T.orb[b].x;
+  double sm = 0.0;
+  for (int JT = abs(ja - jb); JT <= ja + jb; JT += 2) sm += (JT + 1) * v_elem(T, H, herm, a, b, a, b, JT);
+  mono[t] = sm / (ja + 1.0) / (jb + 1.0);
+}
+
+// ETA one-body (fph) and two-body (pphh) elements; everything else was zeroed.
+__global__ void __launch_bounds__(256) k_white(DevTables T, const double *__restrict__ H, int herm,
+                                               const double *__restrict__ mono, double *ETA) {
+  long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  long nph1 = (long)T.P * T.A;
+  if (t < nph1) {
+    int a = (int)(t % T.P), i = (int)(t / T.P);
+    int ak = T.part_orb[a], ik = T.hole_orb[i];
+    int4 oa = T.orb[ak], oi = T.orb[ik];
+    double v = 0.0;
+    if (oa.x == oi.x && oa.y == oi.y && oa.z == oi.z) {
+      int ji = oi.x;
+      double Eden = 0.0;
+      for (int JT = 0; JT <= 2 * ji; JT += 2) Eden = Eden - (JT + 1) * v_elem(T, H, herm, ak, ik, ak, ik, JT);
+      Eden = Eden / (ji + 1.0) / (ji + 1.0);
+      Eden = Eden + H[T.off_fpp + a + (long)a * T.P] - H[T.off_fhh + i + (long)i * T.A];
+      v = H[T.off_fph + t] / Eden;
+    }
+    ETA[T.off_fph + t] = v;
+    return;
+  }
+  t -= nph1;
+  // two-body: walk the pphh arrays of all blocks
+  for (int q = 0; q < T.nblocks; q++) {
+    int s = q * 6 + 2;
+    long n = (long)T.gam_n1[s] * T.gam_n2[s];
+    if (t >= n) {
+      t -= n;
+      continue;
+    }
+    int np = T.gam_n1[s];
+    int IX = (int)(t % np), JX = (int)(t / np);
+    const int *qp = T.qn + T.qn_start[q * 3 + 0] + 2 * IX;
+    const int *qh = T.qn + T.qn_start[q * 3 + 2] + 2 * JX;
+    int a = qp[0], b = qp[1], i = qh[0], j = qh[1];
+    int N = T.norb;
+    double Eden = 0.0;
+    Eden = Eden + mono[a * N + b];
+    Eden = Eden + mono[i * N + j];
+    Eden = Eden - mono[a * N + i];
+    Eden = Eden - mono[a * N + j];
+    Eden = Eden - mono[i * N + b];
+    Eden = Eden - mono[j * N + b];
+    Eden = Eden + f_elem(T, H, herm, a, a) + f_elem(T, H, herm, b, b) - f_elem(T, H, herm, i, i) -
+           f_elem(T, H, herm, j, j);
+    long e = T.gam_off[s] + t;
+    ETA[e] = H[e] / Eden;
+    return;
+  }
+}
+
+__global__ void k_pack(const double *__restrict__ flat, const long *__restrict__ src, double *packed, long n) {
+  long k = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (k < n) packed[k] = flat[src[k]];
+}
+
+__global__ void k_unpack(const double *__restrict__ packed, const long *__restrict__ src,
+                         const long *__restrict__ mirror, int herm, double *flat, long n) {
+  long k = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= n) return;
+  double v = packed[k];
+  flat[src[k]] = v;
+  if (mirror[k] >= 0) flat[mirror[k]] = v * herm;
+}
+
+__global__ void k_check_finite(const double *__restrict__ op, long n, int *flag) {
+  long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  long stride = (long)gridDim.x * blockDim.x;
+  int bad = 0;
+  for (; i < n; i += stride)
+    if (!isfinite(op[i])) bad = 1;
+  if (__syncthreads_or(bad) && threadIdx.x == 0) *flag = 1;
+}
+
+}  // namespace
+
+int launch_axpby(imsrg_basis *b, const double *A, double ax, const double *B, double bx, double *C) {
+  long n = b->nfull;
+  int grid = (int)std::min<long>((n + 255) / 256, 152 * 8);
+  k_axpby<<<grid, 256, 0, b->stream>>>(A, ax, B, bx, C, n);
+  b->launches++;
+  return cuda_status(cudaGetLastError());
+}
+
+int launch_norm(imsrg_basis *b, const double *op, double *d_out) {
+  k_norm_partial<<<b->nchunks, 256, 0, b->stream>>>(op, b->d_chunks, b->partials);
+  k_final_sum<<<1, 256, 0, b->stream>>>(b->partials, b->nchunks, d_out, 1);
+  b->launches += 2;
+  return cuda_status(cudaGetLastError());
+}
+
+int launch_mbpt2(imsrg_basis *b, const double *H, int herm, double *d_out) {
+  k_mbpt2_partial<<<b->nblocks, 256, 0, b->stream>>>(b->T, H, herm, b->partials);
+  k_final_sum<<<1, 256, 0, b->stream>>>(b->partials, b->nblocks, d_out, 0);
+  b->launches += 2;
+  return cuda_status(cudaGetLastError());
+}
+
+int launch_white(imsrg_basis *b, const double *H, int hH, double *ETA) {
+  double *mono = b->mono;
+  IMSRG_CUDA_TRY(cudaMemsetAsync(ETA + 1, 0, (b->nfull - 1) * sizeof(double), b->stream));
+  int nn = b->norb * b->norb;
+  k_monopole<<<(nn + 127) / 128, 128, 0, b->stream>>>(b->T, H, hH, mono);
+  long n3 = 0;
+  for (int q = 0; q < b->nblocks; q++) n3 += (long)b->gam_n1[q * 6 + 2] * b->gam_n2[q * 6 + 2];
+  long n = (long)b->P * b->A + n3;
+  if (n > 0) k_white<<<(unsigned)((n + 255) / 256), 256, 0, b->stream>>>(b->T, H, hH, mono, ETA);
+  b->launches += 2;
+  return cuda_status(cudaGetLastError());
+}
+
+int launch_pack(imsrg_basis *b, const double *flat, double *packed) {
+  k_pack<<<(unsigned)((b->neq + 255) / 256), 256, 0, b->stream>>>(flat, b->d_pack_src, packed, b->neq);
+  b->launches++;
+  return cuda_status(cudaGetLastError());
+}
+
+int launch_unpack(imsrg_basis *b, const double *packed, int herm, double *flat) {
+  k_unpack<<<(unsigned)((b->neq + 255) / 256), 256, 0, b->stream>>>(packed, b->d_pack_src, b->d_pack_mirror, herm,
+                                                                      flat, b->neq);
+  b->launches++;
+  return cuda_status(cudaGetLastError());
+}
+
+int launch_check_finite(imsrg_basis *b, const double *op, int *d_flag) {
+  IMSRG_CUDA_TRY(cudaMemsetAsync(d_flag, 0, sizeof(int), b->stream));
+  k_check_finite<<<152 * 4, 256, 0, b->stream>>>(op, b->nfull, d_flag);
+  b->launches++;
+  return cuda_status(cudaGetLastError());
+}
+
+}  // namespace imsrg

@@ -1,0 +1,307 @@
+"""Python mirror of the reference operator interface over libimsrg_gpu.so.
+
+Names follow the Fortran routines they replace (n-parzuchowski/EOM-IMSRG_FULL,
+im-SRG/): ``commutator`` is the 110..222_ph sequence of IMSRG_MAGNUS.f90:207-219,
+``build_gs_white`` generators.f90:4, ``magnus_expand`` / ``bch_expand`` /
+``euler_step`` / ``magnus_decouple`` IMSRG_MAGNUS.f90:622 / :149 / :756 / :15,
+``add_sq_op`` / ``copy_sq_op`` / ``clear_sq_op`` / ``mat_frob_norm`` /
+``mbpt2`` basic_IMSRG.f90:3450 / :2942 / :3537 / :3921 / :4030.
+
+Every call goes through the C ABI of include/imsrg_gpu.h; a failing status
+raises ImsrgError (the reference STOPs instead).  There is no CPU fallback:
+a missing library or device raises.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libimsrg_gpu.so")
+
+PREC = {"fp64": 0, "ozaki": 1}
+
+SYMBOLS = (
+    "imsrg_gpu_basis_create", "imsrg_gpu_basis_destroy", "imsrg_gpu_basis_info", "imsrg_gpu_block_dims",
+    "imsrg_gpu_synchronize", "imsrg_gpu_op_create", "imsrg_gpu_op_destroy", "imsrg_gpu_op_set_herm",
+    "imsrg_gpu_op_get_herm", "imsrg_gpu_op_upload", "imsrg_gpu_op_download", "imsrg_gpu_op_upload_flat",
+    "imsrg_gpu_op_download_flat", "imsrg_gpu_op_upload_packed", "imsrg_gpu_op_download_packed",
+    "imsrg_gpu_op_device_ptr", "imsrg_gpu_op_copy", "imsrg_gpu_op_clear", "imsrg_gpu_op_add",
+    "imsrg_gpu_op_norm", "imsrg_gpu_op_mbpt2", "imsrg_gpu_op_get_e0", "imsrg_gpu_commutator",
+    "imsrg_gpu_build_gs_white", "imsrg_gpu_magnus_expand", "imsrg_gpu_bch_expand", "imsrg_gpu_euler_step",
+    "imsrg_gpu_magnus_decouple", "imsrg_gpu_strerror", "imsrg_gpu_launch_count",
+)
+
+
+class ImsrgError(RuntimeError):
+    def __init__(self, status: int, where: str):
+        self.status = status
+        super().__init__(f"{where}: {strerror(status)} (status {status})")
+
+
+class BasisInfo(C.Structure):
+    _fields_ = [("norb", C.c_int), ("nholes", C.c_int), ("nparts", C.c_int), ("nblocks", C.c_int),
+                ("jtotal_max", C.c_int), ("ccblocks", C.c_int), ("nfull", C.c_long), ("neq", C.c_long),
+                ("cc_total", C.c_long), ("wcc_total", C.c_long)]
+
+
+_lib = None
+
+
+def lib():
+    """Load the CUDA library (raises if it was not built)."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise RuntimeError(f"{LIB_PATH} is missing: run __graft_entry__.build() first")
+        L = C.CDLL(LIB_PATH)
+        vp, dp, ip, i, d = C.c_void_p, C.POINTER(C.c_double), C.POINTER(C.c_int), C.c_int, C.c_double
+        sig = {
+            "imsrg_gpu_basis_create": [i, ip, ip, ip, ip, ip, C.POINTER(vp)],
+            "imsrg_gpu_basis_destroy": [vp],
+            "imsrg_gpu_basis_info": [vp, C.POINTER(BasisInfo)],
+            "imsrg_gpu_block_dims": [vp, i, ip, ip, ip],
+            "imsrg_gpu_synchronize": [vp],
+            "imsrg_gpu_op_create": [vp, i, C.POINTER(vp)],
+            "imsrg_gpu_op_destroy": [vp],
+            "imsrg_gpu_op_set_herm": [vp, i],
+            "imsrg_gpu_op_get_herm": [vp, ip],
+            "imsrg_gpu_op_upload": [vp, d, dp, dp, dp, C.POINTER(dp)],
+            "imsrg_gpu_op_download": [vp, dp, dp, dp, dp, C.POINTER(dp)],
+            "imsrg_gpu_op_upload_flat": [vp, dp],
+            "imsrg_gpu_op_download_flat": [vp, dp],
+            "imsrg_gpu_op_upload_packed": [vp, dp],
+            "imsrg_gpu_op_download_packed": [vp, dp],
+            "imsrg_gpu_op_device_ptr": [vp, C.POINTER(vp)],
+            "imsrg_gpu_op_copy": [vp, vp],
+            "imsrg_gpu_op_clear": [vp],
+            "imsrg_gpu_op_add": [vp, d, vp, d, vp],
+            "imsrg_gpu_op_norm": [vp, dp],
+            "imsrg_gpu_op_mbpt2": [vp, dp],
+            "imsrg_gpu_op_get_e0": [vp, dp],
+            "imsrg_gpu_commutator": [vp, vp, vp, i, i],
+            "imsrg_gpu_build_gs_white": [vp, vp],
+            "imsrg_gpu_magnus_expand": [vp, vp, i, ip],
+            "imsrg_gpu_bch_expand": [vp, vp, vp, i, ip],
+            "imsrg_gpu_euler_step": [vp, vp, dp, d],
+            "imsrg_gpu_magnus_decouple": [vp, vp, d, d, i, i, dp, ip, ip],
+            "imsrg_gpu_launch_count": [vp, C.POINTER(C.c_long)],
+        }
+        for name, args in sig.items():
+            f = getattr(L, name)
+            f.argtypes = args
+            f.restype = C.c_int
+        L.imsrg_gpu_strerror.argtypes = [C.c_int]
+        L.imsrg_gpu_strerror.restype = C.c_char_p
+        _lib = L
+    return _lib
+
+
+def strerror(status: int) -> str:
+    return lib().imsrg_gpu_strerror(status).decode()
+
+
+def _check(status: int, where: str):
+    if status != 0:
+        raise ImsrgError(status, where)
+
+
+def _dp(a: np.ndarray):
+    assert a.dtype == np.float64 and a.flags["C_CONTIGUOUS"]
+    return a.ctypes.data_as(C.POINTER(C.c_double))
+
+
+class Basis:
+    """Device basis tables (imsrg_gpu_basis_create)."""
+
+    def __init__(self, nn, ll, jj, itzp, con):
+        arrs = [np.ascontiguousarray(x, np.int32) for x in (nn, ll, jj, itzp, con)]
+        self._h = C.c_void_p()
+        _check(lib().imsrg_gpu_basis_create(len(arrs[2]), *[a.ctypes.data_as(C.POINTER(C.c_int)) for a in arrs],
+                                            C.byref(self._h)), "basis_create")
+        info = BasisInfo()
+        _check(lib().imsrg_gpu_basis_info(self._h, C.byref(info)), "basis_info")
+        self.info = info
+        self.nfull = info.nfull
+        self.neq = info.neq
+
+    @classmethod
+    def from_dict(cls, d):
+        return cls(d["nn"], d["ll"], d["jj"], d["itzp"], d["con"])
+
+    @property
+    def handle(self):
+        return self._h
+
+    def synchronize(self):
+        _check(lib().imsrg_gpu_synchronize(self._h), "synchronize")
+
+    def launch_count(self) -> int:
+        n = C.c_long(0)
+        _check(lib().imsrg_gpu_launch_count(self._h, C.byref(n)), "launch_count")
+        return n.value
+
+    def block_dims(self, q):
+        a, b, c = C.c_int(), C.c_int(), C.c_int()
+        _check(lib().imsrg_gpu_block_dims(self._h, q, C.byref(a), C.byref(b), C.byref(c)), "block_dims")
+        return a.value, b.value, c.value
+
+    def close(self):
+        if self._h:
+            lib().imsrg_gpu_basis_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Operator:
+    """A scalar operator resident in HBM (sq_op)."""
+
+    def __init__(self, basis: Basis, herm: int = 1, flat: np.ndarray | None = None):
+        self.basis = basis
+        self._h = C.c_void_p()
+        _check(lib().imsrg_gpu_op_create(basis.handle, herm, C.byref(self._h)), "op_create")
+        if flat is not None:
+            self.upload(flat)
+
+    @property
+    def handle(self):
+        return self._h
+
+    @property
+    def herm(self) -> int:
+        h = C.c_int()
+        _check(lib().imsrg_gpu_op_get_herm(self._h, C.byref(h)), "op_get_herm")
+        return h.value
+
+    @herm.setter
+    def herm(self, v: int):
+        _check(lib().imsrg_gpu_op_set_herm(self._h, int(v)), "op_set_herm")
+
+    def upload(self, flat: np.ndarray):
+        flat = np.ascontiguousarray(flat, np.float64)
+        assert flat.size == self.basis.nfull
+        _check(lib().imsrg_gpu_op_upload_flat(self._h, _dp(flat)), "op_upload_flat")
+
+    def download(self) -> np.ndarray:
+        out = np.empty(self.basis.nfull)
+        _check(lib().imsrg_gpu_op_download_flat(self._h, _dp(out)), "op_download_flat")
+        return out
+
+    def upload_packed(self, vec: np.ndarray):
+        vec = np.ascontiguousarray(vec, np.float64)
+        assert vec.size == self.basis.neq
+        _check(lib().imsrg_gpu_op_upload_packed(self._h, _dp(vec)), "op_upload_packed")
+
+    def download_packed(self) -> np.ndarray:
+        out = np.empty(self.basis.neq)
+        _check(lib().imsrg_gpu_op_download_packed(self._h, _dp(out)), "op_download_packed")
+        return out
+
+    def upload_arrays(self, e0, fhh, fph, fpp, gams):
+        """Fortran sq_op style: gams[(q-1)*6 + g-1] is gam(g) of block q (column-major)."""
+        keep = [np.asfortranarray(x, np.float64) for x in (fhh, fph, fpp)]
+        gk = [np.asfortranarray(g, np.float64) for g in gams]
+        ptrs = (C.POINTER(C.c_double) * len(gk))(*[g.ctypes.data_as(C.POINTER(C.c_double)) for g in gk])
+        _check(lib().imsrg_gpu_op_upload(self._h, float(e0), *[k.ctypes.data_as(C.POINTER(C.c_double)) for k in keep],
+                                         ptrs), "op_upload")
+
+    def download_arrays(self, shapes):
+        """Inverse of upload_arrays; shapes = (fhh, fph, fpp, [gam shapes])."""
+        fhh, fph, fpp = [np.zeros(s, order="F") for s in shapes[:3]]
+        gk = [np.zeros(s, order="F") for s in shapes[3]]
+        ptrs = (C.POINTER(C.c_double) * len(gk))(*[g.ctypes.data_as(C.POINTER(C.c_double)) for g in gk])
+        e0 = C.c_double()
+        _check(lib().imsrg_gpu_op_download(self._h, C.byref(e0), *[k.ctypes.data_as(C.POINTER(C.c_double))
+                                                                  for k in (fhh, fph, fpp)], ptrs), "op_download")
+        return e0.value, fhh, fph, fpp, gk
+
+    def device_ptr(self) -> int:
+        p = C.c_void_p()
+        _check(lib().imsrg_gpu_op_device_ptr(self._h, C.byref(p)), "op_device_ptr")
+        return p.value
+
+    def e0(self) -> float:
+        v = C.c_double()
+        _check(lib().imsrg_gpu_op_get_e0(self._h, C.byref(v)), "op_get_e0")
+        return v.value
+
+    def close(self):
+        if self._h:
+            lib().imsrg_gpu_op_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+# --- reference-named operations -------------------------------------------
+def copy_sq_op(src: Operator, dst: Operator):
+    _check(lib().imsrg_gpu_op_copy(src.handle, dst.handle), "op_copy")
+
+
+def clear_sq_op(op: Operator):
+    _check(lib().imsrg_gpu_op_clear(op.handle), "op_clear")
+
+
+def add_sq_op(A: Operator, ax: float, B: Operator, bx: float, C_: Operator):
+    _check(lib().imsrg_gpu_op_add(A.handle, float(ax), B.handle, float(bx), C_.handle), "op_add")
+
+
+def mat_frob_norm(op: Operator) -> float:
+    v = C.c_double()
+    _check(lib().imsrg_gpu_op_norm(op.handle, C.byref(v)), "op_norm")
+    return v.value
+
+
+def mbpt2(H: Operator) -> float:
+    v = C.c_double()
+    _check(lib().imsrg_gpu_op_mbpt2(H.handle, C.byref(v)), "op_mbpt2")
+    return v.value
+
+
+def commutator(L: Operator, R: Operator, RES: Operator, precision: str = "fp64", with_e0: bool = True):
+    """[L, R] -> RES (RES herm = -herm(L) herm(R)); asynchronous on the basis stream."""
+    _check(lib().imsrg_gpu_commutator(L.handle, R.handle, RES.handle, PREC[precision], int(with_e0)), "commutator")
+
+
+def build_gs_white(H: Operator, ETA: Operator):
+    _check(lib().imsrg_gpu_build_gs_white(H.handle, ETA.handle), "build_gs_white")
+
+
+def magnus_expand(DG: Operator, G: Operator, precision: str = "fp64") -> int:
+    n = C.c_int(0)
+    _check(lib().imsrg_gpu_magnus_expand(DG.handle, G.handle, PREC[precision], C.byref(n)), "magnus_expand")
+    return n.value
+
+
+def bch_expand(HS: Operator, G: Operator, H: Operator, precision: str = "fp64") -> int:
+    n = C.c_int(0)
+    _check(lib().imsrg_gpu_bch_expand(HS.handle, G.handle, H.handle, PREC[precision], C.byref(n)), "bch_expand")
+    return n.value
+
+
+def euler_step(G: Operator, DG: Operator, s: float, ds: float) -> float:
+    sv = C.c_double(s)
+    _check(lib().imsrg_gpu_euler_step(G.handle, DG.handle, C.byref(sv), float(ds)), "euler_step")
+    return sv.value
+
+
+def magnus_decouple(HS: Operator, G: Operator, s_max: float = 50.0, ds: float = 0.5, max_steps: int = 1000,
+                    precision: str = "fp64"):
+    trace = np.zeros(5 * (max_steps + 1))
+    steps, nc = C.c_int(0), C.c_int(0)
+    _check(lib().imsrg_gpu_magnus_decouple(HS.handle, G.handle, float(s_max), float(ds), int(max_steps),
+                                           PREC[precision], _dp(trace), C.byref(steps), C.byref(nc)),
+           "magnus_decouple")
+    n = steps.value + 1
+    return dict(steps=steps.value, ncomm=nc.value, trace=trace[:5 * n].reshape(n, 5))

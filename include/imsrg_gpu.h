@@ -1,0 +1,165 @@
+/*
+ * imsrg_gpu.h -- C ABI of the GB300 IMSRG(2) commutator engine.
+ *
+ * Drop-in boundary for the scalar-operator hot path of
+ * n-parzuchowski/EOM-IMSRG_FULL (paths below are relative to im-SRG/).  Each
+ * entry point names the Fortran routine it replaces.  A Fortran caller binds
+ * these with ISO_C_BINDING interfaces (bind(C, name=...), integer(c_int),
+ * value), in the style the reference already uses for zlib in gzipmod.f90:5-39.
+ *
+ * Conventions
+ *  - Every function returns an int status: IMSRG_OK (0) or an IMSRG_ERR_*
+ *    code.  Nothing aborts or exits the calling process.
+ *  - Orbit arrays are 0-based C arrays of length norb holding the values of
+ *    the reference's jbas%nn, %ll, %jj (= 2j), %itzp (= 2tz), %con (1 hole,
+ *    0 particle), in the reference orbit order.
+ *  - Matrices are Fortran column-major, exactly as the reference allocates
+ *    them in allocate_blocks (basic_IMSRG.f90:477-641): per (2J,Tz,parity)
+ *    block q = 3*2J + 2*(Tz+1) + parity + 1 the six arrays gam(1..6) =
+ *    pppp (npp,npp), ppph (npp,nph), pphh (npp,nhh), phph (nph,nph),
+ *    hhhh (nhh,nhh), phhh (nph,nhh), with rows/columns in the pair order of
+ *    the block's qn lists.  One-body: fhh (A,A), fph (P,A), fpp (P,P).
+ *  - The "flat" layout used by the *_flat calls is
+ *        [E0 | fhh | fph | fpp | q=1..nblocks: gam(1..6)]
+ *    with no padding (imsrg_basis_info_t::nfull doubles).
+ *  - The "packed" layout is the reference's vectorize order
+ *    (basic_IMSRG.f90:3794-3918, length neq), the format of its operator
+ *    checkpoints.
+ *  - All device work of one basis runs, in order, on that basis's CUDA
+ *    stream.  Calls that return host values synchronise that stream.  A basis
+ *    and its operators must be used from one host thread at a time.
+ *  - The library keeps no global mutable state apart from these handles (the
+ *    reference's v_elem/v_same COMMON cache, basic_IMSRG.f90:1282, is not
+ *    mirrored).
+ */
+#ifndef IMSRG_GPU_H
+#define IMSRG_GPU_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+enum {
+  IMSRG_OK = 0,
+  IMSRG_ERR_INVALID = 1,        /* bad argument, shape or handle */
+  IMSRG_ERR_CUDA = 2,           /* CUDA runtime error */
+  IMSRG_ERR_OOM = 3,            /* device allocation failed */
+  IMSRG_ERR_NOT_CONVERGED = 4,  /* BCH series clipped (IMSRG_MAGNUS.f90:232) */
+  IMSRG_ERR_NONFINITE = 5,      /* NaN/Inf detected in a result */
+  IMSRG_ERR_TIMEOUT = 6,        /* a bounded device wait gave up */
+  IMSRG_ERR_MISMATCH = 7,       /* operators of different bases */
+  IMSRG_ERR_NO_DEVICE = 8       /* no usable CUDA device */
+};
+
+/* Arithmetic of the dense two-body contractions (222_pp_hh ladders and the
+ * particle-hole WCC product).  Everything else is always FP64. */
+enum {
+  IMSRG_PREC_FP64 = 0,   /* plain FP64 */
+  IMSRG_PREC_OZAKI = 1   /* FP64 operands split into BF16 slices on tcgen05
+                            tensor cores, exact FP32 slice products,
+                            recombined in FP64 */
+};
+
+typedef struct imsrg_basis imsrg_basis_t;
+typedef struct imsrg_op imsrg_op_t;
+
+typedef struct {
+  int norb, nholes, nparts;
+  int nblocks;       /* (Jtotal_max + 1) * 6 */
+  int jtotal_max;    /* maxval(jj) */
+  int ccblocks;      /* (Jtotal_max + 1) * 4 */
+  long nfull;        /* doubles in the flat layout */
+  long neq;          /* doubles in the packed (vectorize) layout */
+  long cc_total;     /* doubles of one cross-coupled operator (all CCX) */
+  long wcc_total;    /* doubles of the WCC workspace */
+} imsrg_basis_info_t;
+
+/* --- basis (replaces read_sp_basis/find_holes + allocate_blocks +
+ *     allocate_CCMAT + store_6j: basic_IMSRG.f90:152-400, 477-641,
+ *     2183-2288; cross_coupled.f90:61-177) ---------------------------- */
+int imsrg_gpu_basis_create(int norb, const int *nn, const int *ll, const int *jj, const int *itzp,
+                           const int *con, imsrg_basis_t **out);
+int imsrg_gpu_basis_destroy(imsrg_basis_t *b);
+int imsrg_gpu_basis_info(const imsrg_basis_t *b, imsrg_basis_info_t *info);
+/* npp/nph/nhh of block q (1-based), as op%mat(q)%npp etc. */
+int imsrg_gpu_block_dims(const imsrg_basis_t *b, int q, int *npp, int *nph, int *nhh);
+/* Blocks until all queued work of the basis has finished. */
+int imsrg_gpu_synchronize(imsrg_basis_t *b);
+
+/* --- operators (replaces allocate_blocks/duplicate_sq_op storage,
+ *     basic_IMSRG.f90:2736-2918) ------------------------------------- */
+int imsrg_gpu_op_create(imsrg_basis_t *b, int herm, imsrg_op_t **out);
+int imsrg_gpu_op_destroy(imsrg_op_t *op);
+int imsrg_gpu_op_set_herm(imsrg_op_t *op, int herm);
+int imsrg_gpu_op_get_herm(const imsrg_op_t *op, int *herm);
+/* Fortran sq_op arrays: gam[(q-1)*6 + (g-1)] points to op%mat(q)%gam(g)%X. */
+int imsrg_gpu_op_upload(imsrg_op_t *op, double e0, const double *fhh, const double *fph, const double *fpp,
+                        const double *const *gam);
+int imsrg_gpu_op_download(const imsrg_op_t *op, double *e0, double *fhh, double *fph, double *fpp,
+                          double *const *gam);
+int imsrg_gpu_op_upload_flat(imsrg_op_t *op, const double *flat);
+int imsrg_gpu_op_download_flat(const imsrg_op_t *op, double *flat);
+/* vectorize / repackage (basic_IMSRG.f90:3794-3918) */
+int imsrg_gpu_op_upload_packed(imsrg_op_t *op, const double *packed);
+int imsrg_gpu_op_download_packed(const imsrg_op_t *op, double *packed);
+/* Device address of the flat layout (nfull doubles), for callers that keep
+ * their own device buffers in the same layout. */
+int imsrg_gpu_op_device_ptr(imsrg_op_t *op, double **dptr);
+
+/* copy_sq_op (basic_IMSRG.f90:2942-2969): dst = src, herm included */
+int imsrg_gpu_op_copy(const imsrg_op_t *src, imsrg_op_t *dst);
+/* clear_sq_op (basic_IMSRG.f90:3537-3562) */
+int imsrg_gpu_op_clear(imsrg_op_t *op);
+/* add_sq_op (basic_IMSRG.f90:3450-3478): C = ax*A + bx*B (C may alias A/B) */
+int imsrg_gpu_op_add(const imsrg_op_t *A, double ax, const imsrg_op_t *B, double bx, imsrg_op_t *C);
+/* mat_frob_norm (basic_IMSRG.f90:3921-3952) */
+int imsrg_gpu_op_norm(const imsrg_op_t *op, double *out);
+/* mbpt2 (basic_IMSRG.f90:4030-4064) */
+int imsrg_gpu_op_mbpt2(const imsrg_op_t *H, double *out);
+/* E0 of the operator (a device read) */
+int imsrg_gpu_op_get_e0(const imsrg_op_t *op, double *e0);
+
+/* --- commutator engine -------------------------------------------------
+ * [L,R] into RES, which is overwritten; RES herm becomes -herm(L)*herm(R)
+ * (brute_force_testing.f90:509).  Replaces the sequence
+ *   calculate_cross_coupled(L), calculate_cross_coupled(R),
+ *   commutator_110 + commutator_220, commutator_111, commutator_121,
+ *   commutator_122, commutator_222_pp_hh, commutator_221, commutator_222_ph
+ * of IMSRG_MAGNUS.f90:207-219 (commutators.f90:10-925,
+ * cross_coupled.f90:1190-1300).  with_e0 = 0 skips 110/220 and leaves
+ * RES E0 unchanged, as MAGNUS_EXPAND does (IMSRG_MAGNUS.f90:676-685).
+ * RES must not alias L or R. */
+int imsrg_gpu_commutator(const imsrg_op_t *L, const imsrg_op_t *R, imsrg_op_t *RES, int precision, int with_e0);
+
+/* build_gs_white (generators.f90:4-106): ETA (herm -1) from H.  ETA E0 is
+ * left unchanged, as in the reference. */
+int imsrg_gpu_build_gs_white(const imsrg_op_t *H, imsrg_op_t *ETA);
+
+/* --- Magnus flow ------------------------------------------------------- */
+/* MAGNUS_EXPAND (IMSRG_MAGNUS.f90:622-693): DG in = eta, out = dOmega/ds.
+ * *ncomm = commutators evaluated. */
+int imsrg_gpu_magnus_expand(imsrg_op_t *DG, const imsrg_op_t *G, int precision, int *ncomm);
+/* BCH_EXPAND (IMSRG_MAGNUS.f90:149-234): HS = exp(G) H exp(-G).
+ * Returns IMSRG_ERR_NOT_CONVERGED where the reference STOPs ('clipping BCH'). */
+int imsrg_gpu_bch_expand(imsrg_op_t *HS, const imsrg_op_t *G, const imsrg_op_t *H, int precision, int *ncomm);
+/* euler_step (IMSRG_MAGNUS.f90:756-766): G += ds*DG, *s += ds */
+int imsrg_gpu_euler_step(imsrg_op_t *G, const imsrg_op_t *DG, double *s, double ds);
+/* magnus_decouple (IMSRG_MAGNUS.f90:15-128) with build_gs_white and an added
+ * stop at s >= s_max.  HS: in = normal-ordered H, out = H(s).  G: out =
+ * Omega(s).  trace (optional, 5*(max_steps+1) doubles) receives the rows
+ * (step, s, E0, E0 + mbpt2, |mbpt2|) of the reference's _0b_magnus_flow.dat.
+ * *steps = Magnus steps taken, *ncomm = commutators evaluated. */
+int imsrg_gpu_magnus_decouple(imsrg_op_t *HS, imsrg_op_t *G, double s_max, double ds, int max_steps, int precision,
+                              double *trace, int *steps, int *ncomm);
+
+const char *imsrg_gpu_strerror(int status);
+/* Number of library kernel launches issued so far on this basis. */
+int imsrg_gpu_launch_count(const imsrg_basis_t *b, long *count);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* IMSRG_GPU_H */

@@ -9,12 +9,13 @@ from __future__ import annotations
 
 import ctypes as C
 import os
+import platform
 import subprocess
 
 import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-LIB_PATH = os.path.join(HERE, "_build", "liborc.so")
+LIB_PATH = os.path.join(HERE, "_build", platform.machine(), "liborc.so")
 
 _lib = None
 
