@@ -1,0 +1,387 @@
+#!/usr/bin/env python
+"""Benchmark: J-coupled IMSRG(2) [Omega, H] commutators per second at emax = 6.
+
+Workload: one scalar-scalar commutator [Omega, H] (Omega anti-Hermitian,
+H Hermitian) in the 16O harmonic-oscillator basis with emax = 6 (56 j-orbits,
+84 (2J,Tz,parity) blocks, 850,034 two-body doubles per operator), exactly the
+sequence 110+220, 111, 121, 122, 222_pp_hh, 221, 222_ph with both Pandya
+transforms.  Inputs are seeded synthetic operators (see imsrg_gpu.synth).
+A step is one commutator; L2 is flushed (a 256 MiB write) between timed
+steps, because one operator pair plus workspace is smaller than L2.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+
+N > 1 runs N independent replicas (one per GPU, launched by torchrun); the
+commutator of one Hamiltonian does not shard.  Rank 0 prints one JSON line.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+PKG = os.path.join(ROOT, "eom-imsrg_full_gb300")
+for _p in (ROOT, PKG):
+    if _p not in sys.path:
+        sys.path.insert(0, _p)
+
+METRIC = "emax=6 [Ω,H] commutators/s, split-prec vs FP64 GPU at |ΔE0|<1e-6 MeV"
+UNIT = "commutators/s"
+EMAX = 6
+
+
+def _workload_flops(lay):
+    """Algorithmic FLOPs of the dense contractions of one commutator: the
+    twelve ladder products per block of 222_pp_hh plus WCC = LCC RCC^T per
+    cross-coupled block (2mnk each)."""
+    f = 0
+    for b in lay.blocks:
+        np_, nb, nh = b.npp, b.nph, b.nhh
+        f += 2 * (np_ ** 3 + nh ** 3)
+        f += 2 * (nh * nh * np_ + np_ * np_ * nh + 2 * np_ * nh * np_ + 2 * np_ * nh * nh)
+        f += 2 * (nb * nb * nh + 2 * nb * nh * nh + nb * nb * np_ + 2 * np_ * nb * np_)
+        f += 2 * (2 * nb * nh * np_ + 2 * np_ * nb * nh)
+    return f
+
+
+def _cc_flops(orb):
+    """2 * rlen^2 * nph summed over cross-coupled blocks (222_ph product)."""
+    import numpy as np
+    nn, ll, jj, tz, con = (np.asarray(orb[k]) for k in ("nn", "ll", "jj", "itzp", "con"))
+    N = len(jj)
+    jtm = int(jj.max())
+    f = 0
+    for q1 in range(4 * (jtm + 1)):
+        JC = (q1 % (jtm + 1)) * 2
+        PAR = q1 // (2 * jtm + 2)
+        TZ = (q1 % (2 * jtm + 2)) // (jtm + 1)
+        r = nb = 0
+        for i in range(N):
+            for j in range(N):
+                if not (abs(jj[i] - jj[j]) <= JC <= jj[i] + jj[j]):
+                    continue
+                if (ll[i] + ll[j]) % 2 != PAR or abs(tz[i] - tz[j]) // 2 != TZ:
+                    continue
+                r += 1
+                nb += int(con[i] == 0 and con[j] == 1)
+        f += 2 * r * r * nb
+    return f
+
+
+def _compulsory_bytes(lay):
+    """Read L and R, write RES: 3 x nfull doubles."""
+    return 3 * lay.nfull * 8
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except OSError:
+            self.proc = None
+        return self
+
+    def __exit__(self, *exc):
+        self.lines = []
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                out, _ = self.proc.communicate(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+                out, _ = self.proc.communicate()
+            self.lines = [l for l in out.splitlines() if l.strip()]
+        return False
+
+    def summary(self):
+        sm, smax, reasons = [], None, set()
+        names = ("hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap")
+        for l in getattr(self, "lines", []):
+            f = [x.strip() for x in l.split(",")]
+            if len(f) < 8:
+                continue
+            try:
+                sm.append(float(f[0]))
+                smax = float(f[1])
+            except ValueError:
+                continue
+            for n, v in zip(names, f[4:8]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"], "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": smax, "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def dist_setup():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return world, rank, local
+
+
+def cpu_baseline(orb, lay, seconds: float = 12.0, threads: int | None = None):
+    """The oracle (C restatement of the reference CPU path) on host cores."""
+    from oracle import oracle
+    from imsrg_gpu.synth import synth_hamiltonian, synth_omega
+    threads = threads or os.cpu_count()
+    oracle.set_threads(threads)
+    orc = oracle.Oracle(**orb)
+    Hh, Oh = synth_hamiltonian(lay, 1), synth_omega(lay, 1)
+    orc.commutator(Oh, -1, Hh, 1)  # warm
+    n, t0 = 0, time.perf_counter()
+    while True:
+        orc.commutator(Oh, -1, Hh, 1)
+        n += 1
+        dt = time.perf_counter() - t0
+        if dt >= seconds or n >= 400:
+            break
+    return {"value": n / dt, "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": f"{n} emax=6 [Omega,H] commutators in {dt:.1f} s (OpenMP C oracle, own FP64 GEMM)"}
+
+
+def run_reference(args, world, rank):
+    if rank != 0:
+        return 0
+    from imsrg_gpu.layout import Layout, ho_basis
+    from imsrg_gpu.synth import synth_hamiltonian, synth_omega
+    from oracle import oracle
+    orb = ho_basis(EMAX)
+    lay = Layout(**orb)
+    threads = os.cpu_count()
+    oracle.set_threads(threads)
+    orc = oracle.Oracle(**orb)
+    Hh, Oh = synth_hamiltonian(lay, 1), synth_omega(lay, 1)
+    for _ in range(args.warmup):
+        orc.commutator(Oh, -1, Hh, 1)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        orc.commutator(Oh, -1, Hh, 1)
+    dt = time.perf_counter() - t0
+    value = args.steps / dt
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * dt / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": "emax=6 [Omega,H] commutator, 16O, 56 j-orbits", "emax": EMAX},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
+                         "sample": f"{args.steps} commutators after {args.warmup} warm-up (OpenMP C oracle)"},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def run_gpu(args, world, rank, local):
+    import numpy as np
+    import torch
+
+    from imsrg_gpu import api
+    from imsrg_gpu.layout import Layout, ho_basis
+    from imsrg_gpu.synth import synth_hamiltonian, synth_omega
+
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    orb = ho_basis(EMAX)
+    lay = Layout(**orb)
+    B = api.Basis.from_dict(orb)
+    Hh, Oh = synth_hamiltonian(lay, 1 + rank), synth_omega(lay, 1 + rank)
+    O, H, RES = api.Operator(B, -1, Oh), api.Operator(B, 1, Hh), api.Operator(B, 1)
+    RES64 = api.Operator(B, 1)
+    stream = torch.cuda.ExternalStream(B.stream())
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+
+    precision = args.precision
+    if precision == "auto":
+        try:
+            api.commutator(O, H, RES, precision="ozaki")
+            B.synchronize()
+            precision = "ozaki"
+        except api.ImsrgError:
+            precision = "fp64"
+
+    def timed(prec, steps, warmup):
+        for _ in range(warmup):
+            api.commutator(O, H, RES, precision=prec)
+        B.synchronize()
+        B.profile_reset()
+        B.profile(True)
+        launches0 = B.launch_count()
+        total = 0.0
+        with ClockSampler(local) as clk:
+            for _ in range(steps):
+                flush.fill_(1.0)
+                torch.cuda.synchronize()
+                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                e0.record(stream)
+                api.commutator(O, H, RES, precision=prec)
+                e1.record(stream)
+                e1.synchronize()
+                total += e0.elapsed_time(e1)
+        launches = B.launch_count() - launches0
+        prof = B.profile_read()
+        B.profile(False)
+        return total, launches, prof, clk.summary()
+
+    if world > 1:
+        torch.distributed.barrier()
+    total_ms, launches, prof, clocks = timed(precision, args.steps, args.warmup)
+    if world > 1:
+        t = torch.tensor([total_ms], device="cuda", dtype=torch.float64)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        total_ms = float(t.item())
+    value = world * args.steps / (total_ms / 1e3)
+
+    # FP64 path beside the split-precision one, and their difference
+    extra = {}
+    if precision != "fp64":
+        t64, _, prof64, _ = timed("fp64", max(args.steps // 2, 3), 3)
+        extra["fp64_value"] = max(args.steps // 2, 3) / (t64 / 1e3)
+        api.commutator(O, H, RES, precision=precision)
+        api.commutator(O, H, RES64, precision="fp64")
+        a, b_ = RES.download(), RES64.download()
+        extra["split_vs_fp64"] = {"abs_dE0_MeV": abs(float(a[0] - b_[0])),
+                                  "max_rel_elem": float(np.max(np.abs(a - b_)) / np.max(np.abs(b_)))}
+    else:
+        extra["fp64_value"] = value
+
+    # roofline of the dominant kernel (measured live with events on the library stream)
+    kname, (kms, kn) = max(prof.items(), key=lambda kv: kv[1][0])
+    per_launch_s = (kms / 1e3) / max(kn, 1)
+    peaks = {}
+    try:
+        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except (OSError, ValueError):
+        pass
+    if kname in ("gemm_fp64",):
+        work = _workload_flops(lay) + _cc_flops(orb)
+        fp64_peak = _fp64_peak_tflops()
+        roof = {"kernel": kname, "bound": "fp64", "achieved": work / per_launch_s / 1e12, "peak": fp64_peak,
+                "unit": "TFLOP/s", "peak_source": "cuBLAS DGEMM 8192^3 measured in this run (FP64 pipe)"}
+    elif kname.startswith("ozaki_mma"):
+        work = prof_work_ozaki(lay, orb)
+        peak = peaks.get("bf16_tflops", 1951.5)
+        roof = {"kernel": kname, "bound": "tensor", "achieved": work / per_launch_s / 1e12, "peak": peak,
+                "unit": "TFLOP/s", "peak_source": "MEASURED_PEAKS.json bf16_tflops (of measured)"}
+    else:
+        work = _compulsory_bytes(lay)
+        peak = peaks.get("hbm_gbs", 6795.5)
+        roof = {"kernel": kname, "bound": "hbm", "achieved": work / per_launch_s / 1e9, "peak": peak,
+                "unit": "GB/s", "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)"}
+    roof["frac"] = roof["achieved"] / roof["peak"]
+    roof["traffic"] = _traffic_from_profiles(kname)
+    roof["per_launch_us"] = per_launch_s * 1e6
+    roof["kernel_share"] = {k: round(v[0] / max(sum(x[0] for x in prof.values()), 1e-12), 4)
+                            for k, v in prof.items() if v[1]}
+
+    # end to end through the C ABI with pinned host buffers
+    pin_o = torch.empty(lay.nfull, dtype=torch.float64, pin_memory=True).numpy()
+    pin_h = torch.empty(lay.nfull, dtype=torch.float64, pin_memory=True).numpy()
+    pin_r = torch.empty(lay.nfull, dtype=torch.float64, pin_memory=True).numpy()
+    pin_o[:], pin_h[:] = Oh, Hh
+    n_e2e = max(args.steps // 2, 3)
+    for _ in range(2):
+        O.upload(pin_o); H.upload(pin_h); api.commutator(O, H, RES, precision=precision)
+        pin_r[:] = RES.download()
+    B.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(n_e2e):
+        O.upload(pin_o)
+        H.upload(pin_h)
+        api.commutator(O, H, RES, precision=precision)
+        pin_r[:] = RES.download()
+    e2e_dt = time.perf_counter() - t0
+    e2e = {"value": world * n_e2e / e2e_dt, "unit": UNIT, "h2d_bytes_per_step": 2 * lay.nfull * 8,
+           "d2h_bytes_per_step": lay.nfull * 8}
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None,
+            "dtype": "f64" if precision == "fp64" else "bf16-slices/f64",
+            "data": "synthetic (seeded HO basis, hw=20 MeV, N(0,1) MeV two-body, N(0,0.05) Omega)",
+            "config": {"workload": "emax=6 [Omega,H] commutator, 16O, 56 j-orbits", "emax": EMAX,
+                       "precision": precision, "parallelism": f"replicas x{world}",
+                       "l2": "flushed between timed steps (256 MiB write)", "nfull": lay.nfull},
+            "roofline": roof, "e2e": e2e, "gpu_launches": launches, "clocks": clocks,
+        }
+        line.update(extra)
+        if world == 1 and not args.no_cpu_baseline:
+            line["cpu_baseline"] = cpu_baseline(orb, lay, seconds=args.cpu_seconds)
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        torch.distributed.barrier()
+        torch.distributed.destroy_process_group()
+    return 0
+
+
+def prof_work_ozaki(lay, orb):
+    return _workload_flops(lay) + _cc_flops(orb)
+
+
+def _fp64_peak_tflops():
+    import torch
+    n = 8192
+    a = torch.randn(n, n, dtype=torch.float64, device="cuda")
+    b = torch.randn(n, n, dtype=torch.float64, device="cuda")
+    torch.matmul(a, b)
+    torch.cuda.synchronize()
+    best = 1e30
+    for _ in range(3):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        torch.matmul(a, b)
+        e1.record()
+        e1.synchronize()
+        best = min(best, e0.elapsed_time(e1))
+    return 2 * n ** 3 / (best / 1e3) / 1e12
+
+
+def _traffic_from_profiles(kname):
+    """DRAM bytes per launch of a kernel from the committed ncu summary, or None."""
+    try:
+        d = json.load(open(os.path.join(ROOT, "profiles", "dram_traffic.json")))
+        return d.get(kname, {}).get("bytes_per_launch")
+    except (OSError, ValueError):
+        return None
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=50)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--precision", default="auto", choices=["auto", "ozaki", "fp64"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--cpu-seconds", type=float, default=12.0)
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3)
+    world, rank, local = dist_setup()
+    if args.impl == "reference":
+        return run_reference(args, world, rank)
+    return run_gpu(args, world, rank, local)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

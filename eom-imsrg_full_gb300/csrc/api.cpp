@@ -26,6 +26,7 @@ int check_op(const imsrg_op *op) { return (op && op->b && op->d) ? IMSRG_OK : IM
 int read_scalar(imsrg_basis *b, const double *d, double *out) {
   IMSRG_CUDA_TRY(cudaMemcpyAsync(b->h_scal, d, sizeof(double), cudaMemcpyDeviceToHost, b->stream));
   IMSRG_CUDA_TRY(cudaStreamSynchronize(b->stream));
+  IMSRG_TRY(imsrg::ozaki_check_error(b));
   *out = b->h_scal[0];
   return IMSRG_OK;
 }
@@ -60,6 +61,8 @@ namespace imsrg {
 
 int commutator_dev(imsrg_basis *b, const double *L, int hL, const double *R, int hR, double *RES, int hRES,
                    int precision, int with_e0) {
+  if (precision != IMSRG_PREC_FP64 && precision != IMSRG_PREC_OZAKI) return IMSRG_ERR_INVALID;
+  if (precision == IMSRG_PREC_OZAKI) IMSRG_TRY(ozaki_prepare(b));
   IMSRG_TRY(launch_cc_forward(b, L, hL, R, hR));
   if (precision == IMSRG_PREC_FP64) {
     IMSRG_TRY(launch_gemm_fp64(b, L, hL, R, hR));
@@ -163,7 +166,8 @@ int imsrg_gpu_block_dims(const imsrg_basis_t *b, int q, int *npp, int *nph, int 
 
 int imsrg_gpu_synchronize(imsrg_basis_t *b) {
   if (!b) return IMSRG_ERR_INVALID;
-  return cuda_status(cudaStreamSynchronize(b->stream));
+  IMSRG_CUDA_TRY(cudaStreamSynchronize(b->stream));
+  return imsrg::ozaki_check_error(b);
 }
 
 int imsrg_gpu_launch_count(const imsrg_basis_t *b, long *count) {

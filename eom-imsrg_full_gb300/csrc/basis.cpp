@@ -350,7 +350,8 @@ int build_basis(imsrg_basis *b) {
   // --- device copies
   cudaError_t ce = cudaGetDevice(&b->device);
   if (ce != cudaSuccess) return cuda_status(ce);
-  IMSRG_CUDA_TRY(cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking));
+  IMSRG_CUDA_TRY(cudaStreamCreateWithFlags(&b->own_stream, cudaStreamNonBlocking));
+  b->stream = b->own_stream;
   DevTables &T = b->T;
   T.norb = N;
   T.A = A;
@@ -383,6 +384,13 @@ int build_basis(imsrg_basis *b) {
   IMSRG_TRY(dev_upload(b, qn_flat, &T.qn));
   IMSRG_TRY(dev_upload(b, qn_start, &T.qn_start));
   IMSRG_TRY(dev_upload(b, six, &T.six));
+  std::vector<double> six_w(six.size()), sqrt_j21(nJ), jp1(2 * nJ + 2);
+  for (size_t k = 0; k < six.size(); k++) six_w[k] = (double)(2 * (k % nJ) + 1) * six[k];
+  for (int J = 0; J < nJ; J++) sqrt_j21[J] = std::sqrt(2.0 * J + 1.0);
+  for (int J2 = 0; J2 < 2 * nJ + 2; J2++) jp1[J2] = J2 + 1.0;
+  IMSRG_TRY(dev_upload(b, six_w, &T.six_w));
+  IMSRG_TRY(dev_upload(b, sqrt_j21, &T.sqrt_j21));
+  IMSRG_TRY(dev_upload(b, jp1, &T.jp1));
   IMSRG_TRY(dev_upload(b, ljt_start, &T.ljt_start));
   IMSRG_TRY(dev_upload(b, ljt_count, &T.ljt_count));
   IMSRG_TRY(dev_upload(b, ljt_list, &T.ljt_list));
@@ -440,14 +448,15 @@ int build_basis(imsrg_basis *b) {
 
 void free_basis_device(imsrg_basis *b) {
   if (b->stream) cudaStreamSynchronize(b->stream);
+  profile_free(b);
   ozaki_free(b);
   for (void *p : b->dev_allocs) cudaFree(p);
   b->dev_allocs.clear();
   if (b->h_scal) cudaFreeHost(b->h_scal);
   if (b->h_stage) cudaFreeHost(b->h_stage);
   b->h_scal = b->h_stage = nullptr;
-  if (b->stream) cudaStreamDestroy(b->stream);
-  b->stream = nullptr;
+  if (b->own_stream) cudaStreamDestroy(b->own_stream);
+  b->stream = b->own_stream = nullptr;
 }
 
 }  // namespace imsrg

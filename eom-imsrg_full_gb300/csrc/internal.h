@@ -26,6 +26,9 @@ struct DevTables {
   const int *qn;           // pair lists: qn[qn_start[q*3+c] + 2*IX + k], 0-based orbits
   const int *qn_start;     // [q*3+c], c = 0 pp, 1 ph, 2 hh
   const double *six;       // dense 6j table, see sixj_index()
+  const double *six_w;     // (J6 + 1) * 6j, same index
+  const double *sqrt_j21;  // sqrt(J2 + 1) for J2 = 0, 2, .. (index J2/2)
+  const double *jp1;       // (double)(J2 + 1) for J2 = 0 .. 2*nJ (index J2)
   const int *ljt_start;    // [a]: start of orbits sharing (l,j,tz) with a
   const int *ljt_count;    // [a]
   const int *ljt_list;     // concatenated lists (0-based orbits, ascending)
@@ -86,6 +89,21 @@ struct NormChunk {
 
 struct imsrg_op;
 
+namespace imsrg {
+// Live kernel timing with CUDA events on the basis stream.
+struct Profiler {
+  bool on = false;
+  struct Pending {
+    int kind;
+    cudaEvent_t start, stop;
+  };
+  std::vector<cudaEvent_t> pool;
+  std::vector<Pending> pending;
+  double ms[IMSRG_KERNEL_COUNT] = {};
+  long n[IMSRG_KERNEL_COUNT] = {};
+};
+}  // namespace imsrg
+
 struct imsrg_basis {
   // host copies
   int norb, A, P, nblocks, jtm, ccblocks;
@@ -103,8 +121,10 @@ struct imsrg_basis {
   // device
   imsrg::DevTables T{};
   std::vector<void *> dev_allocs;
-  cudaStream_t stream = nullptr;
+  cudaStream_t stream = nullptr;      // where all work is enqueued
+  cudaStream_t own_stream = nullptr;  // the library's own stream
   int device = 0;
+  imsrg::Profiler prof;
   // commutator workspace
   double *w1 = nullptr, *w2 = nullptr, *lcc = nullptr, *rcc = nullptr, *wcc = nullptr;
   double *mono = nullptr;       // norb x norb monopole table of the White generator
@@ -158,8 +178,22 @@ int launch_unpack(imsrg_basis *b, const double *packed, int herm, double *flat);
 int launch_check_finite(imsrg_basis *b, const double *op, int *d_flag);
 
 // Ozaki split-precision contraction engine (ozaki.cu)
+int ozaki_prepare(imsrg_basis *b);  // plans and allocates the engine once; errors if unavailable
 int ozaki_gemm(imsrg_basis *b, const double *L, int hL, const double *R, int hR);
+int ozaki_check_error(imsrg_basis *b);  // IMSRG_ERR_TIMEOUT if a bounded device wait gave up
 void ozaki_free(imsrg_basis *b);
+
+// Records CUDA events around the launches of one kernel class while profiling
+// is enabled (profile.cpp).
+struct ProfScope {
+  imsrg_basis *b;
+  int kind;
+  cudaEvent_t start = nullptr;
+  ProfScope(imsrg_basis *b, int kind);
+  ~ProfScope();
+};
+int profile_collect(imsrg_basis *b);
+void profile_free(imsrg_basis *b);
 
 // one full commutator (api.cpp)
 int commutator_dev(imsrg_basis *b, const double *L, int hL, const double *R, int hR, double *RES, int hRES,

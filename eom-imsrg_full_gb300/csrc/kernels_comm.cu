@@ -63,9 +63,10 @@ __global__ void __launch_bounds__(256) k_cc_forward(DevTables T, const double *L
     int Jmin = max(abs(jp - jb), abs(ja - jh));
     int Jmax = min(jp + jb, ja + jh);
     double sm = 0.0;
+    // sum_J (-1)^J (2J+1) {jp jh J'; ja jb J} V^J_{hapb}: one DFMA per J
     for (int JT = Jmin; JT <= Jmax; JT += 2)
-      sm += m1pow(JT / 2) * (JT + 1) * sixj(T, jp, jh, JC, ja, jb, JT) * v_elem(T, op, herm, h, a, p, b, JT);
-    x = sm * m1pow((jh + jb + JC) / 2) * sqrt(JC + 1.0);
+      sm = fma(dflip(sixj_w(T, jp, jh, JC, ja, jb, JT), JT >> 1), v_elem(T, op, herm, h, a, p, b, JT), sm);
+    x = dflip(sm, (jh + jb + JC) >> 1) * T.sqrt_j21[JC >> 1];
   }
   out[e] = x;
 }
@@ -165,7 +166,9 @@ __global__ void __launch_bounds__(256) k_gemm_fp64(const GemmProb *__restrict__ 
 // ---------------------------------------------------------------------------
 // 3. Two-body assembly.
 // ---------------------------------------------------------------------------
-// One-body insertions of commutator_122 for element <ab|..|cd> at J2.
+// One-body insertions of commutator_122 for element <ab|..|cd> at J2: each
+// term resolves the location once and reads it from R and from L (the
+// reference's v_elem / v_same pair), two DFMAs per term.
 __device__ __forceinline__ double c122(const DevTables &T, const double *L, int hL, const double *R, int hR, int a,
                                        int b, int c, int d, int J2) {
   double sm = 0.0;
@@ -173,30 +176,37 @@ __device__ __forceinline__ double c122(const DevTables &T, const double *L, int 
   for (int k = 0; k < n; k++) {
     int i = T.ljt_list[s + k];
     VLoc vl = v_loc(T, i, b, c, d, J2);
-    sm += f_elem(T, L, hL, a, i) * v_read(R, hR, vl) - f_elem(T, R, hR, a, i) * v_read(L, hL, vl);
+    sm = fma(f_elem(T, L, hL, a, i), v_read(R, hR, vl), sm);
+    sm = fma(-f_elem(T, R, hR, a, i), v_read(L, hL, vl), sm);
   }
   s = T.ljt_start[b];
   n = T.ljt_count[b];
   for (int k = 0; k < n; k++) {
     int i = T.ljt_list[s + k];
     VLoc vl = v_loc(T, a, i, c, d, J2);
-    sm += f_elem(T, L, hL, b, i) * v_read(R, hR, vl) - f_elem(T, R, hR, b, i) * v_read(L, hL, vl);
+    sm = fma(f_elem(T, L, hL, b, i), v_read(R, hR, vl), sm);
+    sm = fma(-f_elem(T, R, hR, b, i), v_read(L, hL, vl), sm);
   }
   s = T.ljt_start[c];
   n = T.ljt_count[c];
   for (int k = 0; k < n; k++) {
     int i = T.ljt_list[s + k];
     VLoc vl = v_loc(T, a, b, i, d, J2);
-    sm += -f_elem(T, L, hL, i, c) * v_read(R, hR, vl) + f_elem(T, R, hR, i, c) * v_read(L, hL, vl);
+    sm = fma(-f_elem(T, L, hL, i, c), v_read(R, hR, vl), sm);
+    sm = fma(f_elem(T, R, hR, i, c), v_read(L, hL, vl), sm);
   }
   s = T.ljt_start[d];
   n = T.ljt_count[d];
   for (int k = 0; k < n; k++) {
     int i = T.ljt_list[s + k];
     VLoc vl = v_loc(T, a, b, c, i, J2);
-    sm += -f_elem(T, L, hL, i, d) * v_read(R, hR, vl) + f_elem(T, R, hR, i, d) * v_read(L, hL, vl);
+    sm = fma(-f_elem(T, L, hL, i, d), v_read(R, hR, vl), sm);
+    sm = fma(f_elem(T, R, hR, i, d), v_read(L, hL, vl), sm);
   }
-  return sm / sqrt(1.0 + (a == b)) / sqrt(1.0 + (c == d));
+  // / sqrt(1 + delta_ab) / sqrt(1 + delta_cd)
+  int nd = (a == b) + (c == d);
+  if (nd) sm = sm * (nd == 1 ? 0.7071067811865476 : 0.5);
+  return sm;
 }
 
 __device__ __forceinline__ double wcc_at(const DevTables &T, const double *W, int qx, int r, int c) {
@@ -208,12 +218,15 @@ __device__ __forceinline__ int cc_r(const DevTables &T, int q1, int i, int j) {
 }
 
 // Inverse Pandya recoupling of commutator_222_ph (commutators.f90:855-910).
-// Returns false where the reference's Tz/parity 'cycle' would skip the update.
+// The +-1 factors (herm, phases) become sign flips of the 6j symbol, leaving
+// four DFMAs per J'.  Returns false where the reference's Tz/parity 'cycle'
+// would skip the update.
 __device__ __forceinline__ bool c222ph(const DevTables &T, const double *W, int hL, int hR, int i, int j, int k,
                                        int l, int Jtot, double *out) {
   int4 oi = T.orb[i], oj = T.orb[j], ok = T.orb[k], ol = T.orb[l];
   int ji = oi.x, jj = oj.x, jk = ok.x, jl = ol.x;
   int JTM = T.jtm;
+  int nL = hL < 0, nR = hR < 0;
   double sm = 0.0;
   int jmin = max(abs(jj - jl), abs(ji - jk));
   int jmax = min(jj + jl, ji + jk);
@@ -221,16 +234,19 @@ __device__ __forceinline__ bool c222ph(const DevTables &T, const double *W, int 
   if (abs(ol.z - oj.z) != Tz * 2) return false;
   int PAR = (oi.y + ok.y) & 1;
   if (((ol.y + oj.y) & 1) != PAR) return false;
-  double phase = m1pow((ji + jj + jk + jl) / 2);
-  double ph2 = m1pow((jl + jk + Jtot) / 2);
+  int nph = ((ji + jj + jk + jl) >> 1) & 1;
+  // 'inside' terms enter with -(-1)^((jl+jk+J)/2)
+  int n2 = (((jl + jk + Jtot) >> 1) + 1) & 1;
   for (int JP = jmin; JP <= jmax; JP += 2) {
     int qx = JP / 2 + Tz * (JTM + 1) + 2 * PAR * (JTM + 1);
     int rjl = cc_r(T, qx, j, l), rik = cc_r(T, qx, i, k);
     int gjl = cc_r(T, qx, l, j), gik = cc_r(T, qx, k, i);
-    sm = sm - ph2 *
-                  ((wcc_at(T, W, qx, gik, rjl) + phase * wcc_at(T, W, qx, gjl, rik)) * hL -
-                   (phase * wcc_at(T, W, qx, rik, gjl) + wcc_at(T, W, qx, rjl, gik)) * hR) *
-                  sixj(T, ji, jj, Jtot, jl, jk, JP);
+    double s6 = sixj(T, ji, jj, Jtot, jl, jk, JP);
+    double c1 = dflip(s6, n2 ^ nL), c4 = dflip(s6, n2 ^ nR ^ 1);
+    sm = fma(c1, wcc_at(T, W, qx, gik, rjl), sm);
+    sm = fma(dflip(c1, nph), wcc_at(T, W, qx, gjl, rik), sm);
+    sm = fma(dflip(c4, nph), wcc_at(T, W, qx, rik, gjl), sm);
+    sm = fma(c4, wcc_at(T, W, qx, rjl, gik), sm);
   }
   Tz = abs(oi.z - ol.z) / 2;
   if (abs(ok.z - oj.z) != Tz * 2) return false;
@@ -242,9 +258,12 @@ __device__ __forceinline__ bool c222ph(const DevTables &T, const double *W, int 
     int qx = JP / 2 + Tz * (JTM + 1) + 2 * PAR * (JTM + 1);
     int ril = cc_r(T, qx, i, l), rjk = cc_r(T, qx, j, k);
     int gil = cc_r(T, qx, l, i), gjk = cc_r(T, qx, k, j);
-    sm = sm + ((wcc_at(T, W, qx, gil, rjk) + phase * wcc_at(T, W, qx, gjk, ril)) * hL -
-               (phase * wcc_at(T, W, qx, ril, gjk) + wcc_at(T, W, qx, rjk, gil)) * hR) *
-                  sixj(T, ji, jj, Jtot, jk, jl, JP);
+    double s6 = sixj(T, ji, jj, Jtot, jk, jl, JP);
+    double c1 = dflip(s6, nL), c4 = dflip(s6, nR ^ 1);
+    sm = fma(c1, wcc_at(T, W, qx, gil, rjk), sm);
+    sm = fma(dflip(c1, nph), wcc_at(T, W, qx, gjk, ril), sm);
+    sm = fma(dflip(c4, nph), wcc_at(T, W, qx, ril, gjk), sm);
+    sm = fma(c4, wcc_at(T, W, qx, rjk, gil), sm);
   }
   *out = sm;
   return true;
@@ -268,25 +287,26 @@ __global__ void __launch_bounds__(256) k_assemble_2body(DevTables T, const doubl
   const int *qc = T.qn + T.qn_start[q * 3 + c2tab[g]] + 2 * JX;
   int a = qr[0], b = qr[1], c = qc[0], d = qc[1];
   int J2 = T.blk_J2[q];
-  int pm = hL * hR;
+  int nres = hRES < 0, npm = (hL * hR) < 0;
   double t = c122(T, L, hL, R, hR, a, b, c, d, J2);
   long em = T.gam_off[s] + JX + (long)IX * n1;  // mirror (JX, IX) of a square array
   bool diag = square && IX == JX;
-  if (diag) t = t * hRES;
+  if (diag) t = dflip(t, nres);
   t = t + W1[e];
   t = t - W2[e];
-  if (square) t = t - (W1[em] - W2[em]) * pm;
+  if (square) t = t - dflip(W1[em] - W2[em], npm);
   double sm;
   if (c222ph(T, WCC, hL, hR, a, b, c, d, J2, &sm)) {
-    double pre = (a == b) ? .70710678118 : 1.0;
-    double pre2 = (c == d) ? .70710678118 : 1.0;
-    t = t + sm * pre * pre2;
+    // the reference's truncated 1/sqrt(2) literal for identical orbits
+    int nd = (a == b) + (c == d);
+    if (nd) sm = sm * (nd == 1 ? .70710678118 : .70710678118 * .70710678118);
+    t = t + sm;
   }
   if (diag) {
-    RES[e] = t * hRES;
+    RES[e] = dflip(t, nres);
   } else {
     RES[e] = t;
-    if (square) RES[em] = t * hRES;
+    if (square) RES[em] = dflip(t, nres);
   }
 }
 
@@ -457,6 +477,7 @@ __global__ void __launch_bounds__(256) k_assemble_1body(DevTables T, const doubl
 int launch_cc_forward(imsrg_basis *b, const double *L, int hL, const double *R, int hR) {
   long n = 2 * b->cc_total;
   if (n == 0) return IMSRG_OK;
+  ProfScope ps(b, IMSRG_KERNEL_CC_FORWARD);
   k_cc_forward<<<(unsigned)((n + 255) / 256), 256, 0, b->stream>>>(b->T, L, hL, R, hR, b->lcc, b->rcc);
   b->launches++;
   return cuda_status(cudaGetLastError());
@@ -475,6 +496,7 @@ int launch_gemm_fp64(imsrg_basis *b, const double *L, int hL, const double *R, i
   ops.dst[SRC_W1] = b->w1;
   ops.dst[SRC_W2] = b->w2;
   ops.dst[SRC_WCC] = b->wcc;
+  ProfScope ps(b, IMSRG_KERNEL_GEMM_FP64);
   k_gemm_fp64<<<b->ntiles, 256, 0, b->stream>>>(b->d_probs, b->nprobs, ops, hL, hR);
   b->launches++;
   return cuda_status(cudaGetLastError());
@@ -484,6 +506,7 @@ int launch_assemble_2body(imsrg_basis *b, const double *L, int hL, const double 
   long off2b = b->off_fpp + (long)b->P * b->P;
   long n = b->nfull - off2b;
   if (n <= 0) return IMSRG_OK;
+  ProfScope ps(b, IMSRG_KERNEL_ASSEMBLE_2BODY);
   k_assemble_2body<<<(unsigned)((n + 255) / 256), 256, 0, b->stream>>>(b->T, L, hL, R, hR, b->w1, b->w2, b->wcc, RES,
                                                                       hRES, off2b);
   b->launches++;
@@ -494,6 +517,7 @@ int launch_assemble_1body(imsrg_basis *b, const double *L, int hL, const double 
                           int with_e0) {
   long nel = (long)b->A * b->A + (long)b->P * b->A + (long)b->P * b->P;
   int nblk = (int)((nel + 7) / 8);
+  ProfScope ps(b, IMSRG_KERNEL_ASSEMBLE_1BODY);
   k_assemble_1body<<<nblk + 1, 256, 0, b->stream>>>(b->T, L, hL, R, hR, b->w1, b->w2, RES, hRES, with_e0, nblk);
   b->launches++;
   return cuda_status(cudaGetLastError());

@@ -173,12 +173,14 @@ __global__ void k_check_finite(const double *__restrict__ op, long n, int *flag)
 int launch_axpby(imsrg_basis *b, const double *A, double ax, const double *B, double bx, double *C) {
   long n = b->nfull;
   int grid = (int)std::min<long>((n + 255) / 256, 152 * 8);
+  ProfScope ps(b, IMSRG_KERNEL_OPS);
   k_axpby<<<grid, 256, 0, b->stream>>>(A, ax, B, bx, C, n);
   b->launches++;
   return cuda_status(cudaGetLastError());
 }
 
 int launch_norm(imsrg_basis *b, const double *op, double *d_out) {
+  ProfScope ps(b, IMSRG_KERNEL_OPS);
   k_norm_partial<<<b->nchunks, 256, 0, b->stream>>>(op, b->d_chunks, b->partials);
   k_final_sum<<<1, 256, 0, b->stream>>>(b->partials, b->nchunks, d_out, 1);
   b->launches += 2;
@@ -186,6 +188,7 @@ int launch_norm(imsrg_basis *b, const double *op, double *d_out) {
 }
 
 int launch_mbpt2(imsrg_basis *b, const double *H, int herm, double *d_out) {
+  ProfScope ps(b, IMSRG_KERNEL_OPS);
   k_mbpt2_partial<<<b->nblocks, 256, 0, b->stream>>>(b->T, H, herm, b->partials);
   k_final_sum<<<1, 256, 0, b->stream>>>(b->partials, b->nblocks, d_out, 0);
   b->launches += 2;
@@ -194,6 +197,7 @@ int launch_mbpt2(imsrg_basis *b, const double *H, int herm, double *d_out) {
 
 int launch_white(imsrg_basis *b, const double *H, int hH, double *ETA) {
   double *mono = b->mono;
+  ProfScope ps(b, IMSRG_KERNEL_OPS);
   IMSRG_CUDA_TRY(cudaMemsetAsync(ETA + 1, 0, (b->nfull - 1) * sizeof(double), b->stream));
   int nn = b->norb * b->norb;
   k_monopole<<<(nn + 127) / 128, 128, 0, b->stream>>>(b->T, H, hH, mono);

@@ -32,7 +32,12 @@ SYMBOLS = (
     "imsrg_gpu_op_norm", "imsrg_gpu_op_mbpt2", "imsrg_gpu_op_get_e0", "imsrg_gpu_commutator",
     "imsrg_gpu_build_gs_white", "imsrg_gpu_magnus_expand", "imsrg_gpu_bch_expand", "imsrg_gpu_euler_step",
     "imsrg_gpu_magnus_decouple", "imsrg_gpu_strerror", "imsrg_gpu_launch_count",
+    "imsrg_gpu_basis_get_stream", "imsrg_gpu_basis_set_stream", "imsrg_gpu_profile_enable",
+    "imsrg_gpu_profile_read", "imsrg_gpu_profile_reset",
 )
+
+KERNELS = ("cc_forward", "gemm_fp64", "assemble_2body", "assemble_1body", "ozaki_slice", "ozaki_mma",
+           "ozaki_epilogue", "ops")
 
 
 class ImsrgError(RuntimeError):
@@ -88,6 +93,11 @@ def lib():
             "imsrg_gpu_euler_step": [vp, vp, dp, d],
             "imsrg_gpu_magnus_decouple": [vp, vp, d, d, i, i, dp, ip, ip],
             "imsrg_gpu_launch_count": [vp, C.POINTER(C.c_long)],
+            "imsrg_gpu_basis_get_stream": [vp, C.POINTER(vp)],
+            "imsrg_gpu_basis_set_stream": [vp, vp],
+            "imsrg_gpu_profile_enable": [vp, i],
+            "imsrg_gpu_profile_read": [vp, i, dp, C.POINTER(C.c_long)],
+            "imsrg_gpu_profile_reset": [vp],
         }
         for name, args in sig.items():
             f = getattr(L, name)
@@ -142,6 +152,30 @@ class Basis:
         n = C.c_long(0)
         _check(lib().imsrg_gpu_launch_count(self._h, C.byref(n)), "launch_count")
         return n.value
+
+    def stream(self) -> int:
+        """cudaStream_t (as an int) that all work of this basis runs on."""
+        p = C.c_void_p()
+        _check(lib().imsrg_gpu_basis_get_stream(self._h, C.byref(p)), "basis_get_stream")
+        return p.value or 0
+
+    def set_stream(self, stream: int | None):
+        _check(lib().imsrg_gpu_basis_set_stream(self._h, C.c_void_p(stream or 0)), "basis_set_stream")
+
+    def profile(self, on: bool = True):
+        _check(lib().imsrg_gpu_profile_enable(self._h, int(on)), "profile_enable")
+
+    def profile_reset(self):
+        _check(lib().imsrg_gpu_profile_reset(self._h), "profile_reset")
+
+    def profile_read(self) -> dict:
+        """{kernel: (total_ms, launches)} since the last reset."""
+        out = {}
+        for k, name in enumerate(KERNELS):
+            ms, n = C.c_double(), C.c_long()
+            _check(lib().imsrg_gpu_profile_read(self._h, k, C.byref(ms), C.byref(n)), "profile_read")
+            out[name] = (ms.value, n.value)
+        return out
 
     def block_dims(self, q):
         a, b, c = C.c_int(), C.c_int(), C.c_int()

@@ -158,6 +158,29 @@ const char *imsrg_gpu_strerror(int status);
 /* Number of library kernel launches issued so far on this basis. */
 int imsrg_gpu_launch_count(const imsrg_basis_t *b, long *count);
 
+/* --- streams and instrumentation (no reference counterpart) ------------ */
+/* The cudaStream_t all work of the basis runs on.  set_stream makes the
+ * library enqueue on a caller-owned stream instead (NULL restores its own). */
+int imsrg_gpu_basis_get_stream(imsrg_basis_t *b, void **stream);
+int imsrg_gpu_basis_set_stream(imsrg_basis_t *b, void *stream);
+/* Kernel timing with CUDA events on the basis stream, per kernel class
+ * IMSRG_KERNEL_*.  read returns the summed milliseconds and launch count
+ * since the last reset (it synchronises the stream). */
+enum {
+  IMSRG_KERNEL_CC_FORWARD = 0,
+  IMSRG_KERNEL_GEMM_FP64 = 1,
+  IMSRG_KERNEL_ASSEMBLE_2BODY = 2,
+  IMSRG_KERNEL_ASSEMBLE_1BODY = 3,
+  IMSRG_KERNEL_OZAKI_SLICE = 4,
+  IMSRG_KERNEL_OZAKI_MMA = 5,
+  IMSRG_KERNEL_OZAKI_EPILOGUE = 6,
+  IMSRG_KERNEL_OPS = 7,
+  IMSRG_KERNEL_COUNT = 8
+};
+int imsrg_gpu_profile_enable(imsrg_basis_t *b, int on);
+int imsrg_gpu_profile_read(imsrg_basis_t *b, int kernel, double *ms, long *launches);
+int imsrg_gpu_profile_reset(imsrg_basis_t *b);
+
 #ifdef __cplusplus
 }
 #endif

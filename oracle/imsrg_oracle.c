@@ -519,23 +519,48 @@ static double twobody_monopole(const obasis *b, int a, int bb, int ja, int jb, c
 /* ------------------------------------------------------------------ */
 /* dense FP64 GEMM with BLAS dgemm semantics (column-major)            */
 /* ------------------------------------------------------------------ */
+/* op(A) and op(B) are packed column-major, then each 8-column x 128-row tile
+ * of C is accumulated as rank-1 updates over k (the i loop vectorises without
+ * reassociation). */
+#define GEMM_NB 8
+#define GEMM_MB 128
 static void dgemm_(char ta, char tb, int m, int n, int k, double alpha, const double *A, int lda, const double *B,
                    int ldb, double beta, double *C, int ldc) {
   if (m <= 0 || n <= 0) return;
+  double *Ap = malloc(((long)m * (k > 0 ? k : 1)) * sizeof(double));
+  double *Bp = malloc(((long)k * n + 1) * sizeof(double));
+  for (int l = 0; l < k; l++)
+    for (int i = 0; i < m; i++) Ap[i + (long)l * m] = (ta == 'N') ? A[i + (long)l * lda] : A[l + (long)i * lda];
+  for (int j = 0; j < n; j++)
+    for (int l = 0; l < k; l++) Bp[l + (long)j * k] = (tb == 'N') ? B[l + (long)j * ldb] : B[j + (long)l * ldb];
+  int nj = (n + GEMM_NB - 1) / GEMM_NB, ni = (m + GEMM_MB - 1) / GEMM_MB;
   long work = (long)m * n * (k > 0 ? k : 1);
-#pragma omp parallel for schedule(static) if (work > 200000)
-  for (int j = 0; j < n; j++) {
-    for (int i = 0; i < m; i++) {
-      double s = 0.0;
+#pragma omp parallel for schedule(dynamic) collapse(2) if (work > 200000)
+  for (int jb = 0; jb < nj; jb++)
+    for (int ib = 0; ib < ni; ib++) {
+      double acc[GEMM_NB][GEMM_MB];
+      int j0 = jb * GEMM_NB, i0 = ib * GEMM_MB;
+      int jn = (n - j0 < GEMM_NB) ? n - j0 : GEMM_NB;
+      int in = (m - i0 < GEMM_MB) ? m - i0 : GEMM_MB;
+      for (int jj = 0; jj < GEMM_NB; jj++)
+        for (int i = 0; i < GEMM_MB; i++) acc[jj][i] = 0.0;
       for (int l = 0; l < k; l++) {
-        double av = (ta == 'N') ? A[i + (long)l * lda] : A[l + (long)i * lda];
-        double bv = (tb == 'N') ? B[l + (long)j * ldb] : B[j + (long)l * ldb];
-        s += av * bv;
+        const double *a = Ap + i0 + (long)l * m;
+        for (int jj = 0; jj < jn; jj++) {
+          double bv = Bp[l + (long)(j0 + jj) * k];
+          double *c = acc[jj];
+          for (int i = 0; i < in; i++) c[i] += a[i] * bv;
+        }
       }
-      double cv = (beta == 0.0) ? 0.0 : beta * C[i + (long)j * ldc];
-      C[i + (long)j * ldc] = alpha * s + cv;
+      for (int jj = 0; jj < jn; jj++)
+        for (int i = 0; i < in; i++) {
+          long ci = (i0 + i) + (long)(j0 + jj) * ldc;
+          double cv = (beta == 0.0) ? 0.0 : beta * C[ci];
+          C[ci] = alpha * acc[jj][i] + cv;
+        }
     }
-  }
+  free(Ap);
+  free(Bp);
 }
 
 /* ------------------------------------------------------------------ */
