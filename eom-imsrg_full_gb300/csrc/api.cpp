@@ -91,6 +91,7 @@ const char *imsrg_gpu_strerror(int s) {
     case IMSRG_ERR_TIMEOUT: return "a bounded device wait gave up";
     case IMSRG_ERR_MISMATCH: return "operators belong to different bases";
     case IMSRG_ERR_NO_DEVICE: return "no usable CUDA device";
+    case IMSRG_ERR_TOO_LARGE: return "basis too large for the fixed allocation-free workspace";
     default: return "unknown status";
   }
 }

@@ -177,6 +177,14 @@ int launch_pack(imsrg_basis *b, const double *flat, double *packed);
 int launch_unpack(imsrg_basis *b, const double *packed, int herm, double *flat);
 int launch_check_finite(imsrg_basis *b, const double *op, int *d_flag);
 
+// Intermediates of one commutator: W1, W2 (flat operators), LCC, RCC (all
+// cross-coupled blocks) and WCC.
+struct Workspace {
+  double *w1, *w2, *lcc, *rcc, *wcc;
+};
+int launch_commutator_fp64_ws(imsrg_basis *b, const Workspace &ws, const double *L, int hL, const double *R, int hR,
+                              double *RES, int hRES, int with_e0, cudaStream_t st);
+
 // Ozaki split-precision contraction engine (ozaki.cu)
 int ozaki_prepare(imsrg_basis *b);  // plans and allocates the engine once; errors if unavailable
 int ozaki_gemm(imsrg_basis *b, const double *L, int hL, const double *R, int hR);

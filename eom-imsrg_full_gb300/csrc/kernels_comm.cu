@@ -523,4 +523,43 @@ int launch_assemble_1body(imsrg_basis *b, const double *L, int hL, const double 
   return cuda_status(cudaGetLastError());
 }
 
+// The four FP64 launches of one commutator with caller-chosen workspace and
+// stream; used by the allocation-free entry point (noalloc.cu).  Allocates
+// nothing and records no profiling events.
+int launch_commutator_fp64_ws(imsrg_basis *b, const Workspace &ws, const double *L, int hL, const double *R, int hR,
+                              double *RES, int hRES, int with_e0, cudaStream_t st) {
+  long ncc = 2 * b->cc_total;
+  if (ncc > 0) {
+    k_cc_forward<<<(unsigned)((ncc + 255) / 256), 256, 0, st>>>(b->T, L, hL, R, hR, ws.lcc, ws.rcc);
+    b->launches++;
+  }
+  if (b->ntiles > 0) {
+    Operands ops{};
+    ops.src[SRC_L] = L;
+    ops.src[SRC_R] = R;
+    ops.src[SRC_W1] = ws.w1;
+    ops.src[SRC_W2] = ws.w2;
+    ops.src[SRC_LCC] = ws.lcc;
+    ops.src[SRC_RCC] = ws.rcc;
+    ops.src[SRC_WCC] = ws.wcc;
+    ops.dst[SRC_W1] = ws.w1;
+    ops.dst[SRC_W2] = ws.w2;
+    ops.dst[SRC_WCC] = ws.wcc;
+    k_gemm_fp64<<<b->ntiles, 256, 0, st>>>(b->d_probs, b->nprobs, ops, hL, hR);
+    b->launches++;
+  }
+  long off2b = b->off_fpp + (long)b->P * b->P;
+  long n2 = b->nfull - off2b;
+  if (n2 > 0) {
+    k_assemble_2body<<<(unsigned)((n2 + 255) / 256), 256, 0, st>>>(b->T, L, hL, R, hR, ws.w1, ws.w2, ws.wcc, RES,
+                                                                   hRES, off2b);
+    b->launches++;
+  }
+  long nel = (long)b->A * b->A + (long)b->P * b->A + (long)b->P * b->P;
+  int nblk = (int)((nel + 7) / 8);
+  k_assemble_1body<<<nblk + 1, 256, 0, st>>>(b->T, L, hL, R, hR, ws.w1, ws.w2, RES, hRES, with_e0, nblk);
+  b->launches++;
+  return cuda_status(cudaGetLastError());
+}
+
 }  // namespace imsrg

@@ -33,7 +33,7 @@ SYMBOLS = (
     "imsrg_gpu_build_gs_white", "imsrg_gpu_magnus_expand", "imsrg_gpu_bch_expand", "imsrg_gpu_euler_step",
     "imsrg_gpu_magnus_decouple", "imsrg_gpu_strerror", "imsrg_gpu_launch_count",
     "imsrg_gpu_basis_get_stream", "imsrg_gpu_basis_set_stream", "imsrg_gpu_profile_enable",
-    "imsrg_gpu_profile_read", "imsrg_gpu_profile_reset",
+    "imsrg_gpu_profile_read", "imsrg_gpu_profile_reset", "imsrg_gpu_commutator_noalloc",
 )
 
 KERNELS = ("cc_forward", "gemm_fp64", "assemble_2body", "assemble_1body", "ozaki_slice", "ozaki_mma",
@@ -98,6 +98,7 @@ def lib():
             "imsrg_gpu_profile_enable": [vp, i],
             "imsrg_gpu_profile_read": [vp, i, dp, C.POINTER(C.c_long)],
             "imsrg_gpu_profile_reset": [vp],
+            "imsrg_gpu_commutator_noalloc": [vp, vp, i, vp, i, vp, i, vp],
         }
         for name, args in sig.items():
             f = getattr(L, name)
@@ -306,6 +307,17 @@ def mbpt2(H: Operator) -> float:
 def commutator(L: Operator, R: Operator, RES: Operator, precision: str = "fp64", with_e0: bool = True):
     """[L, R] -> RES (RES herm = -herm(L) herm(R)); asynchronous on the basis stream."""
     _check(lib().imsrg_gpu_commutator(L.handle, R.handle, RES.handle, PREC[precision], int(with_e0)), "commutator")
+
+
+def commutator_noalloc(basis: Basis, d_L: int, herm_L: int, d_R: int, herm_R: int, d_RES: int,
+                       with_e0: bool = True, stream: int | None = None):
+    """FP64 [L, R] on caller-owned device buffers (flat layout) that allocates
+    no device memory: for callers that may not allocate while they run.  The
+    intermediates use one fixed 8 MiB library array (bases up to emax = 4);
+    larger bases raise ImsrgError with status IMSRG_ERR_TOO_LARGE (9)."""
+    _check(lib().imsrg_gpu_commutator_noalloc(basis.handle, C.c_void_p(d_L), int(herm_L), C.c_void_p(d_R),
+                                              int(herm_R), C.c_void_p(d_RES), int(with_e0),
+                                              C.c_void_p(stream or 0)), "commutator_noalloc")
 
 
 def build_gs_white(H: Operator, ETA: Operator):

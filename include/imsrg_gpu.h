@@ -50,7 +50,8 @@ enum {
   IMSRG_ERR_NONFINITE = 5,      /* NaN/Inf detected in a result */
   IMSRG_ERR_TIMEOUT = 6,        /* a bounded device wait gave up */
   IMSRG_ERR_MISMATCH = 7,       /* operators of different bases */
-  IMSRG_ERR_NO_DEVICE = 8       /* no usable CUDA device */
+  IMSRG_ERR_NO_DEVICE = 8,      /* no usable CUDA device */
+  IMSRG_ERR_TOO_LARGE = 9       /* basis exceeds a fixed workspace limit */
 };
 
 /* Arithmetic of the dense two-body contractions (222_pp_hh ladders and the
@@ -180,6 +181,31 @@ enum {
 int imsrg_gpu_profile_enable(imsrg_basis_t *b, int on);
 int imsrg_gpu_profile_read(imsrg_basis_t *b, int kernel, double *ms, long *launches);
 int imsrg_gpu_profile_reset(imsrg_basis_t *b);
+
+/* --- allocation-free commutator (no counterpart in the reference) --------
+ * For callers that may not allocate device memory while they run: a host
+ * program whose device memory is owned by another allocator or capped, code
+ * running where a cudaMalloc/cudaFree (which can synchronise the whole
+ * device) is not allowed, or a driver that reserves all memory up front.
+ * Same result as imsrg_gpu_commutator(..., IMSRG_PREC_FP64, with_e0) on
+ * caller-owned device buffers d_L, d_R, d_RES in the flat layout (nfull
+ * doubles each; herm_L, herm_R = +1 or -1; RES herm is -herm_L*herm_R).  The
+ * intermediates live in one fixed array of IMSRG_NOALLOC_SCRATCH_DOUBLES
+ * doubles (8 MiB) that the library holds on every device that loads it, so
+ * the call allocates nothing.  Bases whose intermediates
+ * (2*nfull + 2*cc_total + wcc_total doubles) do not fit are rejected with
+ * IMSRG_ERR_TOO_LARGE (emax <= 4 fits; emax = 6 does not).
+ *  - The basis must have been created beforehand (creating it allocates the
+ *    device tables once) and its device must be current.
+ *  - The first call on each device looks up the array's device address; make
+ *    that first call before any stream capture.
+ *  - Work is enqueued on `stream` (NULL: the basis stream).  All calls share
+ *    the one array, so calls that overlap on the GPU race; serialise them.
+ *    The array keeps the last call's contents; every element a call reads is
+ *    written earlier in the same call, so nothing needs clearing. */
+#define IMSRG_NOALLOC_SCRATCH_DOUBLES 1048576
+int imsrg_gpu_commutator_noalloc(imsrg_basis_t *b, const double *d_L, int herm_L, const double *d_R, int herm_R,
+                                 double *d_RES, int with_e0, void *stream);
 
 #ifdef __cplusplus
 }
