@@ -1,0 +1,45 @@
+"""Generate the golden fixtures of tests/golden/ from the CPU oracle.
+
+Run from the repository root:  python tests/golden/make_golden.py
+Writes emax2_golden.npz: the 4He emax=2 basis, seeded synthetic Omega and H
+(H normal-ordered), the oracle's [Omega,H], White generator of H, one BCH
+transform, and the Magnus-flow trace (step, s, E0, E0+mbpt2, |mbpt2|) to s=50;
+plus a uniform-[-5,5] operator pair (brute_force_testing.f90 style) and its
+commutator.
+"""
+import os
+import sys
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
+sys.path.insert(0, ROOT)
+sys.path.insert(0, os.path.join(ROOT, "eom-imsrg_full_gb300"))
+
+from imsrg_gpu.layout import Layout, ho_basis  # noqa: E402
+from imsrg_gpu.synth import random_operator, synth_hamiltonian, synth_omega  # noqa: E402
+from oracle.oracle import Oracle  # noqa: E402
+
+
+def main():
+    bas = ho_basis(2)
+    lay = Layout(**bas)
+    orc = Oracle(**bas)
+    H = orc.normal_order(synth_hamiltonian(lay, 1))
+    O = synth_omega(lay, 1)
+    comm = orc.commutator(O, -1, H, 1)
+    eta = orc.white(H)
+    hs, nbch = orc.bch_expand(O, H)
+    flow = orc.magnus_decouple(H, s_max=50.0, ds=0.5)
+    A = random_operator(lay, -1, 1001, 1)
+    Bm = random_operator(lay, 1, 1002, 2)
+    commAB = orc.commutator(A, -1, Bm, 1)
+    out = os.path.join(os.path.dirname(os.path.abspath(__file__)), "emax2_golden.npz")
+    np.savez_compressed(out, nn=bas["nn"], ll=bas["ll"], jj=bas["jj"], itzp=bas["itzp"], con=bas["con"],
+                        H=H, Omega=O, comm=comm, eta=eta, bch=hs, nbch=nbch, flow_trace=flow["trace"],
+                        flow_H=flow["H"], A=A, B=Bm, commAB=commAB)
+    print("wrote", out, "flow steps", flow["steps"], "E0", flow["trace"][-1, 2])
+
+
+if __name__ == "__main__":
+    main()
