@@ -71,7 +71,7 @@ int commutator_dev(imsrg_basis *b, const double *L, int hL, const double *R, int
   } else {
     return IMSRG_ERR_INVALID;
   }
-  IMSRG_TRY(launch_assemble_2body(b, L, hL, R, hR, RES, hRES));
+  IMSRG_TRY(launch_assemble_2body(b, L, hL, R, hR, RES, hRES, with_e0));
   IMSRG_TRY(launch_assemble_1body(b, L, hL, R, hR, RES, hRES, with_e0));
   return IMSRG_OK;
 }

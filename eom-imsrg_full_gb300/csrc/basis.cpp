@@ -405,6 +405,232 @@ int build_basis(imsrg_basis *b) {
   IMSRG_TRY(dev_upload(b, cc_colpair, &T.cc_colpair));
   IMSRG_TRY(dev_upload(b, cc_colstart, &T.cc_colstart));
   IMSRG_TRY(dev_upload(b, ph_pairs, &T.ph_pairs));
+
+  // --- work orders (see DevTables::asm2_order)
+  {
+    auto ljtn = [&](int a) { return ljt_count[a]; };
+    auto jpcount = [&](int lo, int hi) { return hi >= lo ? (hi - lo) / 2 + 1 : 0; };
+    long off2b = b->off_fpp + (long)P * P;
+    std::vector<std::pair<long, int>> items;  // (signature, element)
+    static const int c1tab[6] = {0, 0, 0, 1, 2, 1}, c2tab[6] = {0, 1, 2, 1, 2, 2};
+    for (int qb = 0; qb < b->nblocks; qb++)
+      for (int g = 0; g < 6; g++) {
+        int n1 = b->gam_n1[qb * 6 + g], n2 = b->gam_n2[qb * 6 + g];
+        for (int JX = 0; JX < n2; JX++)
+          for (int IX = 0; IX < n1; IX++) {
+            if (sq[g] && IX > JX) continue;
+            const std::vector<int> &qr = b->qn[qb * 3 + c1tab[g]], &qc = b->qn[qb * 3 + c2tab[g]];
+            int i = qr[2 * IX], j = qr[2 * IX + 1], k = qc[2 * JX], l = qc[2 * JX + 1];
+            int ji = b->jj[i], jjv = b->jj[j], jk = b->jj[k], jl = b->jj[l];
+            int n_in = jpcount(std::max(std::abs(jjv - jl), std::abs(ji - jk)), std::min(jjv + jl, ji + jk));
+            int n_out = jpcount(std::max(std::abs(ji - jl), std::abs(jjv - jk)), std::min(ji + jl, jjv + jk));
+            long sig = ((((long)n_in * 32 + n_out) * 8 + ljtn(i)) * 8 + ljtn(j)) * 64 + ljtn(k) * 8 + ljtn(l);
+            items.push_back({sig, (int)(b->gam_off[qb * 6 + g] + IX + (long)JX * n1 - off2b)});
+          }
+      }
+    std::stable_sort(items.begin(), items.end(),
+                     [](const std::pair<long, int> &x, const std::pair<long, int> &y) { return x.first < y.first; });
+    std::vector<int> order(items.size());
+    for (size_t t = 0; t < items.size(); t++) order[t] = items[t].second;
+    T.n_asm2 = (int)order.size();
+    IMSRG_TRY(dev_upload(b, order, &T.asm2_order));
+
+    std::vector<std::pair<long, int>> cit;
+    for (int q1 = 0; q1 < b->ccblocks; q1++) {
+      int rlen = b->cc_rlen[q1], nph = b->cc_nph[q1], JC = b->cc_J2[q1];
+      const int *rows = cc_rowpair.data() + cc_rowstart[q1];
+      const int *cols = cc_colpair.data() + cc_colstart[q1];
+      for (int nb = 0; nb < nph; nb++)
+        for (int r = 0; r < rlen; r++) {
+          int a = rows[r] >> 16, bb = rows[r] & 0xffff, p = cols[nb] >> 16, h = cols[nb] & 0xffff;
+          int n = 0;
+          if ((b->ll[a] + b->ll[h]) % 2 == (b->ll[bb] + b->ll[p]) % 2 && b->itzp[a] + b->itzp[h] == b->itzp[bb] + b->itzp[p])
+            n = jpcount(std::max(std::abs(b->jj[p] - b->jj[bb]), std::abs(b->jj[a] - b->jj[h])),
+                        std::min(b->jj[p] + b->jj[bb], b->jj[a] + b->jj[h]));
+          (void)JC;
+          cit.push_back({n, (int)(b->cc_off[q1] + r + (long)nb * rlen)});
+        }
+    }
+    std::stable_sort(cit.begin(), cit.end(),
+                     [](const std::pair<long, int> &x, const std::pair<long, int> &y) { return x.first < y.first; });
+    std::vector<int> corder(cit.size());
+    for (size_t t = 0; t < cit.size(); t++) corder[t] = cit[t].second;
+    T.n_ccf = (int)corder.size();
+    IMSRG_TRY(dev_upload(b, corder, &T.ccf_order));
+  }
+
+  // --- gather lists of the one-body assembly (commutators.f90:83-280, 435-578)
+  {
+    // host restatement of the element location of v_elem (basic_IMSRG.f90:1270-1385)
+    auto hloc = [&](int a, int bb, int c, int d, int J2, long *idx, double *pre, int *trans) {
+      *idx = -1;
+      if (!(tri(b->jj[a], b->jj[bb], J2) && tri(b->jj[c], b->jj[d], J2))) return;
+      int Pp = (b->ll[a] + b->ll[bb]) & 1;
+      if (((b->ll[c] + b->ll[d]) & 1) != Pp) return;
+      int tz2 = b->itzp[a] + b->itzp[bb];
+      if (b->itzp[c] + b->itzp[d] != tz2) return;
+      int qq = 3 * J2 + 2 * (tz2 / 2 + 1) + Pp;
+      int C1 = b->con[a] + b->con[bb] + 1, C2 = b->con[c] + b->con[d] + 1;
+      int qx = C1 * C2;
+      if (qx == 9) qx = 5;
+      double pr = 1.0;
+      int i1, i2;
+      if (a > bb) {
+        i1 = pairrow[((size_t)bb * N + a) * nJ + J2 / 2];
+        pr = ((1 + (b->jj[a] + b->jj[bb] - J2) / 2) % 2) ? -1.0 : 1.0;
+      } else {
+        if (a == bb) pr = pr * 1.4142135623730951;
+        i1 = pairrow[((size_t)a * N + bb) * nJ + J2 / 2];
+      }
+      if (c > d) {
+        i2 = pairrow[((size_t)d * N + c) * nJ + J2 / 2];
+        pr = pr * (((1 + (b->jj[c] + b->jj[d] - J2) / 2) % 2) ? -1.0 : 1.0);
+      } else {
+        if (c == d) pr = pr * 1.4142135623730951;
+        i2 = pairrow[((size_t)c * N + d) * nJ + J2 / 2];
+      }
+      int sg = qq * 6 + qx - 1;
+      *trans = C1 > C2;
+      *idx = *trans ? b->gam_off[sg] + i2 + (long)i1 * b->gam_n1[sg] : b->gam_off[sg] + i1 + (long)i2 * b->gam_n1[sg];
+      *pre = pr;
+    };
+    std::vector<OneBodyTerm> terms;
+    long nel = (long)A * A + (long)P * A + (long)P * P;
+    std::vector<int> ostart(nel), ocount(nel);
+    auto same = [&](int x, int y) { return b->jj[x] == b->jj[y] && b->ll[x] == b->ll[y] && b->itzp[x] == b->itzp[y]; };
+    for (long e = 0; e < nel; e++) {
+      ostart[e] = (int)terms.size();
+      int pk, qk;
+      bool upper_only = true, with_pm = true;
+      if (e < (long)A * A) {
+        int p = (int)(e % A), q = (int)(e / A);
+        pk = b->holes[p];
+        qk = b->holes[q];
+        if (p > q) upper_only = false;
+      } else if (e < (long)A * A + (long)P * A) {
+        long e2 = e - (long)A * A;
+        pk = b->parts[e2 % P];
+        qk = b->holes[e2 / P];
+        with_pm = false;
+      } else {
+        long e3 = e - (long)A * A - (long)P * A;
+        int p = (int)(e3 % P), q = (int)(e3 / P);
+        pk = b->parts[p];
+        qk = b->parts[q];
+        if (p > q) upper_only = false;
+      }
+      if (!upper_only || !same(pk, qk)) {
+        ocount[e] = 0;
+        continue;
+      }
+      // commutator_121 inner sum (commutators.f90:117-150)
+      int jq = b->jj[qk];
+      for (size_t k = 0; k < ph_pairs.size() / 2; k++) {
+        int a = ph_pairs[2 * k], i = ph_pairs[2 * k + 1];
+        int ak = b->parts[a], ik = b->holes[i];
+        int ji = b->jj[ik];
+        int ph = a + i * P;
+        for (int JT = std::abs(ji - jq); JT <= ji + jq; JT += 2) {
+          long idx;
+          double pr;
+          int tr;
+          hloc(ak, pk, ik, qk, JT, &idx, &pr, &tr);
+          if (idx >= 0) terms.push_back({(int)idx, 0 | (tr << 2) | (ph << 8), (JT + 1.0) * pr});
+          hloc(ik, pk, ak, qk, JT, &idx, &pr, &tr);
+          if (idx >= 0) terms.push_back({(int)idx, 1 | (tr << 2) | (ph << 8), (JT + 1.0) * pr});
+        }
+      }
+      // commutator_221 (commutators.f90:470-486)
+      int ji = b->jj[pk];
+      for (int c = 0; c < N; c++) {
+        int jc = b->jj[c];
+        int w2 = b->con[c] ? 0 : 1;
+        for (int JT = std::abs(jc - ji); JT <= jc + ji; JT += 2) {
+          long idx;
+          double pr;
+          int tr;
+          hloc(c, pk, c, qk, JT, &idx, &pr, &tr);
+          if (idx >= 0) terms.push_back({(int)idx, 2 | (w2 << 3), (JT + 1.0) * pr});
+          if (with_pm) {
+            hloc(c, qk, c, pk, JT, &idx, &pr, &tr);
+            if (idx >= 0) terms.push_back({(int)idx, 3 | (w2 << 3), (JT + 1.0) * pr});
+          }
+        }
+      }
+      ocount[e] = (int)terms.size() - ostart[e];
+    }
+    IMSRG_TRY(dev_upload(b, terms, &T.obt));
+    IMSRG_TRY(dev_upload(b, ostart, &T.obt_start));
+    IMSRG_TRY(dev_upload(b, ocount, &T.obt_count));
+    // work split of the one-body kernel: allowed upper-triangle elements
+    // (longest gather list first) and all elements without a gather list
+    std::vector<int> heavy, light;
+    for (long e = 0; e < nel; e++) {
+      int pk, qk, p = 0, q = 0;
+      bool square = true;
+      if (e < (long)A * A) {
+        p = (int)(e % A);
+        q = (int)(e / A);
+        pk = b->holes[p];
+        qk = b->holes[q];
+      } else if (e < (long)A * A + (long)P * A) {
+        long e2 = e - (long)A * A;
+        pk = b->parts[e2 % P];
+        qk = b->holes[e2 / P];
+        square = false;
+      } else {
+        long e3 = e - (long)A * A - (long)P * A;
+        p = (int)(e3 % P);
+        q = (int)(e3 / P);
+        pk = b->parts[p];
+        qk = b->parts[q];
+      }
+      if (!same(pk, qk)) light.push_back((int)e);
+      else if (!square || p <= q) heavy.push_back((int)e);
+    }
+    std::stable_sort(heavy.begin(), heavy.end(), [&](int x, int y) { return ocount[x] > ocount[y]; });
+    T.n_asm1_heavy = (int)heavy.size();
+    T.n_asm1_light = (int)light.size();
+    IMSRG_TRY(dev_upload(b, heavy, &T.asm1_heavy));
+    IMSRG_TRY(dev_upload(b, light, &T.asm1_light));
+
+    // Pandya transform, cross_coupled.f90:1247-1291: CCX(r(a,b), nb(p,h)) =
+    // (-1)^((jh+jb+J')/2) sqrt(2J'+1) sum_J (-1)^J (2J+1) {jp jh J'; ja jb J} V^J_{hapb}
+    std::vector<int> cstart(b->cc_total + 1), cidx;
+    std::vector<double> ccoef;
+    for (int q1 = 0; q1 < b->ccblocks; q1++) {
+      int rlen = b->cc_rlen[q1], nph = b->cc_nph[q1], JC = b->cc_J2[q1];
+      const int *rows = cc_rowpair.data() + cc_rowstart[q1];
+      const int *cols = cc_colpair.data() + cc_colstart[q1];
+      for (int nb = 0; nb < nph; nb++)
+        for (int r = 0; r < rlen; r++) {
+          long e = b->cc_off[q1] + r + (long)nb * rlen;
+          cstart[e] = (int)cidx.size();
+          int a = rows[r] >> 16, bb = rows[r] & 0xffff, p = cols[nb] >> 16, h = cols[nb] & 0xffff;
+          if (!((b->ll[a] + b->ll[h]) % 2 == (b->ll[bb] + b->ll[p]) % 2 &&
+                b->itzp[a] + b->itzp[h] == b->itzp[bb] + b->itzp[p]))
+            continue;
+          int jp = b->jj[p], jh = b->jj[h], ja = b->jj[a], jb = b->jj[bb];
+          double outer = (((jh + jb + JC) / 2) % 2 ? -1.0 : 1.0) * std::sqrt(JC + 1.0);
+          for (int JT = std::max(std::abs(jp - jb), std::abs(ja - jh)); JT <= std::min(jp + jb, ja + jh); JT += 2) {
+            long idx;
+            double pr;
+            int tr;
+            hloc(h, a, p, bb, JT, &idx, &pr, &tr);
+            if (idx < 0) continue;
+            double s6 = six[((((size_t)(jp >> 1) * nj + (jh >> 1)) * nj + (ja >> 1)) * nj + (jb >> 1)) * nJ * nJ +
+                            (JC >> 1) * nJ + (JT >> 1)];
+            double w = ((JT / 2) % 2 ? -1.0 : 1.0) * (JT + 1) * s6;
+            cidx.push_back((int)idx | (tr ? (int)0x80000000u : 0));
+            ccoef.push_back(w * outer * pr);
+          }
+        }
+    }
+    cstart[b->cc_total] = (int)cidx.size();
+    IMSRG_TRY(dev_upload(b, cstart, &T.cct_start));
+    IMSRG_TRY(dev_upload(b, cidx, &T.cct_idx));
+    IMSRG_TRY(dev_upload(b, ccoef, &T.cct_coef));
+  }
   IMSRG_TRY(dev_upload(b, b->holes, &T.hole_orb));
   IMSRG_TRY(dev_upload(b, b->parts, &T.part_orb));
   T.n_ph_pairs = (int)ph_pairs.size() / 2;
@@ -435,7 +661,7 @@ int build_basis(imsrg_basis *b) {
   b->mono = (double *)p;
   IMSRG_TRY(dev_alloc(b, 64 * sizeof(double), &p));
   b->scal = (double *)p;
-  b->partials_len = std::max(b->nchunks, b->nblocks) + 64;
+  b->partials_len = std::max(std::max(b->nchunks, b->nblocks), (T.n_asm2 + 255) / 256) + 64;
   IMSRG_TRY(dev_alloc(b, b->partials_len * sizeof(double), &p));
   b->partials = (double *)p;
   IMSRG_TRY(dev_alloc(b, std::max(b->nfull, b->neq) * sizeof(double), &p));

@@ -46,7 +46,41 @@ struct DevTables {
   int n_ph_pairs;
   const int *hole_orb;     // [hole position] -> orbit
   const int *part_orb;     // [particle position] -> orbit
+  // Work orders: element indices grouped by identical loop-trip signatures so
+  // the lanes of a warp run the same FP64 instruction sequence (GB300 issues
+  // an FP64 warp instruction at full cost whatever the active lanes).
+  const int *asm2_order;   // two-body elements (offset from the first gam), upper triangles only
+  int n_asm2;
+  const int *ccf_order;    // cross-coupled elements
+  int n_ccf;
+  // Gather lists of the Pandya transform: element e of every CC block is
+  // sum_k cct_coef[k] * op[cct_idx[k] & 0x7fffffff] (bit 31: read transposed,
+  // times herm), k in [cct_start[e], cct_start[e + 1]).
+  const int *cct_start;
+  const int *cct_idx;
+  const double *cct_coef;
+  // Gather lists of the one-body assembly (121 and 221 sums), per one-body
+  // element in flat order: obt[obt_start[e] .. + obt_count[e]).
+  const struct OneBodyTerm *obt;
+  const int *obt_start;
+  const int *obt_count;
+  // One-body work split: elements with gather lists (a CTA each, longest
+  // first) and the rest (a warp each); mirrored lower triangles are in neither.
+  const int *asm1_heavy;
+  int n_asm1_heavy;
+  const int *asm1_light;
+  int n_asm1_light;
   long cc_total, wcc_total;
+};
+
+// One term of a one-body sum.  kind 0/1: commutator_121 terms at the two
+// locations <a p|i q> and <i p|a q> (idx into L and R, ph = fph offset of the
+// (a,i) pair, trans = read transposed); kind 2/3: commutator_221 terms
+// <c i|c j> and the -herm(L)herm(R) <c j|c i> term (idx into W1 or W2).
+struct OneBodyTerm {
+  int idx;
+  int meta;     // bits 0-1 kind, bit 2 trans, bit 3 W2 (else W1), bits 8.. ph
+  double coef;  // (2J+1) x phase x sqrt(2)^n
 };
 
 // One term alpha * op(A) * op(B) of a grouped GEMM problem.  Operand ids:
@@ -166,7 +200,8 @@ int cuda_status(cudaError_t e);
 // launchers (kernels_*.cu); all enqueue on b->stream and bump b->launches
 int launch_cc_forward(imsrg_basis *b, const double *L, int hL, const double *R, int hR);
 int launch_gemm_fp64(imsrg_basis *b, const double *L, int hL, const double *R, int hR);
-int launch_assemble_2body(imsrg_basis *b, const double *L, int hL, const double *R, int hR, double *RES, int hRES);
+int launch_assemble_2body(imsrg_basis *b, const double *L, int hL, const double *R, int hR, double *RES, int hRES,
+                          int with_e0);
 int launch_assemble_1body(imsrg_basis *b, const double *L, int hL, const double *R, int hR, double *RES, int hRES,
                           int with_e0);
 int launch_axpby(imsrg_basis *b, const double *A, double ax, const double *B, double bx, double *C);
@@ -181,6 +216,7 @@ int launch_check_finite(imsrg_basis *b, const double *op, int *d_flag);
 // cross-coupled blocks) and WCC.
 struct Workspace {
   double *w1, *w2, *lcc, *rcc, *wcc;
+  double *e0p;  // per-CTA commutator_220 partials of the two-body kernel
 };
 int launch_commutator_fp64_ws(imsrg_basis *b, const Workspace &ws, const double *L, int hL, const double *R, int hR,
                               double *RES, int hRES, int with_e0, cudaStream_t st);

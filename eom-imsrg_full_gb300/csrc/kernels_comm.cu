@@ -37,38 +37,23 @@ __device__ __forceinline__ int upper_bound_l(const long *a, int n, long x) {
 // ---------------------------------------------------------------------------
 // 1. Pandya transform: CCX(r(a,b), nb(p,h)) of cross_coupled.f90:1247-1291.
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(256) k_cc_forward(DevTables T, const double *L, int hL, const double *R, int hR,
-                                                    double *LCC, double *RCC) {
+__global__ void __launch_bounds__(256) k_cc_forward(DevTables T, const double *__restrict__ L, int hL,
+                                                    const double *__restrict__ R, int hR, double *LCC, double *RCC) {
   long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= 2 * T.cc_total) return;
-  int which = t >= T.cc_total;
-  long e = which ? t - T.cc_total : t;
-  const double *op = which ? R : L;
-  int herm = which ? hR : hL;
-  double *out = which ? RCC : LCC;
-  int q1 = upper_bound_l(T.cc_off, T.ccblocks, e) - 1;
-  // skip empty blocks that share this offset
-  while (q1 + 1 < T.ccblocks && T.cc_off[q1 + 1] <= e) q1++;
-  int rlen = T.cc_rlen[q1];
-  long loc = e - T.cc_off[q1];
-  int r = (int)(loc % rlen), nb = (int)(loc / rlen);
-  int ab = T.cc_rowpair[T.cc_rowstart[q1] + r];
-  int ph = T.cc_colpair[T.cc_colstart[q1] + nb];
-  int a = ab >> 16, b = ab & 0xffff, p = ph >> 16, h = ph & 0xffff;
-  int4 oa = T.orb[a], ob = T.orb[b], op_ = T.orb[p], oh = T.orb[h];
-  int JC = T.cc_J2[q1];
-  double x = 0.0;
-  if (((oa.y + oh.y) & 1) == ((ob.y + op_.y) & 1) && (oa.z + oh.z) == (ob.z + op_.z)) {
-    int jp = op_.x, jh = oh.x, ja = oa.x, jb = ob.x;
-    int Jmin = max(abs(jp - jb), abs(ja - jh));
-    int Jmax = min(jp + jb, ja + jh);
-    double sm = 0.0;
-    // sum_J (-1)^J (2J+1) {jp jh J'; ja jb J} V^J_{hapb}: one DFMA per J
-    for (int JT = Jmin; JT <= Jmax; JT += 2)
-      sm = fma(dflip(sixj_w(T, jp, jh, JC, ja, jb, JT), JT >> 1), v_elem(T, op, herm, h, a, p, b, JT), sm);
-    x = dflip(sm, (jh + jb + JC) >> 1) * T.sqrt_j21[JC >> 1];
+  if (t >= T.cc_total) return;
+  const long e = T.ccf_order[t];  // elements grouped by term count
+  const int k0 = T.cct_start[e], k1 = T.cct_start[e + 1];
+  const int nL = hL < 0, nR = hR < 0;
+  double sl = 0.0, sr = 0.0;
+  for (int k = k0; k < k1; k++) {
+    const int ix = T.cct_idx[k];
+    const int tr = (int)((unsigned)ix >> 31), idx = ix & 0x7fffffff;
+    const double c = T.cct_coef[k];
+    sl = fma(c, dflip(L[idx], tr & nL), sl);
+    sr = fma(c, dflip(R[idx], tr & nR), sr);
   }
-  out[e] = x;
+  LCC[e] = sl;
+  RCC[e] = sr;
 }
 
 // ---------------------------------------------------------------------------
@@ -271,20 +256,23 @@ __device__ __forceinline__ bool c222ph(const DevTables &T, const double *W, int 
 
 __global__ void __launch_bounds__(256) k_assemble_2body(DevTables T, const double *L, int hL, const double *R, int hR,
                                                         const double *W1, const double *W2, const double *WCC,
-                                                        double *RES, int hRES, long off2b) {
-  long e = off2b + (long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (e >= T.nfull) return;
+                                                        double *RES, int hRES, long off2b, double *e0p) {
+  __shared__ double sh220[8];
+  long w = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  double e220 = 0.0;  // this element's commutator_220 term (pphh arrays only)
+  if (w < T.n_asm2) {
+  long e = off2b + T.asm2_order[w];
   int s = upper_bound_l(T.gam_off, T.nblocks * 6, e) - 1;
   int q = s / 6, g = s % 6;
   int n1 = T.gam_n1[s];
   long loc = e - T.gam_off[s];
   int IX = (int)(loc % n1), JX = (int)(loc / n1);
-  bool square = (g == 0 || g == 3 || g == 4);
-  if (square && IX > JX) return;
+  bool square = (g == 0 || g == 3 || g == 4);  // only IX <= JX is in the work order
   // row / column pair categories: sea1 = (1,1,1,2,3,2), sea2 = (1,2,3,2,3,3)
-  const int c1tab[6] = {0, 0, 0, 1, 2, 1}, c2tab[6] = {0, 1, 2, 1, 2, 2};
-  const int *qr = T.qn + T.qn_start[q * 3 + c1tab[g]] + 2 * IX;
-  const int *qc = T.qn + T.qn_start[q * 3 + c2tab[g]] + 2 * JX;
+  // (categories 0 pp, 1 ph, 2 hh; packed two bits per g so no local array is needed)
+  const int c1 = (1600 >> (2 * g)) & 3, c2 = (2660 >> (2 * g)) & 3;
+  const int *qr = T.qn + T.qn_start[q * 3 + c1] + 2 * IX;
+  const int *qc = T.qn + T.qn_start[q * 3 + c2] + 2 * JX;
   int a = qr[0], b = qr[1], c = qc[0], d = qc[1];
   int J2 = T.blk_J2[q];
   int nres = hRES < 0, npm = (hL * hR) < 0;
@@ -308,174 +296,203 @@ __global__ void __launch_bounds__(256) k_assemble_2body(DevTables T, const doubl
     RES[e] = t;
     if (square) RES[em] = dflip(t, nres);
   }
-}
-
-// ---------------------------------------------------------------------------
-// 4. One-body assembly (one warp per element) and E0 (last CTA).
-// ---------------------------------------------------------------------------
-// inner (a,i) sum of commutator_121 (commutators.f90:117-150) for orbits pk,qk
-__device__ double c121_warp(const DevTables &T, const double *L, int hL, const double *R, int hR, int pk, int qk,
-                            int lane) {
-  int jq = T.orb[qk].x;
-  double sm = 0.0;
-  for (int k = lane; k < T.n_ph_pairs; k += 32) {
-    int a = T.ph_pairs[2 * k], i = T.ph_pairs[2 * k + 1];
-    int ak = T.part_orb[a], ik = T.hole_orb[i];
-    int ji = T.orb[ik].x;
-    double smx = 0, smy = 0, smx2 = 0, smy2 = 0;
-    for (int JT = abs(ji - jq); JT <= ji + jq; JT += 2) {
-      VLoc v1 = v_loc(T, ak, pk, ik, qk, JT);
-      smx += v_read(R, hR, v1) * (JT + 1);
-      smx2 += v_read(L, hL, v1) * (JT + 1);
-      VLoc v2 = v_loc(T, ik, pk, ak, qk, JT);
-      smy += v_read(R, hR, v2) * (JT + 1);
-      smy2 += v_read(L, hL, v2) * (JT + 1);
-    }
-    double lph = L[T.off_fph + a + (long)i * T.P], rph = R[T.off_fph + a + (long)i * T.P];
-    sm += lph * (hL * smx - smy) - rph * (hR * smx2 - smy2);
+  // commutator_220 (commutators.f90:409-427): -(2J+1) L_pphh R_pphh herm_R
+  if (e0p && g == 2) e220 = -L[e] * R[e] * hR * (J2 + 1.0);
   }
-  return warp_sum(sm);
-}
-
-// sum of commutator_221 (commutators.f90:470-486) for orbits ik, jk
-__device__ double c221_warp(const DevTables &T, const double *W1, const double *W2, int pm, int ik, int jk,
-                            bool with_pm, int lane) {
-  int ji = T.orb[ik].x;
-  double sm = 0.0;
-  for (int c = lane; c < T.norb; c += 32) {
-    int jc = T.orb[c].x;
-    const double *W = T.orb[c].w ? W1 : W2;
-    for (int JT = abs(jc - ji); JT <= jc + ji; JT += 2) {
-      double v = v_elem(T, W, 1, c, ik, c, jk, JT);
-      if (with_pm) v = v - pm * v_elem(T, W, 1, c, jk, c, ik, JT);
-      sm += v * (JT + 1);
+  if (e0p) {  // per-CTA partial in a fixed order; the one-body kernel sums them
+    e220 = warp_sum(e220);
+    if ((threadIdx.x & 31) == 0) sh220[threadIdx.x >> 5] = e220;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      double t220 = 0.0;
+      for (int k = 0; k < (int)(blockDim.x >> 5); k++) t220 += sh220[k];
+      e0p[blockIdx.x] = t220;
     }
   }
-  return warp_sum(sm);
 }
 
-__device__ double dot_warp(const double *x, long sx, const double *y, long sy, int n, int lane) {
-  double s = 0.0;
-  for (int k = lane; k < n; k += 32) s = fma(x[k * sx], y[k * sy], s);
-  return warp_sum(s);
-}
 
-__device__ double block_sum(double v, double *sh) {
-  v = warp_sum(v);
-  int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  if (lane == 0) sh[w] = v;
+
+
+// Sum of NV values over the CTA (fixed order: warp shuffles, then warps in
+// index order), returned to every thread.
+template <int NV>
+__device__ void cta_sum(double *v, double (*sh)[8]) {
+  int w = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
+#pragma unroll
+  for (int i = 0; i < NV; i++) v[i] = warp_sum(v[i]);
+  if (lane == 0)
+#pragma unroll
+    for (int i = 0; i < NV; i++) sh[w][i] = v[i];
   __syncthreads();
-  double r = 0.0;
-  if (threadIdx.x < 32) {
-    r = (lane < (int)(blockDim.x >> 5)) ? sh[lane] : 0.0;
-    r = warp_sum(r);
+#pragma unroll
+  for (int i = 0; i < NV; i++) {
+    double t = 0.0;
+    for (int k = 0; k < nw; k++) t += sh[k][i];
+    v[i] = t;
   }
   __syncthreads();
-  return r;
 }
 
-__global__ void __launch_bounds__(256) k_assemble_1body(DevTables T, const double *L, int hL, const double *R, int hR,
+// One-body assembly.  The (l,j,tz)-allowed upper-triangle elements carry the
+// 121 and 221 gather lists (a few hundred independent terms each) and get a
+// CTA of four warps; every other element only has the four commutator_111 dot
+// products and gets one warp, four elements per CTA.  Each thread folds its
+// partial dot products and gather sums into the element's final linear
+// combination, so one reduction per element remains.  The last CTA computes E0.
+__global__ void __launch_bounds__(128) k_assemble_1body(DevTables T, const double *L, int hL, const double *R, int hR,
                                                         const double *W1, const double *W2, double *RES, int hRES,
-                                                        int with_e0, int n_elem_blocks) {
-  __shared__ double sh[32];
-  int A = T.A, P = T.P;
+                                                        int with_e0, const double *e0p, int ne0p) {
+  __shared__ double sh[4][8];
+  const int A = T.A, P = T.P;
   const double *Lhh = L + T.off_fhh, *Lph = L + T.off_fph, *Lpp = L + T.off_fpp;
   const double *Rhh = R + T.off_fhh, *Rph = R + T.off_fph, *Rpp = R + T.off_fpp;
-  if ((int)blockIdx.x == n_elem_blocks) {
+  const int nheavy = T.n_asm1_heavy, nlight_cta = (T.n_asm1_light + 3) >> 2;
+  if ((int)blockIdx.x == nheavy + nlight_cta) {
     if (!with_e0) return;
-    // E0 = commutator_110 + commutator_220
-    double s110 = 0.0;
-    for (int k = threadIdx.x; k < P * A; k += blockDim.x) {
+    // E0 = commutator_110 + commutator_220 (commutators.f90:10-33, 399-432)
+    const int tid = threadIdx.x, nt = blockDim.x;
+    double v[2] = {0.0, 0.0};
+    for (int k = tid; k < P * A; k += nt) {
       int ji = T.orb[T.hole_orb[k / P]].x;
-      s110 += (Lph[k] * Rph[k] * hL - Rph[k] * Lph[k] * hR) * (ji + 1);
+      v[0] += (Lph[k] * Rph[k] * hL - Rph[k] * Lph[k] * hR) * (ji + 1);
     }
-    double e110 = block_sum(s110, sh);
-    double s220 = 0.0;
-    if (hL * hR == -1) {
-      for (int q = 0; q < T.nblocks; q++) {
-        long o = T.gam_off[q * 6 + 2];
-        int n = T.gam_n1[q * 6 + 2] * T.gam_n2[q * 6 + 2];
-        double w = T.blk_J2[q] + 1;
-        for (int k = threadIdx.x; k < n; k += blockDim.x) s220 -= L[o + k] * R[o + k] * hR * w;
-      }
-    }
-    double e220 = block_sum(s220, sh) * 2.0;
-    if (threadIdx.x == 0) RES[0] = e110 + e220;
+    if (e0p)  // commutator_220 partials of the two-body kernel
+      for (int k = tid; k < ne0p; k += nt) v[1] += e0p[k];
+    cta_sum<2>(v, sh);
+    if (tid == 0) RES[0] = v[0] + v[1] * 2.0;
     return;
   }
-  int lane = threadIdx.x & 31;
-  long e = (long)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
-  long nA2 = (long)A * A, nPA = (long)P * A, nP2 = (long)P * P;
-  if (e >= nA2 + nPA + nP2) return;
-  const int *hole_orb = T.hole_orb, *part_orb = T.part_orb;
-  if (e < nA2) {
-    int p = (int)(e % A), q = (int)(e / A);
-    int pk = hole_orb[p], qk = hole_orb[q];
-    bool allowed = T.orb[pk].x == T.orb[qk].x && T.orb[pk].y == T.orb[qk].y && T.orb[pk].z == T.orb[qk].z;
-    if (allowed && p > q) return;
-    // th1 = Lhh Rhh, th2 = Lph^T Rph (commutators.f90:56-59)
-    double th1pq = dot_warp(Lhh + p, A, Rhh + (long)q * A, 1, A, lane);
-    double th2pq = dot_warp(Lph + (long)p * P, 1, Rph + (long)q * P, 1, P, lane);
-    double th1qp = dot_warp(Lhh + q, A, Rhh + (long)p * A, 1, A, lane);
-    double th2qp = dot_warp(Lph + (long)q * P, 1, Rph + (long)p * P, 1, P, lane);
-    double t = th1pq + th2pq * hL - (th1qp * hL + th2qp) * hR;
-    if (allowed) {
-      double s121 = c121_warp(T, L, hL, R, hR, pk, qk, lane) / (T.orb[pk].x + 1.0);
-      double s221 = c221_warp(T, W1, W2, hL * hR, pk, qk, true, lane) / (T.orb[pk].x + 1.0);
-      if (p == q) t = ((t + s121) * hRES + s221) * hRES;
-      else t = (t + s121) + s221;
-    }
-    if (lane == 0) {
-      RES[T.off_fhh + p + (long)q * A] = t;
-      if (allowed && p != q) RES[T.off_fhh + q + (long)p * A] = t * hRES;
-    }
-  } else if (e < nA2 + nPA) {
-    long e2 = e - nA2;
-    int p = (int)(e2 % P), q = (int)(e2 / P);
-    int pk = part_orb[p], qk = hole_orb[q];
-    bool allowed = T.orb[pk].x == T.orb[qk].x && T.orb[pk].y == T.orb[qk].y && T.orb[pk].z == T.orb[qk].z;
-    // RES%fph = (Lph Rhh + Lpp Rph) - Rph Lhh - Rpp Lph (commutators.f90:63-71)
-    double tb1 = dot_warp(Lph + p, P, Rhh + (long)q * A, 1, A, lane);
-    double tb2 = dot_warp(Lpp + p, P, Rph + (long)q * P, 1, P, lane);
-    double tb1b = dot_warp(Rph + p, P, Lhh + (long)q * A, 1, A, lane);
-    double tb2b = dot_warp(Rpp + p, P, Lph + (long)q * P, 1, P, lane);
-    double t = tb1 + tb2;
-    t = t - tb1b - tb2b;
-    if (allowed) {
-      double s121 = c121_warp(T, L, hL, R, hR, pk, qk, lane) / (T.orb[pk].x + 1.0);
-      double s221 = c221_warp(T, W1, W2, hL * hR, pk, qk, false, lane) / (T.orb[pk].x + 1.0);
-      t = (t + s121) + s221;
-    }
-    if (lane == 0) RES[T.off_fph + p + (long)q * P] = t;
+  const bool whole = (int)blockIdx.x < nheavy;  // block-uniform
+  long e;
+  int tid, nt;
+  if (whole) {
+    e = T.asm1_heavy[blockIdx.x];
+    tid = threadIdx.x;
+    nt = blockDim.x;
   } else {
-    long e3 = e - nA2 - nPA;
-    int p = (int)(e3 % P), q = (int)(e3 / P);
-    int pk = part_orb[p], qk = part_orb[q];
-    bool allowed = T.orb[pk].x == T.orb[qk].x && T.orb[pk].y == T.orb[qk].y && T.orb[pk].z == T.orb[qk].z;
-    if (allowed && p > q) return;
-    // tp1 = Lph Rph^T, tp2 = Lpp Rpp (commutators.f90:75-78)
-    double tp1pq = dot_warp(Lph + p, P, Rph + q, P, A, lane);
-    double tp2pq = dot_warp(Lpp + p, P, Rpp + (long)q * P, 1, P, lane);
-    double tp1qp = dot_warp(Lph + q, P, Rph + p, P, A, lane);
-    double tp2qp = dot_warp(Lpp + q, P, Rpp + (long)p * P, 1, P, lane);
-    double t = tp1pq * hR + tp2pq - (tp1qp + tp2qp * hR) * hL;
-    if (allowed) {
-      double s121 = c121_warp(T, L, hL, R, hR, pk, qk, lane) / (T.orb[pk].x + 1.0);
-      double s221 = c221_warp(T, W1, W2, hL * hR, pk, qk, true, lane) / (T.orb[pk].x + 1.0);
-      if (p == q) t = ((t + s121) * hRES + s221) * hRES;
-      else t = (t + s121) + s221;
+    const int li = ((int)blockIdx.x - nheavy) * 4 + (int)(threadIdx.x >> 5);
+    if (li >= T.n_asm1_light) return;
+    e = T.asm1_light[li];
+    tid = threadIdx.x & 31;
+    nt = 32;
+  }
+  const long nA2 = (long)A * A, nPA = (long)P * A;
+  int type, p, q, pk, qk;
+  if (e < nA2) {
+    type = 0;
+    p = (int)(e % A);
+    q = (int)(e / A);
+    pk = T.hole_orb[p];
+    qk = T.hole_orb[q];
+  } else if (e < nA2 + nPA) {
+    type = 1;
+    p = (int)((e - nA2) % P);
+    q = (int)((e - nA2) / P);
+    pk = T.part_orb[p];
+    qk = T.hole_orb[q];
+  } else {
+    type = 2;
+    p = (int)((e - nA2 - nPA) % P);
+    q = (int)((e - nA2 - nPA) / P);
+    pk = T.part_orb[p];
+    qk = T.part_orb[q];
+  }
+  const bool allowed = T.orb[pk].x == T.orb[qk].x && T.orb[pk].y == T.orb[qk].y && T.orb[pk].z == T.orb[qk].z;
+  // commutator_111 (commutators.f90:36-80): four dot products
+  double v[6] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
+  if (type == 0) {  // th1 = Lhh Rhh, th2 = Lph^T Rph
+    for (int k = tid; k < A; k += nt) {
+      v[0] = fma(Lhh[p + (long)k * A], Rhh[k + (long)q * A], v[0]);
+      v[2] = fma(Lhh[q + (long)k * A], Rhh[k + (long)p * A], v[2]);
     }
-    if (lane == 0) {
-      RES[T.off_fpp + p + (long)q * P] = t;
-      if (allowed && p != q) RES[T.off_fpp + q + (long)p * P] = t * hRES;
+    for (int k = tid; k < P; k += nt) {
+      v[1] = fma(Lph[k + (long)p * P], Rph[k + (long)q * P], v[1]);
+      v[3] = fma(Lph[k + (long)q * P], Rph[k + (long)p * P], v[3]);
+    }
+  } else if (type == 1) {  // Lph Rhh + Lpp Rph - Rph Lhh - Rpp Lph
+    for (int k = tid; k < A; k += nt) {
+      v[0] = fma(Lph[p + (long)k * P], Rhh[k + (long)q * A], v[0]);
+      v[2] = fma(Rph[p + (long)k * P], Lhh[k + (long)q * A], v[2]);
+    }
+    for (int k = tid; k < P; k += nt) {
+      v[1] = fma(Lpp[p + (long)k * P], Rph[k + (long)q * P], v[1]);
+      v[3] = fma(Rpp[p + (long)k * P], Lph[k + (long)q * P], v[3]);
+    }
+  } else {  // tp1 = Lph Rph^T, tp2 = Lpp Rpp
+    for (int k = tid; k < A; k += nt) {
+      v[0] = fma(Lph[p + (long)k * P], Rph[q + (long)k * P], v[0]);
+      v[2] = fma(Lph[q + (long)k * P], Rph[p + (long)k * P], v[2]);
+    }
+    for (int k = tid; k < P; k += nt) {
+      v[1] = fma(Lpp[p + (long)k * P], Rpp[k + (long)q * P], v[1]);
+      v[3] = fma(Lpp[q + (long)k * P], Rpp[k + (long)p * P], v[3]);
     }
   }
+  // commutator_121 and commutator_221 sums from the gather list
+  if (allowed) {
+    const int st = T.obt_start[e], n = T.obt_count[e];
+    const int nL = hL < 0, nR = hR < 0, npm = hL * hR > 0;
+    for (int k = tid; k < n; k += nt) {
+      const OneBodyTerm t = T.obt[st + k];
+      const int kind = t.meta & 3;
+      if (kind < 2) {
+        const int tr = (t.meta >> 2) & 1, ph = t.meta >> 8;
+        const double rv = dflip(R[t.idx], tr & nR) * t.coef;
+        const double lv = dflip(L[t.idx], tr & nL) * t.coef;
+        const double lph = Lph[ph], rph = Rph[ph];
+        if (kind == 0) {  // L_ai (herm_L R) - R_ai (herm_R L) at <a p|i q>
+          v[4] = fma(dflip(lph, nL), rv, v[4]);
+          v[4] = fma(-dflip(rph, nR), lv, v[4]);
+        } else {  // -L_ai R + R_ai L at <i p|a q>
+          v[4] = fma(-lph, rv, v[4]);
+          v[4] = fma(rph, lv, v[4]);
+        }
+      } else {
+        const double *W = (t.meta & 8) ? W2 : W1;
+        const double w = W[t.idx] * t.coef;
+        v[5] += (kind == 3) ? dflip(w, npm) : w;  // the second 221 term enters with -herm_L herm_R
+      }
+    }
+  }
+  // the element is linear in the six sums:
+  //   type 0: v0 + v1 hL - (v2 hL + v3) hR      type 1: v0 + v1 - v2 - v3
+  //   type 2: v0 hR + v1 - (v2 + v3 hR) hL
+  // plus (v4 + v5) / (2j_p + 1) on allowed elements, where a diagonal of fhh
+  // or fpp takes v5 times herm(RES) (((t + s121) hRES + s221) hRES with hRES^2 = 1)
+  double c0 = 1.0, c1 = 1.0, c2 = -1.0, c3 = -1.0;
+  if (type == 0) {
+    c1 = hL;
+    c2 = -(double)(hL * hR);
+    c3 = -hR;
+  } else if (type == 2) {
+    c0 = hR;
+    c2 = -hL;
+    c3 = -(double)(hR * hL);
+  }
+  double x = fma(c3, v[3], fma(c2, v[2], fma(c1, v[1], c0 * v[0])));
+  if (allowed) {
+    const double rj = 1.0 / (T.orb[pk].x + 1.0);
+    const double c5 = (type != 1 && p == q) ? hRES * rj : rj;
+    x = fma(c5, v[5], fma(rj, v[4], x));
+  }
+  x = warp_sum(x);
+  if (whole) {
+    if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5][0] = x;
+    __syncthreads();
+    x = ((sh[0][0] + sh[1][0]) + sh[2][0]) + sh[3][0];
+  }
+  if (tid != 0) return;
+  const long base = type == 0 ? T.off_fhh : type == 1 ? T.off_fph : T.off_fpp;
+  const int ld = type == 0 ? A : P;
+  RES[base + p + (long)q * ld] = x;
+  if (allowed && type != 1 && p != q) RES[base + q + (long)p * ld] = x * hRES;
 }
 
 }  // namespace
 
 int launch_cc_forward(imsrg_basis *b, const double *L, int hL, const double *R, int hR) {
-  long n = 2 * b->cc_total;
+  long n = b->cc_total;
   if (n == 0) return IMSRG_OK;
   ProfScope ps(b, IMSRG_KERNEL_CC_FORWARD);
   k_cc_forward<<<(unsigned)((n + 255) / 256), 256, 0, b->stream>>>(b->T, L, hL, R, hR, b->lcc, b->rcc);
@@ -502,23 +519,26 @@ int launch_gemm_fp64(imsrg_basis *b, const double *L, int hL, const double *R, i
   return cuda_status(cudaGetLastError());
 }
 
-int launch_assemble_2body(imsrg_basis *b, const double *L, int hL, const double *R, int hR, double *RES, int hRES) {
+int launch_assemble_2body(imsrg_basis *b, const double *L, int hL, const double *R, int hR, double *RES, int hRES,
+                          int with_e0) {
   long off2b = b->off_fpp + (long)b->P * b->P;
-  long n = b->nfull - off2b;
+  long n = b->T.n_asm2;
   if (n <= 0) return IMSRG_OK;
   ProfScope ps(b, IMSRG_KERNEL_ASSEMBLE_2BODY);
+  double *e0p = (with_e0 && hL * hR == -1) ? b->partials : nullptr;
   k_assemble_2body<<<(unsigned)((n + 255) / 256), 256, 0, b->stream>>>(b->T, L, hL, R, hR, b->w1, b->w2, b->wcc, RES,
-                                                                      hRES, off2b);
+                                                                      hRES, off2b, e0p);
   b->launches++;
   return cuda_status(cudaGetLastError());
 }
 
 int launch_assemble_1body(imsrg_basis *b, const double *L, int hL, const double *R, int hR, double *RES, int hRES,
                           int with_e0) {
-  long nel = (long)b->A * b->A + (long)b->P * b->A + (long)b->P * b->P;
-  int nblk = (int)((nel + 7) / 8);
+  const int grid = b->T.n_asm1_heavy + (b->T.n_asm1_light + 3) / 4 + 1;
   ProfScope ps(b, IMSRG_KERNEL_ASSEMBLE_1BODY);
-  k_assemble_1body<<<nblk + 1, 256, 0, b->stream>>>(b->T, L, hL, R, hR, b->w1, b->w2, RES, hRES, with_e0, nblk);
+  const bool e220 = with_e0 && hL * hR == -1;
+  k_assemble_1body<<<grid, 128, 0, b->stream>>>(b->T, L, hL, R, hR, b->w1, b->w2, RES, hRES, with_e0,
+                                                e220 ? b->partials : nullptr, (b->T.n_asm2 + 255) / 256);
   b->launches++;
   return cuda_status(cudaGetLastError());
 }
@@ -528,7 +548,7 @@ int launch_assemble_1body(imsrg_basis *b, const double *L, int hL, const double 
 // nothing and records no profiling events.
 int launch_commutator_fp64_ws(imsrg_basis *b, const Workspace &ws, const double *L, int hL, const double *R, int hR,
                               double *RES, int hRES, int with_e0, cudaStream_t st) {
-  long ncc = 2 * b->cc_total;
+  long ncc = b->cc_total;
   if (ncc > 0) {
     k_cc_forward<<<(unsigned)((ncc + 255) / 256), 256, 0, st>>>(b->T, L, hL, R, hR, ws.lcc, ws.rcc);
     b->launches++;
@@ -549,15 +569,17 @@ int launch_commutator_fp64_ws(imsrg_basis *b, const Workspace &ws, const double 
     b->launches++;
   }
   long off2b = b->off_fpp + (long)b->P * b->P;
-  long n2 = b->nfull - off2b;
+  long n2 = b->T.n_asm2;
   if (n2 > 0) {
+    double *e0p = (with_e0 && hL * hR == -1) ? ws.e0p : nullptr;
     k_assemble_2body<<<(unsigned)((n2 + 255) / 256), 256, 0, st>>>(b->T, L, hL, R, hR, ws.w1, ws.w2, ws.wcc, RES,
-                                                                   hRES, off2b);
+                                                                   hRES, off2b, e0p);
     b->launches++;
   }
-  long nel = (long)b->A * b->A + (long)b->P * b->A + (long)b->P * b->P;
-  int nblk = (int)((nel + 7) / 8);
-  k_assemble_1body<<<nblk + 1, 256, 0, st>>>(b->T, L, hL, R, hR, ws.w1, ws.w2, RES, hRES, with_e0, nblk);
+  const int grid1 = b->T.n_asm1_heavy + (b->T.n_asm1_light + 3) / 4 + 1;
+  const bool e220 = with_e0 && hL * hR == -1;
+  k_assemble_1body<<<grid1, 128, 0, st>>>(b->T, L, hL, R, hR, ws.w1, ws.w2, RES, hRES, with_e0,
+                                          e220 ? ws.e0p : nullptr, (b->T.n_asm2 + 255) / 256);
   b->launches++;
   return cuda_status(cudaGetLastError());
 }

@@ -17,18 +17,24 @@
 //      swizzle), once with the second index contiguous (R image) and once with
 //      the first (C image), so every transposition of every use is K-major.
 //   3. k_oz_mma: persistent kernel, one 128 x 64 output tile at a time.  A
-//      producer thread streams the six A and six B digit planes of each
-//      K = 16 step into shared memory with cp.async.bulk; one thread issues
-//      the 21 tcgen05.mma products d_s x d_t with s + t <= 7 into six FP32
-//      accumulators in TMEM (one per level l = s + t), negating A for terms
-//      with coefficient -1; four epilogue warps read the levels back
-//      (tcgen05.ld), combine them exactly in int64 and write FP64.
+//      producer thread streams the six A digit planes and fifteen B planes
+//      (d_1..d_6, 2^7 d_1..d_5, 2^14 d_1..d_4) of each K = 16 step into
+//      shared memory with cp.async.bulk; one thread issues the 21
+//      tcgen05.mma products d_s x d_t with s + t <= 7 (negating A for terms
+//      with coefficient -1) into four FP32 accumulators in TMEM: one per
+//      level l = s + t = 2, 3, 4 and one "tail" that sums levels 5, 6, 7 in
+//      units of level 7 (the pre-scaled B planes supply 128^(7 - l)).  The
+//      accumulators are double-buffered (2 x 4 x 64 = 512 columns) so the
+//      eight epilogue warps read one tile (tcgen05.ld), combine it in int64
+//      and write FP64 while the next tile's products run.
 //
-// Exactness: level l sums at most 2 terms x K products bounded by
-// 2^12 (l + 1), so every FP32 accumulator holds an exact integer below 2^24
-// while 2 K (l + 1) 2^12 < 2^24 (checked per problem when the plan is built).
-// The result differs from the exact product only by the dropped levels
-// (s + t >= 8) and the digit rounding: about 2^-42 K max|A| max|B|.
+// Exactness: the level sums of levels 2..4 are bounded by 5 * 2^12 per
+// product and term, so those accumulators hold exact integers below 2^24
+// while nterms K 5 2^12 < 2^24 (checked per problem when the plan is built).
+// The tail is rounded to FP32 (relative 2^-24 of a quantity 2^-14 below the
+// leading level).  The result differs from the exact product by the dropped
+// levels (s + t >= 8), the digit rounding and the tail rounding: about
+// 2^-42 K max|A| max|B|.
 //
 // Every mbarrier wait is bounded (about 2 s of %globaltimer); a timeout sets
 // an error flag that the host reports as IMSRG_ERR_TIMEOUT.
@@ -45,14 +51,17 @@ namespace {
 
 constexpr int OZ_S = 6;                      // digits (slices) per operand
 constexpr int OZ_LMAX = OZ_S + 1;            // highest level kept
-constexpr int OZ_NLEV = OZ_LMAX - 1;         // levels 2 .. 7
+constexpr int OZ_NACC = 4;                   // accumulators: levels 2, 3, 4 exact + FP32 tail of 5..7
+constexpr int OZ_BPLANES = 15;               // B planes: d_1..d_6, 2^7 d_1..d_5, 2^14 d_1..d_4
 constexpr int TM = 128, TN = 64, TK = 16;
 constexpr int STAGES = 4;
 constexpr int A_SLICE_BYTES = TM * TK * 2;   // 4096
 constexpr int B_SLICE_BYTES = TN * TK * 2;   // 2048
-constexpr int STAGE_BYTES = OZ_S * (A_SLICE_BYTES + B_SLICE_BYTES);
+constexpr int STAGE_BYTES = OZ_S * A_SLICE_BYTES + OZ_BPLANES * B_SLICE_BYTES;
 constexpr int TMEM_COLS = 512;
-constexpr int OZ_THREADS = 192;              // warp 0 producer, 1 MMA, 2-5 epilogue
+constexpr int EPI_WARPS = 16;                // one per (TMEM lane quadrant, 16-column chunk)
+constexpr int OZ_THREADS = 32 * (2 + EPI_WARPS);  // warp 0 producer, 1 MMA, 2-17 epilogue
+constexpr int ACC_BUF_COLS = OZ_NACC * TN;   // two accumulator sets fill the 512 columns
 constexpr unsigned long long WAIT_NS = 2000000000ull;
 
 struct OzMatrix {
@@ -60,16 +69,19 @@ struct OzMatrix {
   int group;       // exponent group
   long off;        // element offset in the source buffer
   int n1, n2;      // column-major shape
-  long img_r;      // byte offset of the R image (rows n1, K = n2) in the source's image buffer
-  long img_c;      // byte offset of the C image (rows n2, K = n1)
-  int rg_r, rg_c;  // row groups (of 8) of each image, padded to 16
+  long img_r;      // byte offset of the R image (rows n1, K = n2), -1 when no problem reads it
+  long img_c;      // byte offset of the C image (rows n2, K = n1), -1 when no problem reads it
+  int rg_r, rg_c;  // row groups (of 8 rows) of each image
   long plane_r, plane_c;  // bytes per digit plane
-  int tile0;       // first 8x8 core tile of this matrix in the slicing grid
+  int np_r, np_c;         // digit planes stored: 6 (A role only) or 15 (B role: with the scaled tail planes)
+  int line_r0, line_c0;   // first line of this matrix in the R / C slicing grids
 };
 
-struct OzGroup {
-  int src;
-  long off, len;
+// A contiguous chunk of one exponent group's elements.
+struct OzChunk {
+  int group, src;
+  long off;
+  int len;
 };
 
 struct OzTerm {
@@ -90,16 +102,19 @@ struct OzProb {
 
 struct OzPlan {
   std::vector<OzMatrix> mats;
-  std::vector<OzGroup> groups;
+  std::vector<OzChunk> chunks;
   std::vector<OzProb> probs;
   OzMatrix *d_mats = nullptr;
-  OzGroup *d_groups = nullptr;
+  OzChunk *d_chunks = nullptr;
   OzProb *d_probs = nullptr;
-  int *d_exps = nullptr;
+  int *d_sched = nullptr;      // tile ids, grouped by CTA
+  int *d_sched_off = nullptr;  // [grid + 1] start of each CTA's list
+  int *d_exps = nullptr;       // per group: max biased exponent (e = value - 1022)
   int *d_err = nullptr;
   uint8_t *img[4] = {nullptr, nullptr, nullptr, nullptr};
   long img_bytes[4] = {0, 0, 0, 0};
-  int nmats = 0, ngroups = 0, nprobs = 0, ntiles = 0, ncore = 0;
+  int nmats = 0, ngroups = 0, nchunks = 0, nprobs = 0, ntiles = 0;
+  int lines_r = 0, lines_c = 0;
   int grid = 0;
   bool ok = false;
 };
@@ -203,31 +218,31 @@ __device__ __forceinline__ void tmem_ld16(uint32_t taddr, uint32_t *r) {
 __device__ __forceinline__ void tmem_ld_wait() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
 
 // ---------------------------------------------------------------------------
-// 1. block exponents
+// 1. block exponents: max biased exponent of each group (integer atomicMax,
+//    order-independent, so the result is deterministic)
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(256) k_oz_exponents(const OzGroup *groups, const double *L, const double *R,
+__global__ void __launch_bounds__(256) k_oz_exponents(const OzChunk *chunks, const double *L, const double *R,
                                                       const double *LCC, const double *RCC, int *exps) {
   __shared__ int sh[8];
-  OzGroup g = groups[blockIdx.x];
-  const double *src = g.src == 0 ? L : g.src == 1 ? R : g.src == 2 ? LCC : RCC;
+  OzChunk c = chunks[blockIdx.x];
+  const double *src = (c.src == 0 ? L : c.src == 1 ? R : c.src == 2 ? LCC : RCC) + c.off;
   int m = 0;
-  for (long i = threadIdx.x; i < g.len; i += blockDim.x) {
-    int E = (int)((__double_as_longlong(src[g.off + i]) >> 52) & 0x7FF);
-    m = max(m, E);
-  }
+  for (int i = threadIdx.x; i < c.len; i += blockDim.x)
+    m = max(m, (int)((__double_as_longlong(src[i]) >> 52) & 0x7FF));
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) m = max(m, __shfl_xor_sync(0xffffffffu, m, o));
   if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = m;
   __syncthreads();
   if (threadIdx.x == 0) {
     for (int w = 1; w < (int)(blockDim.x >> 5); w++) m = max(m, sh[w]);
-    exps[blockIdx.x] = m - 1022;  // |x| < 2^(E - 1022) for biased exponent E
+    atomicMax(&exps[c.group], m);
   }
 }
 
 // ---------------------------------------------------------------------------
-// 2. digit slicing, one 8 x 8 core tile per thread
+// 2. digit slicing: one thread per 8-element line of a core matrix
 // ---------------------------------------------------------------------------
+// Digits of x with |x| < 2^e: x = 2^(e-42) sum_{s} d_s 128^(5-s), d_0 first.
 __device__ __forceinline__ void digits6(double x, int e, int *d) {
   unsigned long long bits = (unsigned long long)__double_as_longlong(x);
   int E = (int)((bits >> 52) & 0x7FF);
@@ -251,80 +266,78 @@ __device__ __forceinline__ void digits6(double x, int e, int *d) {
   d[0] = neg ? -(int)V : (int)V;
 }
 
-__device__ __forceinline__ uint16_t bf16_bits(int v) {
+__device__ __forceinline__ uint32_t bf16_bits(int v) {
   __nv_bfloat16 h = __float2bfloat16_rn((float)v);
   return *reinterpret_cast<uint16_t *>(&h);
 }
 
-__global__ void __launch_bounds__(256) k_oz_slice(const OzMatrix *mats, int nmats, int ncore, const double *L,
-                                                  const double *R, const double *LCC, const double *RCC,
-                                                  const int *exps, uint8_t *imgL, uint8_t *imgR, uint8_t *imgLCC,
-                                                  uint8_t *imgRCC) {
-  int t = blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= ncore) return;
+__device__ __forceinline__ int find_mat(const OzMatrix *mats, int nmats, int t, bool cimg) {
   int lo = 0, hi = nmats;
   while (lo < hi) {
     int mid = (lo + hi) >> 1;
-    if (mats[mid].tile0 <= t) lo = mid + 1;
+    if ((cimg ? mats[mid].line_c0 : mats[mid].line_r0) <= t) lo = mid + 1;
     else hi = mid;
   }
-  const OzMatrix &m = mats[lo - 1];
-  int lt = t - m.tile0;
-  int RG = (m.n1 + 7) / 8;
-  int rg = lt % RG, cg = lt / RG;
+  return lo - 1;
+}
+
+// Threads [0, lines_c) write C-image lines (8 consecutive rows of one column:
+// one 16-byte row of a C core matrix per digit plane); threads
+// [lines_c, lines_c + lines_r) write R-image lines (8 consecutive columns of
+// one row).  Padding lines of the images are never written and stay zero.
+__global__ void __launch_bounds__(256) k_oz_slice(const OzMatrix *mats, int nmats, int lines_c, int lines_r,
+                                                  const double *L, const double *R, const double *LCC,
+                                                  const double *RCC, const int *exps, uint8_t *imgL,
+                                                  uint8_t *imgR, uint8_t *imgLCC, uint8_t *imgRCC) {
+  int t = blockIdx.x * blockDim.x + threadIdx.x;
+  bool cimg = t < lines_c;
+  if (!cimg) t -= lines_c;
+  if (t >= (cimg ? lines_c : lines_r)) return;
+  const OzMatrix &m = mats[find_mat(mats, nmats, t, cimg)];
   const double *src = (m.src == 0 ? L : m.src == 1 ? R : m.src == 2 ? LCC : RCC) + m.off;
   uint8_t *img = m.src == 0 ? imgL : m.src == 1 ? imgR : m.src == 2 ? imgLCC : imgRCC;
-  int e = exps[m.group];
-  int r0 = rg * 8, c0 = cg * 8;
-  // R image: core matrix (rg, cg) holds rows r0.., cols c0.. with columns contiguous
-  long offR = m.img_r + ((long)((cg >> 1) * m.rg_r + rg) * 2 + (cg & 1)) * 128;
-  // C image: core matrix (cg, rg) holds the transpose
-  long offC = m.img_c + ((long)((rg >> 1) * m.rg_c + cg) * 2 + (rg & 1)) * 128;
-  // pass 1, by columns of the tile: rows of the C image
-  for (int j = 0; j < 8; j++) {
-    uint16_t row[OZ_S][8];
-    int c = c0 + j;
+  int e = exps[m.group] - 1022;
+  double x[8];
+  long off;
+  long plane;
+  if (cimg) {
+    int RG = (m.n1 + 7) >> 3;
+    int l = t - m.line_c0;
+    int rg = l % RG, c = l / RG;
 #pragma unroll
     for (int i = 0; i < 8; i++) {
-      int r = r0 + i;
-      double x = (r < m.n1 && c < m.n2) ? src[r + (long)c * m.n1] : 0.0;
-      int d[OZ_S];
-      digits6(x, e, d);
-#pragma unroll
-      for (int s = 0; s < OZ_S; s++) row[s][i] = bf16_bits(d[s]);
+      int r = rg * 8 + i;
+      x[i] = r < m.n1 ? src[r + (long)c * m.n1] : 0.0;
     }
-#pragma unroll
-    for (int s = 0; s < OZ_S; s++) {
-      uint4 v;
-      v.x = row[s][0] | ((uint32_t)row[s][1] << 16);
-      v.y = row[s][2] | ((uint32_t)row[s][3] << 16);
-      v.z = row[s][4] | ((uint32_t)row[s][5] << 16);
-      v.w = row[s][6] | ((uint32_t)row[s][7] << 16);
-      *reinterpret_cast<uint4 *>(img + offC + s * m.plane_c + j * 16) = v;
-    }
-  }
-  // pass 2, by rows of the tile: rows of the R image
-  for (int i = 0; i < 8; i++) {
-    uint16_t row[OZ_S][8];
-    int r = r0 + i;
+    off = m.img_c + ((long)((rg >> 1) * m.rg_c + (c >> 3)) * 2 + (rg & 1)) * 128 + (c & 7) * 16;
+    plane = m.plane_c;
+  } else {
+    int l = t - m.line_r0;
+    int r = l % m.n1, cg = l / m.n1;
 #pragma unroll
     for (int j = 0; j < 8; j++) {
-      int c = c0 + j;
-      double x = (r < m.n1 && c < m.n2) ? src[r + (long)c * m.n1] : 0.0;
-      int d[OZ_S];
-      digits6(x, e, d);
-#pragma unroll
-      for (int s = 0; s < OZ_S; s++) row[s][j] = bf16_bits(d[s]);
+      int c = cg * 8 + j;
+      x[j] = c < m.n2 ? src[r + (long)c * m.n1] : 0.0;
     }
+    off = m.img_r + ((long)((cg >> 1) * m.rg_r + (r >> 3)) * 2 + (cg & 1)) * 128 + (r & 7) * 16;
+    plane = m.plane_r;
+  }
+  const int nplanes = cimg ? m.np_c : m.np_r;
+  int d[8][OZ_S];
 #pragma unroll
-    for (int s = 0; s < OZ_S; s++) {
-      uint4 v;
-      v.x = row[s][0] | ((uint32_t)row[s][1] << 16);
-      v.y = row[s][2] | ((uint32_t)row[s][3] << 16);
-      v.z = row[s][4] | ((uint32_t)row[s][5] << 16);
-      v.w = row[s][6] | ((uint32_t)row[s][7] << 16);
-      *reinterpret_cast<uint4 *>(img + offR + s * m.plane_r + i * 16) = v;
-    }
+  for (int i = 0; i < 8; i++) digits6(x[i], e, d[i]);
+  // plane k: digit s = k (k < 6), 2^7 d_{k-6} (6 <= k < 11), 2^14 d_{k-11} (k >= 11);
+  // all exact in BF16
+#pragma unroll
+  for (int k = 0; k < OZ_BPLANES; k++) {
+    if (k >= nplanes) break;
+    const int s = k < 6 ? k : k < 11 ? k - 6 : k - 11;
+    const int sh = k < 6 ? 0 : k < 11 ? 7 : 14;
+    uint32_t w4[4];
+#pragma unroll
+    for (int i = 0; i < 8; i += 2)
+      w4[i >> 1] = bf16_bits(d[i][s] * (1 << sh)) | (bf16_bits(d[i + 1][s] * (1 << sh)) << 16);
+    *reinterpret_cast<uint4 *>(img + off + k * plane) = make_uint4(w4[0], w4[1], w4[2], w4[3]);
   }
 }
 
@@ -341,28 +354,41 @@ __device__ __forceinline__ int find_prob(const OzProb *probs, int nprobs, int ti
   return lo - 1;
 }
 
-__global__ void __launch_bounds__(OZ_THREADS, 1) k_oz_mma(const OzProb *__restrict__ probs, int nprobs, int ntiles,
+__global__ void __launch_bounds__(OZ_THREADS, 1) k_oz_mma(const OzProb *__restrict__ probs, int nprobs,
+                                                          const int *__restrict__ sched,
+                                                          const int *__restrict__ sched_off,
                                                           const int *__restrict__ exps, int hL, int hR, int *err) {
   extern __shared__ __align__(1024) uint8_t smem_raw[];
   uint8_t *smem = (uint8_t *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
   uint64_t *full = (uint64_t *)(smem + STAGES * STAGE_BYTES);
   uint64_t *empty = full + STAGES;
-  uint64_t *acc_full = empty + STAGES;
-  uint64_t *acc_empty = acc_full + 1;
-  uint32_t *tmem_slot = (uint32_t *)(acc_empty + 1);
+  uint64_t *acc_full = empty + STAGES;   // [2]
+  uint64_t *acc_empty = acc_full + 2;    // [2]
+  uint32_t *tmem_slot = (uint32_t *)(acc_empty + 2);
   volatile int *abort_flag = (volatile int *)(tmem_slot + 1);
   int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  // this CTA's tiles (longest first, assigned on the host)
+  const int t_begin = sched_off[blockIdx.x], t_end = sched_off[blockIdx.x + 1];
 
   if (threadIdx.x == 0) {
     for (int s = 0; s < STAGES; s++) {
       mbar_init(&full[s], 1);
       mbar_init(&empty[s], 1);
     }
-    mbar_init(acc_full, 1);
-    mbar_init(acc_empty, 4);
+    for (int b = 0; b < 2; b++) {
+      mbar_init(&acc_full[b], 1);
+      mbar_init(&acc_empty[b], EPI_WARPS);
+    }
     *abort_flag = 0;
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
+  // Tiles copy only the row groups that exist; the rows of a stage past M (or
+  // N) keep digits of an earlier tile, which only reach accumulator rows (or
+  // columns) that are never stored.  Zeroing the stages once keeps those rows
+  // finite from the start.
+  for (int i = threadIdx.x; i < STAGES * STAGE_BYTES / 16; i += blockDim.x)
+    reinterpret_cast<uint4 *>(smem)[i] = make_uint4(0u, 0u, 0u, 0u);
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
   if (warp == 1) {
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_slot)),
                  "r"(TMEM_COLS)
@@ -379,29 +405,35 @@ __global__ void __launch_bounds__(OZ_THREADS, 1) k_oz_mma(const OzProb *__restri
       // producer: digit planes of A and B for every K step
       int stage = 0;
       uint32_t phase = 0;
-      for (int tile = blockIdx.x; tile < ntiles && !*abort_flag; tile += gridDim.x) {
+      for (int ti = t_begin; ti < t_end && !*abort_flag; ti++) {
+        int tile = sched[ti];
         const OzProb &P = probs[find_prob(probs, nprobs, tile)];
         if (P.ksteps == 0) continue;
         int lt = tile - P.tile0;
         int tm = lt % P.tiles_m, tn = lt / P.tiles_m;
         for (int it = 0; it < P.nterms; it++) {
           const OzTerm &T = P.t[it];
+          // row groups of this tile present in the images (the rest of the stage is not read back)
+          const uint32_t a_bytes = (uint32_t)min(TM / 8, T.a_rg - tm * (TM / 8)) * 256u;
+          const uint32_t b_bytes = (uint32_t)min(TN / 8, T.b_rg - tn * (TN / 8)) * 256u;
           for (int kk = 0; kk < P.ksteps; kk++) {
             if (!mbar_wait(&empty[stage], phase ^ 1, abort_flag)) {
               atomicExch(err, 1);
               *abort_flag = 1;
               break;
             }
-            mbar_expect_tx(&full[stage], STAGE_BYTES);
+            mbar_expect_tx(&full[stage], OZ_S * a_bytes + OZ_BPLANES * b_bytes);
             uint8_t *sa = smem + stage * STAGE_BYTES;
             uint8_t *sb = sa + OZ_S * A_SLICE_BYTES;
-            const uint8_t *ga = T.a_img + ((long)kk * T.a_rg + tm * 16) * 256;
-            const uint8_t *gb = T.b_img + ((long)kk * T.b_rg + tn * 8) * 256;
+            const uint8_t *ga = T.a_img + ((long)kk * T.a_rg + tm * (TM / 8)) * 256;
+            const uint8_t *gb = T.b_img + ((long)kk * T.b_rg + tn * (TN / 8)) * 256;
 #pragma unroll
             for (int s = 0; s < OZ_S; s++) {
-              bulk_g2s(sa + s * A_SLICE_BYTES, ga + s * T.a_plane, A_SLICE_BYTES, &full[stage]);
-              bulk_g2s(sb + s * B_SLICE_BYTES, gb + s * T.b_plane, B_SLICE_BYTES, &full[stage]);
+              bulk_g2s(sa + s * A_SLICE_BYTES, ga + s * T.a_plane, a_bytes, &full[stage]);
             }
+#pragma unroll
+            for (int k = 0; k < OZ_BPLANES; k++)
+              bulk_g2s(sb + k * B_SLICE_BYTES, gb + k * T.b_plane, b_bytes, &full[stage]);
             if (++stage == STAGES) {
               stage = 0;
               phase ^= 1;
@@ -413,24 +445,29 @@ __global__ void __launch_bounds__(OZ_THREADS, 1) k_oz_mma(const OzProb *__restri
     }
   } else if (warp == 1) {
     if (lane == 0) {
-      // MMA issuer
-      int stage = 0;
-      uint32_t phase = 0, aphase = 0;
-      for (int tile = blockIdx.x; tile < ntiles && !*abort_flag; tile += gridDim.x) {
-        const OzProb &P = probs[find_prob(probs, nprobs, tile)];
+      // MMA issuer: alternates between the two accumulator sets so the next
+      // tile's products overlap the epilogue of the previous one
+      int stage = 0, nt = 0;
+      uint32_t phase = 0;
+      for (int ti = t_begin; ti < t_end && !*abort_flag; ti++) {
+        const OzProb &P = probs[find_prob(probs, nprobs, sched[ti])];
         if (P.ksteps == 0) continue;
-        if (!mbar_wait(acc_empty, aphase ^ 1, abort_flag)) {
+        int buf = nt & 1;
+        uint32_t use = (uint32_t)(nt >> 1);
+        nt++;
+        if (!mbar_wait(&acc_empty[buf], (use & 1) ^ 1, abort_flag)) {
           atomicExch(err, 2);
           *abort_flag = 1;
           break;
         }
-        aphase ^= 1;
         tc_fence_after();
-        uint32_t started = 0;
+        const uint32_t dbase = tmem + (uint32_t)(buf * ACC_BUF_COLS);
+        bool first = true;  // first K step of the tile overwrites the accumulators
+        const uint64_t desc0 = smem_desc(smem_u32(smem), 128, 256);
         for (int it = 0; it < P.nterms && !*abort_flag; it++) {
           const OzTerm &T = P.t[it];
           int neg = T.neg ^ (T.use_hl & (hL < 0)) ^ (T.use_hr & (hR < 0));
-          uint32_t idesc = idesc_bf16(TM, TN, neg);
+          const uint32_t idesc = idesc_bf16(TM, TN, neg);
           for (int kk = 0; kk < P.ksteps; kk++) {
             if (!mbar_wait(&full[stage], phase, abort_flag)) {
               atomicExch(err, 3);
@@ -438,21 +475,25 @@ __global__ void __launch_bounds__(OZ_THREADS, 1) k_oz_mma(const OzProb *__restri
               break;
             }
             tc_fence_after();
-            uint32_t sa = smem_u32(smem + stage * STAGE_BYTES);
-            uint32_t sb = sa + OZ_S * A_SLICE_BYTES;
+            // descriptor start-address fields advance in 16-byte units
+            const uint64_t da = desc0 + (uint64_t)((stage * STAGE_BYTES) >> 4);
+            const uint64_t db = da + (uint64_t)((OZ_S * A_SLICE_BYTES) >> 4);
 #pragma unroll
             for (int s = 0; s < OZ_S; s++) {
 #pragma unroll
-              for (int u = 0; u < OZ_S; u++) {
-                int lvl = s + u + 2;  // digits are 1-based in the level count
-                if (lvl > OZ_LMAX) continue;
-                uint64_t ad = smem_desc(sa + s * A_SLICE_BYTES, 128, 256);
-                uint64_t bd = smem_desc(sb + u * B_SLICE_BYTES, 128, 256);
-                int acc = (started >> lvl) & 1;
-                started |= 1u << lvl;
-                mma_bf16(tmem + (uint32_t)((lvl - 2) * TN), ad, bd, idesc, acc);
+              for (int u = 0; u < OZ_S - s; u++) {
+                // level l = s + u + 2 (digits are 1-based): levels 2..4 have
+                // their own accumulator; 5..7 share the tail accumulator, with
+                // B pre-scaled by 2^(7 (7 - l)); the first product of every
+                // accumulator in a tile (s = 0, u <= 3) overwrites it
+                const int lvl = s + u + 2;
+                const int acc_i = lvl <= 4 ? lvl - 2 : 3;
+                const int bp = lvl <= 4 || lvl == 7 ? u : lvl == 6 ? 6 + u : 11 + u;
+                mma_bf16(dbase + (uint32_t)(acc_i * TN), da + (uint64_t)(s * (A_SLICE_BYTES >> 4)),
+                         db + (uint64_t)(bp * (B_SLICE_BYTES >> 4)), idesc, (first && s == 0 && u <= 3) ? 0 : 1);
               }
             }
+            first = false;
             mma_commit(&empty[stage]);
             if (++stage == STAGES) {
               stage = 0;
@@ -460,64 +501,82 @@ __global__ void __launch_bounds__(OZ_THREADS, 1) k_oz_mma(const OzProb *__restri
             }
           }
         }
-        mma_commit(acc_full);
+        mma_commit(&acc_full[buf]);
       }
     }
   } else {
-    // epilogue warps 2..5: TMEM lane quadrant = warp % 4
-    int quad = warp & 3;
-    int row = quad * 32 + lane;
-    uint32_t aphase = 0;
-    for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+    // epilogue warps 2..17: TMEM lane quadrant = warp % 4 (the lanes a warp
+    // may read), 16-column chunk = (warp - 2) / 4
+    const int quad = warp & 3, chunk = (warp - 2) >> 2;
+    const int row = quad * 32 + lane;
+    int nt = 0;
+    for (int ti = t_begin; ti < t_end; ti++) {
+      int tile = sched[ti];
       const OzProb &P = probs[find_prob(probs, nprobs, tile)];
       int lt = tile - P.tile0;
-      int m = (lt % P.tiles_m) * TM + row;
-      int n0 = (lt / P.tiles_m) * TN;
-      if (P.ksteps == 0) {
-        if (m < P.M)
-          for (int c = 0; c < TN && n0 + c < P.N; c++) P.C[m + (long)(n0 + c) * P.ldc] = 0.0;
+      // problem fields in registers: the stores below could alias the problem
+      // table as far as the compiler knows, which would force a reload per column
+      const int Mp = P.M, Np = P.N, ldc = P.ldc, ksteps = P.ksteps, gA = P.gA, gB = P.gB;
+      const int tiles_m = P.tiles_m;
+      double *const Cbase = P.C;
+      const int m0 = (lt % tiles_m) * TM;
+      const int m = m0 + row;
+      const int n0 = (lt / tiles_m) * TN + 16 * chunk;
+      const bool row_ok = m < Mp;
+      double *crow = Cbase + m;
+      if (ksteps == 0) {
+        if (row_ok)
+          for (int c = 0; c < 16 && n0 + c < Np; c++) crow[(long)(n0 + c) * ldc] = 0.0;
         continue;
       }
+      int buf = nt & 1;
+      uint32_t use = (uint32_t)(nt >> 1);
+      nt++;
       if (*abort_flag) break;
-      if (!mbar_wait(acc_full, aphase, abort_flag)) {
+      if (!mbar_wait(&acc_full[buf], use & 1, abort_flag)) {
         atomicExch(err, 4);
         *abort_flag = 1;
         break;
       }
-      aphase ^= 1;
       tc_fence_after();
-      int k = exps[P.gA] + exps[P.gB] - 7 * OZ_LMAX;  // result = v * 2^k
-      for (int cc = 0; cc < TN; cc += 16) {
-        uint32_t acc[OZ_NLEV][16];
+      // warp-uniform: a piece entirely past M or N is neither read nor converted
+      const bool live = m0 + quad * 32 < Mp && n0 < Np;
+      uint32_t acc[OZ_NACC][16];
+      if (live) {
 #pragma unroll
-        for (int l = 0; l < OZ_NLEV; l++)
-          tmem_ld16(tmem + ((uint32_t)(quad * 32) << 16) + (uint32_t)(l * TN + cc), acc[l]);
-        tmem_ld_wait();
-#pragma unroll
-        for (int c = 0; c < 16; c++) {
-          long long v = 0;
-#pragma unroll
-          for (int l = 0; l < OZ_NLEV; l++) {
-            long long cl = (long long)__float2int_rn(__uint_as_float(acc[l][c]));
-            v += cl << (7 * (OZ_LMAX - 2 - l));
-          }
-          double d = (double)v;
-          // scale by 2^k: add k to the exponent field on the integer pipe
-          unsigned long long bits = (unsigned long long)__double_as_longlong(d);
-          int E = (int)((bits >> 52) & 0x7FF);
-          if (E != 0 && E + k > 0 && E + k < 2047) {
-            bits += (unsigned long long)(long long)k << 52;
-            d = __longlong_as_double((long long)bits);
-          } else if (E != 0) {
-            d = ldexp(d, k);
-          }
-          int n = n0 + cc + c;
-          if (m < P.M && n < P.N) P.C[m + (long)n * P.ldc] = d;
-        }
+        for (int l = 0; l < OZ_NACC; l++)
+          tmem_ld16(tmem + ((uint32_t)(quad * 32) << 16) + (uint32_t)(buf * ACC_BUF_COLS + l * TN + 16 * chunk),
+                    acc[l]);
       }
+      tmem_ld_wait();
+      // the accumulators are in registers: hand the TMEM set back to the MMA issuer
       tc_fence_before();
       __syncwarp();
-      if (lane == 0) mbar_arrive(acc_empty);
+      if (lane == 0) mbar_arrive(&acc_empty[buf]);
+      if (!live) continue;
+      const int k = (exps[gA] - 1022) + (exps[gB] - 1022) - 7 * OZ_LMAX;  // result = v * 2^k
+#pragma unroll
+      for (int c = 0; c < 16; c++) {
+        // exact integer levels 2..4 and the rounded tail, in units of level 7
+        // (hardware conversions: measured faster here than assembling the
+        // double from integer bit operations)
+        long long v = ((long long)__float2int_rn(__uint_as_float(acc[0][c])) << 35) +
+                      ((long long)__float2int_rn(__uint_as_float(acc[1][c])) << 28) +
+                      ((long long)__float2int_rn(__uint_as_float(acc[2][c])) << 21) +
+                      __float2ll_rn(__uint_as_float(acc[3][c]));
+        double d = (double)v;
+        // scale by 2^k: add k to the exponent field on the integer pipe
+        unsigned long long bits = (unsigned long long)__double_as_longlong(d);
+        const int E = (int)((bits >> 52) & 0x7FF);
+        if (E != 0 && E + k > 0 && E + k < 2047) {
+          bits += (unsigned long long)(long long)k << 52;
+          d = __longlong_as_double((long long)bits);
+        } else if (E != 0) {
+          d = ldexp(d, k);
+        }
+        const int n = n0 + c;
+        if (row_ok && n < Np) crow[(long)n * ldc] = d;
+      }
     }
   }
   tc_fence_before();
@@ -536,17 +595,21 @@ int ozaki_prepare(imsrg_basis *b) {
   if (b->ozaki) return plan_of(b)->ok ? IMSRG_OK : IMSRG_ERR_INVALID;
   OzPlan *pl = new OzPlan();
   b->ozaki = pl;
-  int dev = b->device, major = 0, minor = 0, nsm = 0;
+  int dev = b->device, major = 0, nsm = 0;
   IMSRG_CUDA_TRY(cudaDeviceGetAttribute(&major, cudaDevAttrComputeCapabilityMajor, dev));
-  IMSRG_CUDA_TRY(cudaDeviceGetAttribute(&minor, cudaDevAttrComputeCapabilityMinor, dev));
   IMSRG_CUDA_TRY(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
   if (major != 10) return IMSRG_ERR_INVALID;  // tcgen05 needs a Blackwell data-center part
 
-  // matrices and exponent groups: L and R per (2J,Tz,parity) block, LCC and
-  // RCC per cross-coupled block
+  // matrices: L and R arrays per (2J,Tz,parity) block (one exponent group per
+  // block), LCC and RCC per cross-coupled block (one group each)
   std::map<std::pair<int, long>, int> mat_of;  // (src, off) -> matrix index
-  long imgb[4] = {0, 0, 0, 0};
-  int ncore = 0;
+  std::vector<OzChunk> &chunks = pl->chunks;
+  int ngroups = 0;
+  auto add_group = [&](int src, long off, long len) {
+    int g = ngroups++;
+    for (long s0 = 0; s0 < len; s0 += 4096) chunks.push_back({g, src, off + s0, (int)std::min<long>(4096, len - s0)});
+    return g;
+  };
   auto add_matrix = [&](int src, int group, long off, int n1, int n2) {
     if (n1 <= 0 || n2 <= 0) return;
     OzMatrix m{};
@@ -555,50 +618,83 @@ int ozaki_prepare(imsrg_basis *b) {
     m.off = off;
     m.n1 = n1;
     m.n2 = n2;
-    m.rg_r = ((n1 + 127) / 128) * 16;
-    m.rg_c = ((n2 + 127) / 128) * 16;
-    int kc_r = (n2 + 15) / 16, kc_c = (n1 + 15) / 16;
-    m.plane_r = (long)m.rg_r * kc_r * 256;
-    m.plane_c = (long)m.rg_c * kc_c * 256;
-    m.img_r = imgb[src];
-    imgb[src] += OZ_S * m.plane_r;
-    m.img_c = imgb[src];
-    imgb[src] += OZ_S * m.plane_c;
-    m.tile0 = ncore;
-    ncore += ((n1 + 7) / 8) * ((n2 + 7) / 8);
+    m.img_r = m.img_c = -1;
     mat_of[{src, off}] = (int)pl->mats.size();
     pl->mats.push_back(m);
   };
   for (int src = 0; src < 2; src++)
     for (int q = 0; q < b->nblocks; q++) {
-      int g = (int)pl->groups.size();
       long o0 = b->gam_off[q * 6], o1 = (q + 1 < b->nblocks) ? b->gam_off[q * 6 + 6] : b->nfull;
-      pl->groups.push_back({src, o0, o1 - o0});
+      int g = add_group(src, o0, o1 - o0);
       for (int k = 0; k < 6; k++) add_matrix(src, g, b->gam_off[q * 6 + k], b->gam_n1[q * 6 + k], b->gam_n2[q * 6 + k]);
     }
   for (int src = 2; src < 4; src++)
     for (int q1 = 0; q1 < b->ccblocks; q1++) {
-      int g = (int)pl->groups.size();
       long len = (long)b->cc_rlen[q1] * b->cc_nph[q1];
-      pl->groups.push_back({src, b->cc_off[q1], len});
+      int g = add_group(src, b->cc_off[q1], len);
       add_matrix(src, g, b->cc_off[q1], b->cc_rlen[q1], b->cc_nph[q1]);
     }
-  pl->ncore = ncore;
+  pl->ngroups = ngroups;
+  pl->nchunks = (int)chunks.size();
 
-  // device buffers: images (zero padding stays zero), exponents, error flag
+  // which images each matrix needs: op(A) = X reads X's R image, X^T its C
+  // image; op(B) = Y reads Y's C image, Y^T its R image.  An image read as a B
+  // operand also carries the scaled tail planes.
+  auto img_of = [&](int gsrc) -> int {
+    return gsrc == SRC_L ? 0 : gsrc == SRC_R ? 1 : gsrc == SRC_LCC ? 2 : gsrc == SRC_RCC ? 3 : -1;
+  };
+  std::vector<int> role_r(pl->mats.size(), 0), role_c(pl->mats.size(), 0);  // 0 unused, 1 B, 2 A
+  std::vector<int> b_role_r(pl->mats.size(), 0), b_role_c(pl->mats.size(), 0);  // read as a B operand
+  for (const GemmProb &gp : b->probs) {
+    if (gp.K <= 0) continue;
+    for (int it = 0; it < gp.nterms; it++) {
+      const GemmTerm &t = gp.t[it];
+      int sa = img_of(t.a_src), sb = img_of(t.b_src);
+      if (sa < 0 || sb < 0) return IMSRG_ERR_INVALID;
+      auto ia = mat_of.find({sa, t.a_off}), ib = mat_of.find({sb, t.b_off});
+      if (ia == mat_of.end() || ib == mat_of.end()) return IMSRG_ERR_INVALID;
+      (t.ta ? role_c : role_r)[ia->second] = 2;
+      int &rb = (t.tb ? role_r : role_c)[ib->second];
+      rb = std::max(rb, 1);
+      (t.tb ? b_role_r : b_role_c)[ib->second] = 1;
+    }
+  }
+  long imgb[4] = {0, 0, 0, 0};
+  int lines_r = 0, lines_c = 0;
+  for (size_t i = 0; i < pl->mats.size(); i++) {
+    OzMatrix &m = pl->mats[i];
+    m.line_r0 = lines_r;
+    m.line_c0 = lines_c;
+    if (role_r[i]) {
+      m.rg_r = (m.n1 + 7) / 8;
+      m.plane_r = (long)m.rg_r * ((m.n2 + 15) / 16) * 256;
+      m.np_r = b_role_r[i] ? OZ_BPLANES : OZ_S;
+      m.img_r = imgb[m.src];
+      imgb[m.src] += m.np_r * m.plane_r;
+      lines_r += ((m.n2 + 7) / 8) * m.n1;
+    }
+    if (role_c[i]) {
+      m.rg_c = (m.n2 + 7) / 8;
+      m.plane_c = (long)m.rg_c * ((m.n1 + 15) / 16) * 256;
+      m.np_c = b_role_c[i] ? OZ_BPLANES : OZ_S;
+      m.img_c = imgb[m.src];
+      imgb[m.src] += m.np_c * m.plane_c;
+      lines_c += ((m.n1 + 7) / 8) * m.n2;
+    }
+  }
+  pl->lines_r = lines_r;
+  pl->lines_c = lines_c;
   for (int s = 0; s < 4; s++) {
     pl->img_bytes[s] = std::max<long>(imgb[s], 256);
     void *p = nullptr;
     IMSRG_CUDA_TRY(cudaMalloc(&p, pl->img_bytes[s]));
-    IMSRG_CUDA_TRY(cudaMemset(p, 0, pl->img_bytes[s]));
+    IMSRG_CUDA_TRY(cudaMemset(p, 0, pl->img_bytes[s]));  // padding stays zero
     pl->img[s] = (uint8_t *)p;
   }
 
   // problems: the FP64 grouped-GEMM list mapped onto images
-  auto img_of = [&](int gsrc) -> int {  // GemmTerm source id -> image source
-    return gsrc == SRC_L ? 0 : gsrc == SRC_R ? 1 : gsrc == SRC_LCC ? 2 : gsrc == SRC_RCC ? 3 : -1;
-  };
   int tiles = 0;
+  std::vector<int> tile_cost;
   for (const GemmProb &gp : b->probs) {
     OzProb p{};
     p.M = gp.M;
@@ -611,19 +707,14 @@ int ozaki_prepare(imsrg_basis *b) {
     p.ldc = gp.ldc;
     for (int it = 0; it < gp.nterms; it++) {
       const GemmTerm &t = gp.t[it];
-      int sa = img_of(t.a_src), sb = img_of(t.b_src);
-      if (sa < 0 || sb < 0) return IMSRG_ERR_INVALID;
-      auto ia = mat_of.find({sa, t.a_off}), ib = mat_of.find({sb, t.b_off});
-      if (p.K > 0 && (ia == mat_of.end() || ib == mat_of.end())) return IMSRG_ERR_INVALID;
       OzTerm &o = p.t[it];
       if (p.K > 0) {
-        const OzMatrix &A = pl->mats[ia->second], &B = pl->mats[ib->second];
-        // K-major A: op(A) = A uses the R image (K = columns), A^T the C image
-        o.a_img = pl->img[sa] + (t.ta ? A.img_c : A.img_r);
+        const OzMatrix &A = pl->mats[mat_of[{img_of(t.a_src), t.a_off}]];
+        const OzMatrix &B = pl->mats[mat_of[{img_of(t.b_src), t.b_off}]];
+        o.a_img = pl->img[A.src] + (t.ta ? A.img_c : A.img_r);
         o.a_plane = t.ta ? A.plane_c : A.plane_r;
         o.a_rg = t.ta ? A.rg_c : A.rg_r;
-        // K-major B (stored N x K): op(B) = B uses the C image, B^T the R image
-        o.b_img = pl->img[sb] + (t.tb ? B.img_r : B.img_c);
+        o.b_img = pl->img[B.src] + (t.tb ? B.img_r : B.img_c);
         o.b_plane = t.tb ? B.plane_r : B.plane_c;
         o.b_rg = t.tb ? B.rg_r : B.rg_c;
         if (it == 0) {
@@ -636,18 +727,37 @@ int ozaki_prepare(imsrg_basis *b) {
       o.use_hr = t.use_hr;
     }
     // exactness bound of the FP32 level accumulators
-    if ((double)p.nterms * p.K * (OZ_LMAX + 1) * 4096.0 >= 16777216.0) return IMSRG_ERR_INVALID;
+    // (levels 2..4 are exact integers; the tail of 5..7 is rounded FP32)
+    if ((double)p.nterms * p.K * (4 + 1) * 4096.0 >= 16777216.0) return IMSRG_ERR_INVALID;
     p.tiles_m = (p.M + TM - 1) / TM;
     p.tiles = p.tiles_m * ((p.N + TN - 1) / TN);
     p.tile0 = tiles;
     tiles += p.tiles;
+    for (int k = 0; k < p.tiles; k++) tile_cost.push_back(p.nterms * p.ksteps + 2);
     pl->probs.push_back(p);
   }
   pl->nmats = (int)pl->mats.size();
-  pl->ngroups = (int)pl->groups.size();
   pl->nprobs = (int)pl->probs.size();
   pl->ntiles = tiles;
   pl->grid = std::min(nsm, std::max(tiles, 1));
+
+  // longest-processing-time-first assignment of tiles to the persistent CTAs
+  std::vector<int> order(tiles);
+  for (int i = 0; i < tiles; i++) order[i] = i;
+  std::stable_sort(order.begin(), order.end(), [&](int a, int c) { return tile_cost[a] > tile_cost[c]; });
+  std::vector<long> load(pl->grid, 0);
+  std::vector<std::vector<int>> lists(pl->grid);
+  for (int t : order) {
+    int best = (int)(std::min_element(load.begin(), load.end()) - load.begin());
+    load[best] += tile_cost[t];
+    lists[best].push_back(t);
+  }
+  std::vector<int> sched, sched_off(pl->grid + 1, 0);
+  for (int c = 0; c < pl->grid; c++) {
+    sched_off[c] = (int)sched.size();
+    sched.insert(sched.end(), lists[c].begin(), lists[c].end());
+  }
+  sched_off[pl->grid] = (int)sched.size();
 
   auto up = [&](const void *h, size_t bytes, void **d) -> int {
     IMSRG_CUDA_TRY(cudaMalloc(d, std::max<size_t>(bytes, 16)));
@@ -655,8 +765,10 @@ int ozaki_prepare(imsrg_basis *b) {
     return IMSRG_OK;
   };
   IMSRG_TRY(up(pl->mats.data(), pl->mats.size() * sizeof(OzMatrix), (void **)&pl->d_mats));
-  IMSRG_TRY(up(pl->groups.data(), pl->groups.size() * sizeof(OzGroup), (void **)&pl->d_groups));
+  IMSRG_TRY(up(chunks.data(), chunks.size() * sizeof(OzChunk), (void **)&pl->d_chunks));
   IMSRG_TRY(up(pl->probs.data(), pl->probs.size() * sizeof(OzProb), (void **)&pl->d_probs));
+  IMSRG_TRY(up(sched.data(), sched.size() * sizeof(int), (void **)&pl->d_sched));
+  IMSRG_TRY(up(sched_off.data(), sched_off.size() * sizeof(int), (void **)&pl->d_sched_off));
   IMSRG_CUDA_TRY(cudaMalloc((void **)&pl->d_exps, std::max(pl->ngroups, 1) * sizeof(int)));
   IMSRG_CUDA_TRY(cudaMalloc((void **)&pl->d_err, sizeof(int)));
   IMSRG_CUDA_TRY(cudaMemset(pl->d_err, 0, sizeof(int)));
@@ -671,18 +783,22 @@ int ozaki_gemm(imsrg_basis *b, const double *L, int hL, const double *R, int hR)
   OzPlan *pl = plan_of(b);
   {
     ProfScope ps(b, IMSRG_KERNEL_OZAKI_SLICE);
-    k_oz_exponents<<<pl->ngroups, 256, 0, b->stream>>>(pl->d_groups, L, R, b->lcc, b->rcc, pl->d_exps);
-    k_oz_slice<<<(pl->ncore + 127) / 128, 128, 0, b->stream>>>(pl->d_mats, pl->nmats, pl->ncore, L, R, b->lcc,
-                                                                b->rcc, pl->d_exps, pl->img[0], pl->img[1],
-                                                                pl->img[2], pl->img[3]);
+    IMSRG_CUDA_TRY(cudaMemsetAsync(pl->d_exps, 0, std::max(pl->ngroups, 1) * sizeof(int), b->stream));
+    if (pl->nchunks)
+      k_oz_exponents<<<pl->nchunks, 256, 0, b->stream>>>(pl->d_chunks, L, R, b->lcc, b->rcc, pl->d_exps);
+    int lines = pl->lines_c + pl->lines_r;
+    if (lines)
+      k_oz_slice<<<(lines + 255) / 256, 256, 0, b->stream>>>(pl->d_mats, pl->nmats, pl->lines_c, pl->lines_r, L, R,
+                                                              b->lcc, b->rcc, pl->d_exps, pl->img[0], pl->img[1],
+                                                              pl->img[2], pl->img[3]);
     b->launches += 2;
   }
   IMSRG_CUDA_TRY(cudaGetLastError());
   {
     ProfScope ps(b, IMSRG_KERNEL_OZAKI_MMA);
     int smem = STAGES * STAGE_BYTES + 1024 + 256;
-    k_oz_mma<<<pl->grid, OZ_THREADS, smem, b->stream>>>(pl->d_probs, pl->nprobs, pl->ntiles, pl->d_exps, hL, hR,
-                                                       pl->d_err);
+    k_oz_mma<<<pl->grid, OZ_THREADS, smem, b->stream>>>(pl->d_probs, pl->nprobs, pl->d_sched, pl->d_sched_off,
+                                                       pl->d_exps, hL, hR, pl->d_err);
     b->launches++;
   }
   return cuda_status(cudaGetLastError());
@@ -706,8 +822,10 @@ void ozaki_free(imsrg_basis *b) {
   if (!pl) return;
   for (int s = 0; s < 4; s++) cudaFree(pl->img[s]);
   cudaFree(pl->d_mats);
-  cudaFree(pl->d_groups);
+  cudaFree(pl->d_chunks);
   cudaFree(pl->d_probs);
+  cudaFree(pl->d_sched);
+  cudaFree(pl->d_sched_off);
   cudaFree(pl->d_exps);
   cudaFree(pl->d_err);
   delete pl;
