@@ -62,17 +62,37 @@ namespace imsrg {
 int commutator_dev(imsrg_basis *b, const double *L, int hL, const double *R, int hR, double *RES, int hRES,
                    int precision, int with_e0) {
   if (precision != IMSRG_PREC_FP64 && precision != IMSRG_PREC_OZAKI) return IMSRG_ERR_INVALID;
-  if (precision == IMSRG_PREC_OZAKI) IMSRG_TRY(ozaki_prepare(b));
-  IMSRG_TRY(launch_cc_forward(b, L, hL, R, hR));
-  if (precision == IMSRG_PREC_FP64) {
-    IMSRG_TRY(launch_gemm_fp64(b, L, hL, R, hR));
-  } else if (precision == IMSRG_PREC_OZAKI) {
-    IMSRG_TRY(ozaki_gemm(b, L, hL, R, hR));
+  // Independent launches run on the side stream, forked from and joined back
+  // into the basis stream, so the call stays one ordered unit on that stream.
+  auto fork = [&](int k) -> int {
+    IMSRG_CUDA_TRY(cudaEventRecord(b->ev_fork[k], b->stream));
+    IMSRG_CUDA_TRY(cudaStreamWaitEvent(b->side, b->ev_fork[k], 0));
+    return IMSRG_OK;
+  };
+  auto join = [&](int k) -> int {
+    IMSRG_CUDA_TRY(cudaEventRecord(b->ev_join[k], b->side));
+    IMSRG_CUDA_TRY(cudaStreamWaitEvent(b->stream, b->ev_join[k], 0));
+    return IMSRG_OK;
+  };
+  if (precision == IMSRG_PREC_OZAKI) {
+    IMSRG_TRY(ozaki_prepare(b));
+    // digit images of L and R beside the Pandya transform
+    IMSRG_TRY(fork(0));
+    IMSRG_TRY(ozaki_slice(b, L, R, 0, b->side));
+    IMSRG_TRY(launch_cc_forward(b, L, hL, R, hR));
+    IMSRG_TRY(ozaki_slice(b, L, R, 1, b->stream));
+    IMSRG_TRY(join(0));
+    IMSRG_TRY(ozaki_mma(b, hL, hR));
   } else {
-    return IMSRG_ERR_INVALID;
+    IMSRG_TRY(launch_cc_forward(b, L, hL, R, hR));
+    IMSRG_TRY(launch_gemm_fp64(b, L, hL, R, hR));
   }
+  // one-body assembly beside the two-body one; E0 after both
+  IMSRG_TRY(fork(1));
+  IMSRG_TRY(launch_assemble_1body(b, L, hL, R, hR, RES, hRES, b->side));
   IMSRG_TRY(launch_assemble_2body(b, L, hL, R, hR, RES, hRES, with_e0));
-  IMSRG_TRY(launch_assemble_1body(b, L, hL, R, hR, RES, hRES, with_e0));
+  IMSRG_TRY(join(1));
+  if (with_e0) IMSRG_TRY(launch_energy(b, L, hL, R, hR, RES, hL * hR == -1));
   return IMSRG_OK;
 }
 
@@ -91,7 +111,7 @@ const char *imsrg_gpu_strerror(int s) {
     case IMSRG_ERR_TIMEOUT: return "a bounded device wait gave up";
     case IMSRG_ERR_MISMATCH: return "operators belong to different bases";
     case IMSRG_ERR_NO_DEVICE: return "no usable CUDA device";
-    case IMSRG_ERR_TOO_LARGE: return "basis too large for the fixed allocation-free workspace";
+    case IMSRG_ERR_TOO_LARGE: return "basis too large for a fixed-size table or workspace";
     default: return "unknown status";
   }
 }

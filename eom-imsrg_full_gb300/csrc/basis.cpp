@@ -352,6 +352,11 @@ int build_basis(imsrg_basis *b) {
   if (ce != cudaSuccess) return cuda_status(ce);
   IMSRG_CUDA_TRY(cudaStreamCreateWithFlags(&b->own_stream, cudaStreamNonBlocking));
   b->stream = b->own_stream;
+  IMSRG_CUDA_TRY(cudaStreamCreateWithFlags(&b->side, cudaStreamNonBlocking));
+  for (int k = 0; k < 2; k++) {
+    IMSRG_CUDA_TRY(cudaEventCreateWithFlags(&b->ev_fork[k], cudaEventDisableTiming));
+    IMSRG_CUDA_TRY(cudaEventCreateWithFlags(&b->ev_join[k], cudaEventDisableTiming));
+  }
   DevTables &T = b->T;
   T.norb = N;
   T.A = A;
@@ -406,34 +411,171 @@ int build_basis(imsrg_basis *b) {
   IMSRG_TRY(dev_upload(b, cc_colstart, &T.cc_colstart));
   IMSRG_TRY(dev_upload(b, ph_pairs, &T.ph_pairs));
 
-  // --- work orders (see DevTables::asm2_order)
+  // --- host restatement of the element locations of v_elem
+  // (basic_IMSRG.f90:1270-1385) and f_elem (:1147-1177), shared by every
+  // gather list below
+  struct HLoc {
+    long idx;   // flat index, -1 if structurally zero
+    int neg;    // pair-reordering phase
+    int nsq;    // sqrt(2) normalisation factors
+    int trans;  // read transposed (times herm)
+  };
+  auto vloc = [&](int a, int bb, int c, int d, int J2) {
+    HLoc r{-1, 0, 0, 0};
+    if (!(tri(b->jj[a], b->jj[bb], J2) && tri(b->jj[c], b->jj[d], J2))) return r;
+    int Pp = (b->ll[a] + b->ll[bb]) & 1;
+    if (((b->ll[c] + b->ll[d]) & 1) != Pp) return r;
+    int tz2 = b->itzp[a] + b->itzp[bb];
+    if (b->itzp[c] + b->itzp[d] != tz2) return r;
+    int qq = 3 * J2 + 2 * (tz2 / 2 + 1) + Pp;
+    int C1 = b->con[a] + b->con[bb] + 1, C2 = b->con[c] + b->con[d] + 1;
+    int qx = C1 * C2;
+    if (qx == 9) qx = 5;
+    int i1, i2;
+    if (a > bb) {
+      i1 = pairrow[((size_t)bb * N + a) * nJ + J2 / 2];
+      r.neg = (1 + (b->jj[a] + b->jj[bb] - J2) / 2) & 1;
+    } else {
+      r.nsq += (a == bb);
+      i1 = pairrow[((size_t)a * N + bb) * nJ + J2 / 2];
+    }
+    if (c > d) {
+      i2 = pairrow[((size_t)d * N + c) * nJ + J2 / 2];
+      r.neg ^= (1 + (b->jj[c] + b->jj[d] - J2) / 2) & 1;
+    } else {
+      r.nsq += (c == d);
+      i2 = pairrow[((size_t)c * N + d) * nJ + J2 / 2];
+    }
+    int sg = qq * 6 + qx - 1;
+    r.trans = C1 > C2;
+    r.idx = r.trans ? b->gam_off[sg] + i2 + (long)i1 * b->gam_n1[sg] : b->gam_off[sg] + i1 + (long)i2 * b->gam_n1[sg];
+    return r;
+  };
+  // f_elem: flat index and whether the element is read transposed (a ph
+  // element asked as hp takes the operator's herm)
+  auto floc = [&](int a, int bb, int *trans) -> long {
+    int ca = b->con[a], cb = b->con[bb];
+    int pa = orbpos[a], pbp = orbpos[bb];
+    *trans = 0;
+    if (ca + cb == 0) return b->off_fpp + pa + (long)pbp * P;
+    if (ca + cb == 2) return b->off_fhh + pa + (long)pbp * A;
+    if (ca > cb) {
+      *trans = 1;
+      return b->off_fph + pbp + (long)pa * P;
+    }
+    return b->off_fph + pa + (long)pbp * P;
+  };
+  auto ccr = [&](int q1, int i, int j) { return cc_row[((size_t)q1 * N + i) * N + j]; };
+  auto sixidx = [&](int j1, int j2, int J3, int j4, int j5, int J6) -> long {
+    return ((((long)(j1 >> 1) * nj + (j2 >> 1)) * nj + (j4 >> 1)) * nj + (j5 >> 1)) * nJ * nJ + (J3 >> 1) * nJ +
+           (J6 >> 1);
+  };
+
+  // --- two-body assembly: work order and gather lists (see Asm2Head)
   {
-    auto ljtn = [&](int a) { return ljt_count[a]; };
     auto jpcount = [&](int lo, int hi) { return hi >= lo ? (hi - lo) / 2 + 1 : 0; };
-    long off2b = b->off_fpp + (long)P * P;
-    std::vector<std::pair<long, int>> items;  // (signature, element)
     static const int c1tab[6] = {0, 0, 0, 1, 2, 1}, c2tab[6] = {0, 1, 2, 1, 2, 2};
+    std::vector<Asm2Head> heads;
+    std::vector<unsigned long long> terms;
+    std::vector<std::pair<long, int>> items;  // (signature, head)
+    std::vector<unsigned long long> tl;
     for (int qb = 0; qb < b->nblocks; qb++)
       for (int g = 0; g < 6; g++) {
         int n1 = b->gam_n1[qb * 6 + g], n2 = b->gam_n2[qb * 6 + g];
+        const int J2 = blk_J2[qb];
         for (int JX = 0; JX < n2; JX++)
           for (int IX = 0; IX < n1; IX++) {
             if (sq[g] && IX > JX) continue;
             const std::vector<int> &qr = b->qn[qb * 3 + c1tab[g]], &qc = b->qn[qb * 3 + c2tab[g]];
-            int i = qr[2 * IX], j = qr[2 * IX + 1], k = qc[2 * JX], l = qc[2 * JX + 1];
-            int ji = b->jj[i], jjv = b->jj[j], jk = b->jj[k], jl = b->jj[l];
-            int n_in = jpcount(std::max(std::abs(jjv - jl), std::abs(ji - jk)), std::min(jjv + jl, ji + jk));
-            int n_out = jpcount(std::max(std::abs(ji - jl), std::abs(jjv - jk)), std::min(ji + jl, jjv + jk));
-            long sig = ((((long)n_in * 32 + n_out) * 8 + ljtn(i)) * 8 + ljtn(j)) * 64 + ljtn(k) * 8 + ljtn(l);
-            items.push_back({sig, (int)(b->gam_off[qb * 6 + g] + IX + (long)JX * n1 - off2b)});
+            const int i = qr[2 * IX], j = qr[2 * IX + 1], k = qc[2 * JX], l = qc[2 * JX + 1];
+            const int ji = b->jj[i], jjv = b->jj[j], jk = b->jj[k], jl = b->jj[l];
+            Asm2Head h{};
+            h.e = (int)(b->gam_off[qb * 6 + g] + IX + (long)JX * n1);
+            h.em = sq[g] ? (int)(b->gam_off[qb * 6 + g] + JX + (long)IX * n1) : -1;
+            h.start = (int)terms.size();
+            h.J2 = J2;
+            tl.clear();
+            // commutator_122: one-body insertions on the four legs
+            auto add122 = [&](int leg_sign, int fa, int fb, const HLoc &v) {
+              if (v.idx < 0) return;
+              int ftr;
+              long fi = floc(fa, fb, &ftr);
+              tl.push_back((unsigned long long)v.idx | ((unsigned long long)fi << 28) |
+                           ((unsigned long long)(leg_sign ^ v.neg) << 48) | ((unsigned long long)v.nsq << 49) |
+                           ((unsigned long long)v.trans << 51) | ((unsigned long long)ftr << 52));
+            };
+            for (int t = 0; t < ljt_count[i]; t++) {
+              int x = ljt_list[ljt_start[i] + t];
+              add122(0, i, x, vloc(x, j, k, l, J2));
+            }
+            for (int t = 0; t < ljt_count[j]; t++) {
+              int x = ljt_list[ljt_start[j] + t];
+              add122(0, j, x, vloc(i, x, k, l, J2));
+            }
+            for (int t = 0; t < ljt_count[k]; t++) {
+              int x = ljt_list[ljt_start[k] + t];
+              add122(1, x, k, vloc(i, j, x, l, J2));
+            }
+            for (int t = 0; t < ljt_count[l]; t++) {
+              int x = ljt_list[ljt_start[l] + t];
+              add122(1, x, l, vloc(i, j, k, x, J2));
+            }
+            const int n122 = (int)tl.size();
+            // commutator_222_ph recoupling, both exchange channels
+            const int JTM = jtm;
+            int Tz1 = std::abs(b->itzp[i] - b->itzp[k]) / 2, PAR1 = (b->ll[i] + b->ll[k]) & 1;
+            int Tz2 = std::abs(b->itzp[i] - b->itzp[l]) / 2, PAR2 = (b->ll[i] + b->ll[l]) & 1;
+            bool valid = std::abs(b->itzp[l] - b->itzp[j]) == Tz1 * 2 && ((b->ll[l] + b->ll[j]) & 1) == PAR1 &&
+                         std::abs(b->itzp[k] - b->itzp[j]) == Tz2 * 2 && ((b->ll[k] + b->ll[j]) & 1) == PAR2;
+            int n_in = 0, n_out = 0;
+            auto row16 = [](int r) -> unsigned long long { return r < 0 ? 0xFFFFull : (unsigned long long)r; };
+            if (valid) {
+              int jmin = std::max(std::abs(jjv - jl), std::abs(ji - jk)), jmax = std::min(jjv + jl, ji + jk);
+              for (int JP = jmin; JP <= jmax; JP += 2, n_in++) {
+                int qx = JP / 2 + Tz1 * (JTM + 1) + 2 * PAR1 * (JTM + 1);
+                if (JP == jmin) {
+                  h.qx = qx;
+                  h.six1 = (int)sixidx(ji, jjv, J2, jl, jk, JP);
+                }
+                tl.push_back(row16(ccr(qx, k, i)) | (row16(ccr(qx, j, l)) << 16) | (row16(ccr(qx, l, j)) << 32) |
+                             (row16(ccr(qx, i, k)) << 48));
+              }
+              jmin = std::max(std::abs(ji - jl), std::abs(jjv - jk));
+              jmax = std::min(ji + jl, jjv + jk);
+              for (int JP = jmin; JP <= jmax; JP += 2, n_out++) {
+                int qx = JP / 2 + Tz2 * (JTM + 1) + 2 * PAR2 * (JTM + 1);
+                if (JP == jmin) {
+                  h.qx |= qx << 16;
+                  h.six2 = (int)sixidx(ji, jjv, J2, jk, jl, JP);
+                }
+                tl.push_back(row16(ccr(qx, l, i)) | (row16(ccr(qx, j, k)) << 16) | (row16(ccr(qx, k, j)) << 32) |
+                             (row16(ccr(qx, i, l)) << 48));
+              }
+            }
+            if (n122 > 31 || n_in > 31 || n_out > 31) return IMSRG_ERR_TOO_LARGE;
+            const int nd = (i == j) + (k == l);
+            const int n2par = (((jl + jk + J2) >> 1) + 1) & 1;
+            const int nph = ((ji + jjv + jk + jl) >> 1) & 1;
+            h.meta = (unsigned)n122 | ((unsigned)n_in << 5) | ((unsigned)n_out << 10) | ((unsigned)valid << 15) |
+                     ((unsigned)n2par << 16) | ((unsigned)nph << 17) | ((unsigned)nd << 18) |
+                     ((unsigned)(sq[g] && IX == JX) << 20) | ((unsigned)sq[g] << 21) | ((unsigned)(g == 2) << 22);
+            terms.insert(terms.end(), tl.begin(), tl.end());
+            // warps run elements of one loop-trip signature
+            long sig = (((long)n_in * 32 + n_out) * 32 + n122) * 2 + (valid ? 1 : 0);
+            items.push_back({sig, (int)heads.size()});
+            heads.push_back(h);
           }
       }
+    if (b->nfull >= (1L << 28) || b->off_fpp + (long)P * P >= (1L << 20)) return IMSRG_ERR_TOO_LARGE;
+    for (int q1 = 0; q1 < b->ccblocks; q1++)
+      if (b->cc_rlen[q1] >= 0xFFFF) return IMSRG_ERR_TOO_LARGE;
     std::stable_sort(items.begin(), items.end(),
                      [](const std::pair<long, int> &x, const std::pair<long, int> &y) { return x.first < y.first; });
-    std::vector<int> order(items.size());
-    for (size_t t = 0; t < items.size(); t++) order[t] = items[t].second;
-    T.n_asm2 = (int)order.size();
-    IMSRG_TRY(dev_upload(b, order, &T.asm2_order));
+    std::vector<Asm2Head> ordered(heads.size());
+    for (size_t t = 0; t < items.size(); t++) ordered[t] = heads[items[t].second];
+    T.n_asm2 = (int)ordered.size();
+    IMSRG_TRY(dev_upload(b, ordered, &T.asm2_head));
+    IMSRG_TRY(dev_upload(b, terms, &T.asm2_terms));
 
     std::vector<std::pair<long, int>> cit;
     for (int q1 = 0; q1 < b->ccblocks; q1++) {
@@ -461,38 +603,16 @@ int build_basis(imsrg_basis *b) {
 
   // --- gather lists of the one-body assembly (commutators.f90:83-280, 435-578)
   {
-    // host restatement of the element location of v_elem (basic_IMSRG.f90:1270-1385)
+    // location and prefactor (phase x sqrt(2)^nsq, rounded as the reference's
+    // pre * sqrt(2) chain) of v_elem
     auto hloc = [&](int a, int bb, int c, int d, int J2, long *idx, double *pre, int *trans) {
-      *idx = -1;
-      if (!(tri(b->jj[a], b->jj[bb], J2) && tri(b->jj[c], b->jj[d], J2))) return;
-      int Pp = (b->ll[a] + b->ll[bb]) & 1;
-      if (((b->ll[c] + b->ll[d]) & 1) != Pp) return;
-      int tz2 = b->itzp[a] + b->itzp[bb];
-      if (b->itzp[c] + b->itzp[d] != tz2) return;
-      int qq = 3 * J2 + 2 * (tz2 / 2 + 1) + Pp;
-      int C1 = b->con[a] + b->con[bb] + 1, C2 = b->con[c] + b->con[d] + 1;
-      int qx = C1 * C2;
-      if (qx == 9) qx = 5;
-      double pr = 1.0;
-      int i1, i2;
-      if (a > bb) {
-        i1 = pairrow[((size_t)bb * N + a) * nJ + J2 / 2];
-        pr = ((1 + (b->jj[a] + b->jj[bb] - J2) / 2) % 2) ? -1.0 : 1.0;
-      } else {
-        if (a == bb) pr = pr * 1.4142135623730951;
-        i1 = pairrow[((size_t)a * N + bb) * nJ + J2 / 2];
-      }
-      if (c > d) {
-        i2 = pairrow[((size_t)d * N + c) * nJ + J2 / 2];
-        pr = pr * (((1 + (b->jj[c] + b->jj[d] - J2) / 2) % 2) ? -1.0 : 1.0);
-      } else {
-        if (c == d) pr = pr * 1.4142135623730951;
-        i2 = pairrow[((size_t)c * N + d) * nJ + J2 / 2];
-      }
-      int sg = qq * 6 + qx - 1;
-      *trans = C1 > C2;
-      *idx = *trans ? b->gam_off[sg] + i2 + (long)i1 * b->gam_n1[sg] : b->gam_off[sg] + i1 + (long)i2 * b->gam_n1[sg];
+      HLoc v = vloc(a, bb, c, d, J2);
+      *idx = v.idx;
+      if (v.idx < 0) return;
+      double pr = v.neg ? -1.0 : 1.0;
+      for (int k = 0; k < v.nsq; k++) pr = pr * 1.4142135623730951;
       *pre = pr;
+      *trans = v.trans;
     };
     std::vector<OneBodyTerm> terms;
     long nel = (long)A * A + (long)P * A + (long)P * P;
@@ -683,6 +803,13 @@ void free_basis_device(imsrg_basis *b) {
   b->h_scal = b->h_stage = nullptr;
   if (b->own_stream) cudaStreamDestroy(b->own_stream);
   b->stream = b->own_stream = nullptr;
+  if (b->side) cudaStreamDestroy(b->side);
+  b->side = nullptr;
+  for (int k = 0; k < 2; k++) {
+    if (b->ev_fork[k]) cudaEventDestroy(b->ev_fork[k]);
+    if (b->ev_join[k]) cudaEventDestroy(b->ev_join[k]);
+    b->ev_fork[k] = b->ev_join[k] = nullptr;
+  }
 }
 
 }  // namespace imsrg

@@ -46,10 +46,14 @@ struct DevTables {
   int n_ph_pairs;
   const int *hole_orb;     // [hole position] -> orbit
   const int *part_orb;     // [particle position] -> orbit
-  // Work orders: element indices grouped by identical loop-trip signatures so
-  // the lanes of a warp run the same FP64 instruction sequence (GB300 issues
-  // an FP64 warp instruction at full cost whatever the active lanes).
-  const int *asm2_order;   // two-body elements (offset from the first gam), upper triangles only
+  // Work orders: elements grouped by identical loop-trip signatures so the
+  // lanes of a warp run the same FP64 instruction sequence (GB300 issues an
+  // FP64 warp instruction at full cost whatever the active lanes).
+  // Two-body elements (upper triangles only), each with its resolved gather
+  // list: asm2_head[w] for the w-th element of the work order, its terms in
+  // asm2_terms[head.start ..] (see Asm2Head).
+  const struct Asm2Head *asm2_head;
+  const unsigned long long *asm2_terms;
   int n_asm2;
   const int *ccf_order;    // cross-coupled elements
   int n_ccf;
@@ -81,6 +85,32 @@ struct OneBodyTerm {
   int idx;
   int meta;     // bits 0-1 kind, bit 2 trans, bit 3 W2 (else W1), bits 8.. ph
   double coef;  // (2J+1) x phase x sqrt(2)^n
+};
+
+// One two-body element of the assembly kernel with its operator-independent
+// gather list, resolved once per basis on the host.  The list holds, in
+// order:
+//   * n122 commutator_122 terms (commutators.f90:283-396): bits 0-27 flat
+//     index of the two-body element V, bits 28-47 flat index of the one-body
+//     element f, bit 48 sign (leg sign x pair-reordering phase), bits 49-50
+//     number of sqrt(2) factors, bit 51 V read transposed, bit 52 f read
+//     transposed (each transposed read takes the operator's herm);
+//   * n_in + n_out commutator_222_ph recoupling terms (:855-910), one per J'
+//     of the 'inside' and 'outside' channel: four 16-bit cross-coupled rows
+//     x1, y1, x2, y2 (0xFFFF = absent) of WCC block qx, which the kernel reads
+//     as W(x1,y1), W(x2,y2), W(y2,x2), W(y1,x1).  Consecutive J' of a channel
+//     have consecutive qx and consecutive 6j-table entries.
+struct __align__(16) Asm2Head {
+  int e;       // flat index of the element
+  int em;      // flat index of its mirror (JX, IX) in a square array, else -1 (== e on the diagonal)
+  int start;   // first term in asm2_terms
+  int six1;    // 6j-table index of the first J' of each channel
+  int six2;
+  int qx;      // WCC block of the first J': inside | outside << 16
+  unsigned meta;  // bits 0-4 n122, 5-9 n_in, 10-14 n_out, 15 recoupling applies,
+                  // 16 inside phase, 17 (-1)^((ji+jj+jk+jl)/2) phase, 18-19 identical
+                  // orbit pairs, 20 diagonal, 21 square array, 22 pphh array
+  int J2;
 };
 
 // One term alpha * op(A) * op(B) of a grouped GEMM problem.  Operand ids:
@@ -157,6 +187,10 @@ struct imsrg_basis {
   std::vector<void *> dev_allocs;
   cudaStream_t stream = nullptr;      // where all work is enqueued
   cudaStream_t own_stream = nullptr;  // the library's own stream
+  // A second library stream for independent launches inside one commutator,
+  // forked from and joined back into `stream` with events.
+  cudaStream_t side = nullptr;
+  cudaEvent_t ev_fork[2] = {nullptr, nullptr}, ev_join[2] = {nullptr, nullptr};
   int device = 0;
   imsrg::Profiler prof;
   // commutator workspace
@@ -203,7 +237,8 @@ int launch_gemm_fp64(imsrg_basis *b, const double *L, int hL, const double *R, i
 int launch_assemble_2body(imsrg_basis *b, const double *L, int hL, const double *R, int hR, double *RES, int hRES,
                           int with_e0);
 int launch_assemble_1body(imsrg_basis *b, const double *L, int hL, const double *R, int hR, double *RES, int hRES,
-                          int with_e0);
+                          cudaStream_t st);
+int launch_energy(imsrg_basis *b, const double *L, int hL, const double *R, int hR, double *RES, int e220);
 int launch_axpby(imsrg_basis *b, const double *A, double ax, const double *B, double bx, double *C);
 int launch_norm(imsrg_basis *b, const double *op, double *d_out);
 int launch_mbpt2(imsrg_basis *b, const double *H, int herm, double *d_out);
@@ -223,7 +258,10 @@ int launch_commutator_fp64_ws(imsrg_basis *b, const Workspace &ws, const double 
 
 // Ozaki split-precision contraction engine (ozaki.cu)
 int ozaki_prepare(imsrg_basis *b);  // plans and allocates the engine once; errors if unavailable
-int ozaki_gemm(imsrg_basis *b, const double *L, int hL, const double *R, int hR);
+// part 0: exponents and digit images of L and R; part 1: of LCC and RCC (after
+// the Pandya transform).  ozaki_mma then runs every contraction.
+int ozaki_slice(imsrg_basis *b, const double *L, const double *R, int part, cudaStream_t st);
+int ozaki_mma(imsrg_basis *b, int hL, int hR);
 int ozaki_check_error(imsrg_basis *b);  // IMSRG_ERR_TIMEOUT if a bounded device wait gave up
 void ozaki_free(imsrg_basis *b);
 
@@ -233,7 +271,8 @@ struct ProfScope {
   imsrg_basis *b;
   int kind;
   cudaEvent_t start = nullptr;
-  ProfScope(imsrg_basis *b, int kind);
+  cudaStream_t st = nullptr;
+  ProfScope(imsrg_basis *b, int kind, cudaStream_t st = nullptr);
   ~ProfScope();
 };
 int profile_collect(imsrg_basis *b);

@@ -24,16 +24,6 @@ namespace imsrg {
 
 namespace {
 
-__device__ __forceinline__ int upper_bound_l(const long *a, int n, long x) {
-  int lo = 0, hi = n;
-  while (lo < hi) {
-    int mid = (lo + hi) >> 1;
-    if (a[mid] <= x) lo = mid + 1;
-    else hi = mid;
-  }
-  return lo;
-}
-
 // ---------------------------------------------------------------------------
 // 1. Pandya transform: CCX(r(a,b), nb(p,h)) of cross_coupled.f90:1247-1291.
 // ---------------------------------------------------------------------------
@@ -149,155 +139,97 @@ __global__ void __launch_bounds__(256) k_gemm_fp64(const GemmProb *__restrict__ 
 }
 
 // ---------------------------------------------------------------------------
-// 3. Two-body assembly.
+// 3. Two-body assembly from the per-element gather lists (see Asm2Head).
 // ---------------------------------------------------------------------------
-// One-body insertions of commutator_122 for element <ab|..|cd> at J2: each
-// term resolves the location once and reads it from R and from L (the
-// reference's v_elem / v_same pair), two DFMAs per term.
-__device__ __forceinline__ double c122(const DevTables &T, const double *L, int hL, const double *R, int hR, int a,
-                                       int b, int c, int d, int J2) {
-  double sm = 0.0;
-  int s = T.ljt_start[a], n = T.ljt_count[a];
-  for (int k = 0; k < n; k++) {
-    int i = T.ljt_list[s + k];
-    VLoc vl = v_loc(T, i, b, c, d, J2);
-    sm = fma(f_elem(T, L, hL, a, i), v_read(R, hR, vl), sm);
-    sm = fma(-f_elem(T, R, hR, a, i), v_read(L, hL, vl), sm);
+// Cross-coupled W(r, c) of one WCC block, zero where a row is absent (not
+// reached for number-conserving blocks; the guard keeps the read in bounds).
+__device__ __forceinline__ double wcc_at(const double *W, int rlen, unsigned r, unsigned c) {
+  if (r == 0xFFFFu || c == 0xFFFFu) return 0.0;
+  return W[r + (long)c * rlen];
+}
+
+// One exchange channel of the inverse Pandya recoupling of commutator_222_ph
+// (commutators.f90:855-910): the +-1 factors (herm, phases) become sign flips
+// of the 6j symbol, leaving four DFMAs per J'.
+__device__ __forceinline__ double c222ph_channel(const DevTables &T, const double *WCC,
+                                                 const unsigned long long *tm, int n, int qx, long six, int n2,
+                                                 int nL, int nR, int nph, double sm) {
+  for (int k = 0; k < n; k++, qx++, six++) {
+    const unsigned long long u = tm[k];
+    const unsigned x1 = (unsigned)(u & 0xFFFF), y1 = (unsigned)((u >> 16) & 0xFFFF);
+    const unsigned x2 = (unsigned)((u >> 32) & 0xFFFF), y2 = (unsigned)(u >> 48);
+    const double *W = WCC + T.wcc_off[qx];
+    const int rl = T.cc_rlen[qx];
+    const double s6 = T.six[six];
+    const double c1 = dflip(s6, n2 ^ nL), c4 = dflip(s6, n2 ^ nR ^ 1);
+    sm = fma(c1, wcc_at(W, rl, x1, y1), sm);
+    sm = fma(dflip(c1, nph), wcc_at(W, rl, x2, y2), sm);
+    sm = fma(dflip(c4, nph), wcc_at(W, rl, y2, x2), sm);
+    sm = fma(c4, wcc_at(W, rl, y1, x1), sm);
   }
-  s = T.ljt_start[b];
-  n = T.ljt_count[b];
-  for (int k = 0; k < n; k++) {
-    int i = T.ljt_list[s + k];
-    VLoc vl = v_loc(T, a, i, c, d, J2);
-    sm = fma(f_elem(T, L, hL, b, i), v_read(R, hR, vl), sm);
-    sm = fma(-f_elem(T, R, hR, b, i), v_read(L, hL, vl), sm);
-  }
-  s = T.ljt_start[c];
-  n = T.ljt_count[c];
-  for (int k = 0; k < n; k++) {
-    int i = T.ljt_list[s + k];
-    VLoc vl = v_loc(T, a, b, i, d, J2);
-    sm = fma(-f_elem(T, L, hL, i, c), v_read(R, hR, vl), sm);
-    sm = fma(f_elem(T, R, hR, i, c), v_read(L, hL, vl), sm);
-  }
-  s = T.ljt_start[d];
-  n = T.ljt_count[d];
-  for (int k = 0; k < n; k++) {
-    int i = T.ljt_list[s + k];
-    VLoc vl = v_loc(T, a, b, c, i, J2);
-    sm = fma(-f_elem(T, L, hL, i, d), v_read(R, hR, vl), sm);
-    sm = fma(f_elem(T, R, hR, i, d), v_read(L, hL, vl), sm);
-  }
-  // / sqrt(1 + delta_ab) / sqrt(1 + delta_cd)
-  int nd = (a == b) + (c == d);
-  if (nd) sm = sm * (nd == 1 ? 0.7071067811865476 : 0.5);
   return sm;
 }
 
-__device__ __forceinline__ double wcc_at(const DevTables &T, const double *W, int qx, int r, int c) {
-  if (r < 0 || c < 0) return 0.0;  // unreachable for number-conserving blocks; guards the gather
-  return W[T.wcc_off[qx] + r + (long)c * T.cc_rlen[qx]];
-}
-__device__ __forceinline__ int cc_r(const DevTables &T, int q1, int i, int j) {
-  return T.cc_row[((long)q1 * T.norb + i) * T.norb + j];
-}
-
-// Inverse Pandya recoupling of commutator_222_ph (commutators.f90:855-910).
-// The +-1 factors (herm, phases) become sign flips of the 6j symbol, leaving
-// four DFMAs per J'.  Returns false where the reference's Tz/parity 'cycle'
-// would skip the update.
-__device__ __forceinline__ bool c222ph(const DevTables &T, const double *W, int hL, int hR, int i, int j, int k,
-                                       int l, int Jtot, double *out) {
-  int4 oi = T.orb[i], oj = T.orb[j], ok = T.orb[k], ol = T.orb[l];
-  int ji = oi.x, jj = oj.x, jk = ok.x, jl = ol.x;
-  int JTM = T.jtm;
-  int nL = hL < 0, nR = hR < 0;
-  double sm = 0.0;
-  int jmin = max(abs(jj - jl), abs(ji - jk));
-  int jmax = min(jj + jl, ji + jk);
-  int Tz = abs(oi.z - ok.z) / 2;
-  if (abs(ol.z - oj.z) != Tz * 2) return false;
-  int PAR = (oi.y + ok.y) & 1;
-  if (((ol.y + oj.y) & 1) != PAR) return false;
-  int nph = ((ji + jj + jk + jl) >> 1) & 1;
-  // 'inside' terms enter with -(-1)^((jl+jk+J)/2)
-  int n2 = (((jl + jk + Jtot) >> 1) + 1) & 1;
-  for (int JP = jmin; JP <= jmax; JP += 2) {
-    int qx = JP / 2 + Tz * (JTM + 1) + 2 * PAR * (JTM + 1);
-    int rjl = cc_r(T, qx, j, l), rik = cc_r(T, qx, i, k);
-    int gjl = cc_r(T, qx, l, j), gik = cc_r(T, qx, k, i);
-    double s6 = sixj(T, ji, jj, Jtot, jl, jk, JP);
-    double c1 = dflip(s6, n2 ^ nL), c4 = dflip(s6, n2 ^ nR ^ 1);
-    sm = fma(c1, wcc_at(T, W, qx, gik, rjl), sm);
-    sm = fma(dflip(c1, nph), wcc_at(T, W, qx, gjl, rik), sm);
-    sm = fma(dflip(c4, nph), wcc_at(T, W, qx, rik, gjl), sm);
-    sm = fma(c4, wcc_at(T, W, qx, rjl, gik), sm);
-  }
-  Tz = abs(oi.z - ol.z) / 2;
-  if (abs(ok.z - oj.z) != Tz * 2) return false;
-  PAR = (oi.y + ol.y) & 1;
-  if (((ok.y + oj.y) & 1) != PAR) return false;
-  jmin = max(abs(ji - jl), abs(jj - jk));
-  jmax = min(ji + jl, jj + jk);
-  for (int JP = jmin; JP <= jmax; JP += 2) {
-    int qx = JP / 2 + Tz * (JTM + 1) + 2 * PAR * (JTM + 1);
-    int ril = cc_r(T, qx, i, l), rjk = cc_r(T, qx, j, k);
-    int gil = cc_r(T, qx, l, i), gjk = cc_r(T, qx, k, j);
-    double s6 = sixj(T, ji, jj, Jtot, jk, jl, JP);
-    double c1 = dflip(s6, nL), c4 = dflip(s6, nR ^ 1);
-    sm = fma(c1, wcc_at(T, W, qx, gil, rjk), sm);
-    sm = fma(dflip(c1, nph), wcc_at(T, W, qx, gjk, ril), sm);
-    sm = fma(dflip(c4, nph), wcc_at(T, W, qx, ril, gjk), sm);
-    sm = fma(c4, wcc_at(T, W, qx, rjk, gil), sm);
-  }
-  *out = sm;
-  return true;
-}
-
-__global__ void __launch_bounds__(256) k_assemble_2body(DevTables T, const double *L, int hL, const double *R, int hR,
-                                                        const double *W1, const double *W2, const double *WCC,
-                                                        double *RES, int hRES, long off2b, double *e0p) {
+// Every two-body element of RES once (upper triangles of square arrays, the
+// mirror written alongside): the one-body insertions of commutator_122, the
+// antisymmetrised ladder epilogue of 222_pp_hh (:658-764) and the 222_ph
+// recoupling.
+__global__ void __launch_bounds__(256) k_assemble_2body(DevTables T, const double *__restrict__ L, int hL,
+                                                        const double *__restrict__ R, int hR,
+                                                        const double *__restrict__ W1, const double *__restrict__ W2,
+                                                        const double *__restrict__ WCC, double *RES, int hRES,
+                                                        double *e0p) {
   __shared__ double sh220[8];
-  long w = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  const long w = (long)blockIdx.x * blockDim.x + threadIdx.x;
   double e220 = 0.0;  // this element's commutator_220 term (pphh arrays only)
   if (w < T.n_asm2) {
-  long e = off2b + T.asm2_order[w];
-  int s = upper_bound_l(T.gam_off, T.nblocks * 6, e) - 1;
-  int q = s / 6, g = s % 6;
-  int n1 = T.gam_n1[s];
-  long loc = e - T.gam_off[s];
-  int IX = (int)(loc % n1), JX = (int)(loc / n1);
-  bool square = (g == 0 || g == 3 || g == 4);  // only IX <= JX is in the work order
-  // row / column pair categories: sea1 = (1,1,1,2,3,2), sea2 = (1,2,3,2,3,3)
-  // (categories 0 pp, 1 ph, 2 hh; packed two bits per g so no local array is needed)
-  const int c1 = (1600 >> (2 * g)) & 3, c2 = (2660 >> (2 * g)) & 3;
-  const int *qr = T.qn + T.qn_start[q * 3 + c1] + 2 * IX;
-  const int *qc = T.qn + T.qn_start[q * 3 + c2] + 2 * JX;
-  int a = qr[0], b = qr[1], c = qc[0], d = qc[1];
-  int J2 = T.blk_J2[q];
-  int nres = hRES < 0, npm = (hL * hR) < 0;
-  double t = c122(T, L, hL, R, hR, a, b, c, d, J2);
-  long em = T.gam_off[s] + JX + (long)IX * n1;  // mirror (JX, IX) of a square array
-  bool diag = square && IX == JX;
-  if (diag) t = dflip(t, nres);
-  t = t + W1[e];
-  t = t - W2[e];
-  if (square) t = t - dflip(W1[em] - W2[em], npm);
-  double sm;
-  if (c222ph(T, WCC, hL, hR, a, b, c, d, J2, &sm)) {
-    // the reference's truncated 1/sqrt(2) literal for identical orbits
-    int nd = (a == b) + (c == d);
-    if (nd) sm = sm * (nd == 1 ? .70710678118 : .70710678118 * .70710678118);
-    t = t + sm;
-  }
-  if (diag) {
-    RES[e] = dflip(t, nres);
-  } else {
-    RES[e] = t;
-    if (square) RES[em] = dflip(t, nres);
-  }
-  // commutator_220 (commutators.f90:409-427): -(2J+1) L_pphh R_pphh herm_R
-  if (e0p && g == 2) e220 = -L[e] * R[e] * hR * (J2 + 1.0);
+    const Asm2Head h = T.asm2_head[w];
+    const unsigned long long *tm = T.asm2_terms + h.start;
+    const unsigned meta = h.meta;
+    const int nL = hL < 0, nR = hR < 0, nres = hRES < 0, npm = (hL * hR) < 0;
+    // commutator_122 (commutators.f90:283-396): f_L V_R - f_R V_L per leg term
+    const int n122 = meta & 31;
+    double t = 0.0;
+    for (int k = 0; k < n122; k++) {
+      const unsigned long long u = tm[k];
+      const long vi = (long)(u & 0xFFFFFFFull), fi = (long)((u >> 28) & 0xFFFFFull);
+      const int sg = (int)(u >> 48) & 1, nsq = (int)(u >> 49) & 3, tr = (int)(u >> 51) & 1, ftr = (int)(u >> 52) & 1;
+      double vR = dflip(R[vi], tr & nR), vL = dflip(L[vi], tr & nL);
+      if (nsq) {
+        const double c = nsq == 1 ? IMSRG_SQRT2 : 2.0000000000000004;
+        vR = vR * c;
+        vL = vL * c;
+      }
+      const double fL = dflip(L[fi], (ftr & nL) ^ sg), fR = dflip(R[fi], (ftr & nR) ^ sg ^ 1);
+      t = fma(fL, vR, t);
+      t = fma(fR, vL, t);
+    }
+    // / sqrt(1 + delta_ab) / sqrt(1 + delta_cd)
+    const int nd = (meta >> 18) & 3;
+    if (nd) t = t * (nd == 1 ? 0.7071067811865476 : 0.5);
+    const bool diag = (meta >> 20) & 1, square = (meta >> 21) & 1;
+    const long e = h.e, em = h.em;
+    if (diag) t = dflip(t, nres);
+    t = t + W1[e];
+    t = t - W2[e];
+    if (square) t = t - dflip(W1[em] - W2[em], npm);
+    if ((meta >> 15) & 1) {
+      const int n_in = (meta >> 5) & 31, n_out = (meta >> 10) & 31;
+      const int n2 = (meta >> 16) & 1, nph = (meta >> 17) & 1;
+      double sm = c222ph_channel(T, WCC, tm + n122, n_in, h.qx & 0xFFFF, h.six1, n2, nL, nR, nph, 0.0);
+      sm = c222ph_channel(T, WCC, tm + n122 + n_in, n_out, h.qx >> 16, h.six2, 0, nL, nR, nph, sm);
+      // the reference's truncated 1/sqrt(2) literal for identical orbits
+      if (nd) sm = sm * (nd == 1 ? .70710678118 : .70710678118 * .70710678118);
+      t = t + sm;
+    }
+    if (diag) {
+      RES[e] = dflip(t, nres);
+    } else {
+      RES[e] = t;
+      if (square) RES[em] = dflip(t, nres);
+    }
+    // commutator_220 (commutators.f90:409-427): -(2J+1) L_pphh R_pphh herm_R
+    if (e0p && ((meta >> 22) & 1)) e220 = -L[e] * R[e] * hR * (h.J2 + 1.0);
   }
   if (e0p) {  // per-CTA partial in a fixed order; the one-body kernel sums them
     e220 = warp_sum(e220);
@@ -310,9 +242,6 @@ __global__ void __launch_bounds__(256) k_assemble_2body(DevTables T, const doubl
     }
   }
 }
-
-
-
 
 // Sum of NV values over the CTA (fixed order: warp shuffles, then warps in
 // index order), returned to every thread.
@@ -334,35 +263,37 @@ __device__ void cta_sum(double *v, double (*sh)[8]) {
   __syncthreads();
 }
 
+// E0 = commutator_110 + commutator_220 (commutators.f90:10-33, 399-432), one
+// CTA: the 220 sum arrives as the two-body kernel's per-CTA partials.
+__global__ void __launch_bounds__(128) k_energy(DevTables T, const double *L, int hL, const double *R, int hR,
+                                                double *RES, const double *e0p, int ne0p) {
+  __shared__ double sh[4][8];
+  const int A = T.A, P = T.P, tid = threadIdx.x, nt = blockDim.x;
+  const double *Lph = L + T.off_fph, *Rph = R + T.off_fph;
+  double v[2] = {0.0, 0.0};
+  for (int k = tid; k < P * A; k += nt) {
+    int ji = T.orb[T.hole_orb[k / P]].x;
+    v[0] += (Lph[k] * Rph[k] * hL - Rph[k] * Lph[k] * hR) * (ji + 1);
+  }
+  if (e0p)
+    for (int k = tid; k < ne0p; k += nt) v[1] += e0p[k];
+  cta_sum<2>(v, sh);
+  if (tid == 0) RES[0] = v[0] + v[1] * 2.0;
+}
+
 // One-body assembly.  The (l,j,tz)-allowed upper-triangle elements carry the
 // 121 and 221 gather lists (a few hundred independent terms each) and get a
 // CTA of four warps; every other element only has the four commutator_111 dot
 // products and gets one warp, four elements per CTA.  Each thread folds its
 // partial dot products and gather sums into the element's final linear
-// combination, so one reduction per element remains.  The last CTA computes E0.
+// combination, so one reduction per element remains.
 __global__ void __launch_bounds__(128) k_assemble_1body(DevTables T, const double *L, int hL, const double *R, int hR,
-                                                        const double *W1, const double *W2, double *RES, int hRES,
-                                                        int with_e0, const double *e0p, int ne0p) {
+                                                        const double *W1, const double *W2, double *RES, int hRES) {
   __shared__ double sh[4][8];
   const int A = T.A, P = T.P;
   const double *Lhh = L + T.off_fhh, *Lph = L + T.off_fph, *Lpp = L + T.off_fpp;
   const double *Rhh = R + T.off_fhh, *Rph = R + T.off_fph, *Rpp = R + T.off_fpp;
-  const int nheavy = T.n_asm1_heavy, nlight_cta = (T.n_asm1_light + 3) >> 2;
-  if ((int)blockIdx.x == nheavy + nlight_cta) {
-    if (!with_e0) return;
-    // E0 = commutator_110 + commutator_220 (commutators.f90:10-33, 399-432)
-    const int tid = threadIdx.x, nt = blockDim.x;
-    double v[2] = {0.0, 0.0};
-    for (int k = tid; k < P * A; k += nt) {
-      int ji = T.orb[T.hole_orb[k / P]].x;
-      v[0] += (Lph[k] * Rph[k] * hL - Rph[k] * Lph[k] * hR) * (ji + 1);
-    }
-    if (e0p)  // commutator_220 partials of the two-body kernel
-      for (int k = tid; k < ne0p; k += nt) v[1] += e0p[k];
-    cta_sum<2>(v, sh);
-    if (tid == 0) RES[0] = v[0] + v[1] * 2.0;
-    return;
-  }
+  const int nheavy = T.n_asm1_heavy;
   const bool whole = (int)blockIdx.x < nheavy;  // block-uniform
   long e;
   int tid, nt;
@@ -521,24 +452,29 @@ int launch_gemm_fp64(imsrg_basis *b, const double *L, int hL, const double *R, i
 
 int launch_assemble_2body(imsrg_basis *b, const double *L, int hL, const double *R, int hR, double *RES, int hRES,
                           int with_e0) {
-  long off2b = b->off_fpp + (long)b->P * b->P;
   long n = b->T.n_asm2;
   if (n <= 0) return IMSRG_OK;
   ProfScope ps(b, IMSRG_KERNEL_ASSEMBLE_2BODY);
   double *e0p = (with_e0 && hL * hR == -1) ? b->partials : nullptr;
   k_assemble_2body<<<(unsigned)((n + 255) / 256), 256, 0, b->stream>>>(b->T, L, hL, R, hR, b->w1, b->w2, b->wcc, RES,
-                                                                      hRES, off2b, e0p);
+                                                                      hRES, e0p);
   b->launches++;
   return cuda_status(cudaGetLastError());
 }
 
 int launch_assemble_1body(imsrg_basis *b, const double *L, int hL, const double *R, int hR, double *RES, int hRES,
-                          int with_e0) {
-  const int grid = b->T.n_asm1_heavy + (b->T.n_asm1_light + 3) / 4 + 1;
+                          cudaStream_t st) {
+  const int grid = b->T.n_asm1_heavy + (b->T.n_asm1_light + 3) / 4;
+  if (grid == 0) return IMSRG_OK;
+  ProfScope ps(b, IMSRG_KERNEL_ASSEMBLE_1BODY, st);
+  k_assemble_1body<<<grid, 128, 0, st>>>(b->T, L, hL, R, hR, b->w1, b->w2, RES, hRES);
+  b->launches++;
+  return cuda_status(cudaGetLastError());
+}
+
+int launch_energy(imsrg_basis *b, const double *L, int hL, const double *R, int hR, double *RES, int e220) {
   ProfScope ps(b, IMSRG_KERNEL_ASSEMBLE_1BODY);
-  const bool e220 = with_e0 && hL * hR == -1;
-  k_assemble_1body<<<grid, 128, 0, b->stream>>>(b->T, L, hL, R, hR, b->w1, b->w2, RES, hRES, with_e0,
-                                                e220 ? b->partials : nullptr, (b->T.n_asm2 + 255) / 256);
+  k_energy<<<1, 128, 0, b->stream>>>(b->T, L, hL, R, hR, RES, e220 ? b->partials : nullptr, (b->T.n_asm2 + 255) / 256);
   b->launches++;
   return cuda_status(cudaGetLastError());
 }
@@ -568,19 +504,23 @@ int launch_commutator_fp64_ws(imsrg_basis *b, const Workspace &ws, const double 
     k_gemm_fp64<<<b->ntiles, 256, 0, st>>>(b->d_probs, b->nprobs, ops, hL, hR);
     b->launches++;
   }
-  long off2b = b->off_fpp + (long)b->P * b->P;
   long n2 = b->T.n_asm2;
   if (n2 > 0) {
     double *e0p = (with_e0 && hL * hR == -1) ? ws.e0p : nullptr;
     k_assemble_2body<<<(unsigned)((n2 + 255) / 256), 256, 0, st>>>(b->T, L, hL, R, hR, ws.w1, ws.w2, ws.wcc, RES,
-                                                                   hRES, off2b, e0p);
+                                                                   hRES, e0p);
     b->launches++;
   }
-  const int grid1 = b->T.n_asm1_heavy + (b->T.n_asm1_light + 3) / 4 + 1;
-  const bool e220 = with_e0 && hL * hR == -1;
-  k_assemble_1body<<<grid1, 128, 0, st>>>(b->T, L, hL, R, hR, ws.w1, ws.w2, RES, hRES, with_e0,
-                                          e220 ? ws.e0p : nullptr, (b->T.n_asm2 + 255) / 256);
-  b->launches++;
+  const int grid1 = b->T.n_asm1_heavy + (b->T.n_asm1_light + 3) / 4;
+  if (grid1 > 0) {
+    k_assemble_1body<<<grid1, 128, 0, st>>>(b->T, L, hL, R, hR, ws.w1, ws.w2, RES, hRES);
+    b->launches++;
+  }
+  if (with_e0) {
+    const bool e220 = hL * hR == -1;
+    k_energy<<<1, 128, 0, st>>>(b->T, L, hL, R, hR, RES, e220 ? ws.e0p : nullptr, (b->T.n_asm2 + 255) / 256);
+    b->launches++;
+  }
   return cuda_status(cudaGetLastError());
 }
 

@@ -107,7 +107,7 @@ struct OzPlan {
   OzMatrix *d_mats = nullptr;
   OzChunk *d_chunks = nullptr;
   OzProb *d_probs = nullptr;
-  int *d_sched = nullptr;      // tile ids, grouped by CTA
+  int2 *d_sched = nullptr;     // (problem, tile within the problem), grouped by CTA
   int *d_sched_off = nullptr;  // [grid + 1] start of each CTA's list
   int *d_exps = nullptr;       // per group: max biased exponent (e = value - 1022)
   int *d_err = nullptr;
@@ -115,6 +115,12 @@ struct OzPlan {
   long img_bytes[4] = {0, 0, 0, 0};
   int nmats = 0, ngroups = 0, nchunks = 0, nprobs = 0, ntiles = 0;
   int lines_r = 0, lines_c = 0;
+  // The operands fall in two parts that are sliced separately: part 0 = L and
+  // R (available at once), part 1 = LCC and RCC (after the Pandya transform).
+  // Groups, chunks and image lines of part 0 come first.
+  int groups0 = 0, chunks0 = 0, lines_c0 = 0, lines_r0 = 0;
+  int *d_blk_mat = nullptr;  // slicing grids: matrix of each CTA's first line
+  int cblocks[2] = {0, 0}, rblocks[2] = {0, 0}, blk_off[2] = {0, 0};
   int grid = 0;
   bool ok = false;
 };
@@ -243,100 +249,117 @@ __global__ void __launch_bounds__(256) k_oz_exponents(const OzChunk *chunks, con
 // 2. digit slicing: one thread per 8-element line of a core matrix
 // ---------------------------------------------------------------------------
 // Digits of x with |x| < 2^e: x = 2^(e-42) sum_{s} d_s 128^(5-s), d_0 first.
+// One 64-bit shift rounds |x| to the 42-bit integer V; the balanced base-128
+// digits then come from its two 21-bit halves on the 32-bit integer pipe.
 __device__ __forceinline__ void digits6(double x, int e, int *d) {
-  unsigned long long bits = (unsigned long long)__double_as_longlong(x);
-  int E = (int)((bits >> 52) & 0x7FF);
-  int neg = (int)(bits >> 63);
+  const unsigned long long bits = (unsigned long long)__double_as_longlong(x);
+  const int E = (int)((bits >> 52) & 0x7FF);
+  const int neg = (int)(bits >> 63);
   unsigned long long V = 0;
   if (E != 0) {
-    unsigned long long mant = (bits & ((1ull << 52) - 1)) | (1ull << 52);
-    int rs = e + 1033 - E;  // V = round(|x| 2^(42 - e)), rs >= 11
+    const unsigned long long mant = (bits & ((1ull << 52) - 1)) | (1ull << 52);
+    const int rs = e + 1033 - E;  // V = round(|x| 2^(42 - e)), rs >= 11
     if (rs <= 63) V = (mant + (1ull << (rs - 1))) >> rs;
   }
+  unsigned lo = (unsigned)(V & 0x1FFFFFu), hi = (unsigned)(V >> 21);
 #pragma unroll
-  for (int s = OZ_S - 1; s >= 1; s--) {
-    int u = (int)(V & 127);
-    V >>= 7;
+  for (int s = OZ_S - 1; s >= 3; s--) {
+    int u = (int)(lo & 127u);
+    lo >>= 7;
     if (u >= 64) {
       u -= 128;
-      V += 1;
+      lo += 1;
     }
     d[s] = neg ? -u : u;
   }
-  d[0] = neg ? -(int)V : (int)V;
-}
-
-__device__ __forceinline__ uint32_t bf16_bits(int v) {
-  __nv_bfloat16 h = __float2bfloat16_rn((float)v);
-  return *reinterpret_cast<uint16_t *>(&h);
-}
-
-__device__ __forceinline__ int find_mat(const OzMatrix *mats, int nmats, int t, bool cimg) {
-  int lo = 0, hi = nmats;
-  while (lo < hi) {
-    int mid = (lo + hi) >> 1;
-    if ((cimg ? mats[mid].line_c0 : mats[mid].line_r0) <= t) lo = mid + 1;
-    else hi = mid;
+  hi += lo;  // carry out of the low half
+#pragma unroll
+  for (int s = 2; s >= 1; s--) {
+    int u = (int)(hi & 127u);
+    hi >>= 7;
+    if (u >= 64) {
+      u -= 128;
+      hi += 1;
+    }
+    d[s] = neg ? -u : u;
   }
-  return lo - 1;
+  d[0] = neg ? -(int)hi : (int)hi;
 }
 
-// Threads [0, lines_c) write C-image lines (8 consecutive rows of one column:
-// one 16-byte row of a C core matrix per digit plane); threads
-// [lines_c, lines_c + lines_r) write R-image lines (8 consecutive columns of
-// one row).  Padding lines of the images are never written and stay zero.
-__global__ void __launch_bounds__(256) k_oz_slice(const OzMatrix *mats, int nmats, int lines_c, int lines_r,
-                                                  const double *L, const double *R, const double *LCC,
-                                                  const double *RCC, const int *exps, uint8_t *imgL,
-                                                  uint8_t *imgR, uint8_t *imgLCC, uint8_t *imgRCC) {
-  int t = blockIdx.x * blockDim.x + threadIdx.x;
-  bool cimg = t < lines_c;
-  if (!cimg) t -= lines_c;
-  if (t >= (cimg ? lines_c : lines_r)) return;
-  const OzMatrix &m = mats[find_mat(mats, nmats, t, cimg)];
+// Threads of the first cblocks CTAs write C-image lines [c_lo, c_hi) (8
+// consecutive rows of one column: one 16-byte row of a C core matrix per digit
+// plane); the other CTAs write R-image lines [r_lo, r_hi) (8 consecutive
+// columns of one row).  blk_mat[b] is the matrix of CTA b's first line.  Padding lines of the images are never
+// written and stay zero.
+__global__ void __launch_bounds__(256) k_oz_slice(const OzMatrix *__restrict__ mats, int nmats,
+                                                  const int *__restrict__ blk_mat, int cblocks, int c_lo, int c_hi,
+                                                  int r_lo, int r_hi, const double *L, const double *R, const double *LCC,
+                                                  const double *RCC, const int *exps, uint8_t *imgL, uint8_t *imgR,
+                                                  uint8_t *imgLCC, uint8_t *imgRCC) {
+  // BF16 bit patterns of the digits -128..128 (exact), built once per CTA
+  __shared__ uint32_t tab[257];
+  for (int i = threadIdx.x; i < 257; i += blockDim.x) {
+    __nv_bfloat16 h = __float2bfloat16_rn((float)(i - 128));
+    tab[i] = *reinterpret_cast<uint16_t *>(&h);
+  }
+  __syncthreads();
+  const bool cimg = (int)blockIdx.x < cblocks;
+  const int t = (cimg ? c_lo : r_lo) + ((int)blockIdx.x - (cimg ? 0 : cblocks)) * blockDim.x + threadIdx.x;
+  if (t >= (cimg ? c_hi : r_hi)) return;
+  int mi = blk_mat[blockIdx.x];
+  while (mi + 1 < nmats && (cimg ? mats[mi + 1].line_c0 : mats[mi + 1].line_r0) <= t) mi++;
+  const OzMatrix &m = mats[mi];
   const double *src = (m.src == 0 ? L : m.src == 1 ? R : m.src == 2 ? LCC : RCC) + m.off;
   uint8_t *img = m.src == 0 ? imgL : m.src == 1 ? imgR : m.src == 2 ? imgLCC : imgRCC;
-  int e = exps[m.group] - 1022;
+  const int e = exps[m.group] - 1022;
   double x[8];
   long off;
   long plane;
   if (cimg) {
-    int RG = (m.n1 + 7) >> 3;
-    int l = t - m.line_c0;
-    int rg = l % RG, c = l / RG;
+    const int RG = (m.n1 + 7) >> 3;
+    const int l = t - m.line_c0;
+    const int rg = l % RG, c = l / RG;
 #pragma unroll
     for (int i = 0; i < 8; i++) {
-      int r = rg * 8 + i;
+      const int r = rg * 8 + i;
       x[i] = r < m.n1 ? src[r + (long)c * m.n1] : 0.0;
     }
     off = m.img_c + ((long)((rg >> 1) * m.rg_c + (c >> 3)) * 2 + (rg & 1)) * 128 + (c & 7) * 16;
     plane = m.plane_c;
   } else {
-    int l = t - m.line_r0;
-    int r = l % m.n1, cg = l / m.n1;
+    const int l = t - m.line_r0;
+    const int r = l % m.n1, cg = l / m.n1;
 #pragma unroll
     for (int j = 0; j < 8; j++) {
-      int c = cg * 8 + j;
+      const int c = cg * 8 + j;
       x[j] = c < m.n2 ? src[r + (long)c * m.n1] : 0.0;
     }
     off = m.img_r + ((long)((cg >> 1) * m.rg_r + (r >> 3)) * 2 + (cg & 1)) * 128 + (r & 7) * 16;
     plane = m.plane_r;
   }
   const int nplanes = cimg ? m.np_c : m.np_r;
-  int d[8][OZ_S];
+  uint32_t h[8][OZ_S];  // BF16 bits of each digit
 #pragma unroll
-  for (int i = 0; i < 8; i++) digits6(x[i], e, d[i]);
-  // plane k: digit s = k (k < 6), 2^7 d_{k-6} (6 <= k < 11), 2^14 d_{k-11} (k >= 11);
-  // all exact in BF16
+  for (int i = 0; i < 8; i++) {
+    int d[OZ_S];
+    digits6(x[i], e, d);
+#pragma unroll
+    for (int s = 0; s < OZ_S; s++) h[i][s] = tab[d[s] + 128];
+  }
+  // plane k: digit s = k (k < 6), 2^7 d_{k-6} (6 <= k < 11), 2^14 d_{k-11}
+  // (k >= 11): the scaled planes add 7 or 14 to the BF16 exponent of every
+  // non-zero digit, all exact
 #pragma unroll
   for (int k = 0; k < OZ_BPLANES; k++) {
     if (k >= nplanes) break;
     const int s = k < 6 ? k : k < 11 ? k - 6 : k - 11;
-    const int sh = k < 6 ? 0 : k < 11 ? 7 : 14;
+    const uint32_t add = k < 6 ? 0u : k < 11 ? (7u << 7) : (14u << 7);
     uint32_t w4[4];
 #pragma unroll
-    for (int i = 0; i < 8; i += 2)
-      w4[i >> 1] = bf16_bits(d[i][s] * (1 << sh)) | (bf16_bits(d[i + 1][s] * (1 << sh)) << 16);
+    for (int i = 0; i < 8; i += 2) {
+      const uint32_t a0 = h[i][s], a1 = h[i + 1][s];
+      w4[i >> 1] = (a0 ? a0 + add : 0u) | ((a1 ? a1 + add : 0u) << 16);
+    }
     *reinterpret_cast<uint4 *>(img + off + k * plane) = make_uint4(w4[0], w4[1], w4[2], w4[3]);
   }
 }
@@ -344,18 +367,9 @@ __global__ void __launch_bounds__(256) k_oz_slice(const OzMatrix *mats, int nmat
 // ---------------------------------------------------------------------------
 // 3. tensor-core products and exact recombination
 // ---------------------------------------------------------------------------
-__device__ __forceinline__ int find_prob(const OzProb *probs, int nprobs, int tile) {
-  int lo = 0, hi = nprobs;
-  while (lo < hi) {
-    int mid = (lo + hi) >> 1;
-    if (probs[mid].tile0 <= tile) lo = mid + 1;
-    else hi = mid;
-  }
-  return lo - 1;
-}
 
 __global__ void __launch_bounds__(OZ_THREADS, 1) k_oz_mma(const OzProb *__restrict__ probs, int nprobs,
-                                                          const int *__restrict__ sched,
+                                                          const int2 *__restrict__ sched,
                                                           const int *__restrict__ sched_off,
                                                           const int *__restrict__ exps, int hL, int hR, int *err) {
   extern __shared__ __align__(1024) uint8_t smem_raw[];
@@ -406,10 +420,10 @@ __global__ void __launch_bounds__(OZ_THREADS, 1) k_oz_mma(const OzProb *__restri
       int stage = 0;
       uint32_t phase = 0;
       for (int ti = t_begin; ti < t_end && !*abort_flag; ti++) {
-        int tile = sched[ti];
-        const OzProb &P = probs[find_prob(probs, nprobs, tile)];
+        const int2 slot = sched[ti];
+        const OzProb &P = probs[slot.x];
         if (P.ksteps == 0) continue;
-        int lt = tile - P.tile0;
+        const int lt = slot.y;
         int tm = lt % P.tiles_m, tn = lt / P.tiles_m;
         for (int it = 0; it < P.nterms; it++) {
           const OzTerm &T = P.t[it];
@@ -450,7 +464,7 @@ __global__ void __launch_bounds__(OZ_THREADS, 1) k_oz_mma(const OzProb *__restri
       int stage = 0, nt = 0;
       uint32_t phase = 0;
       for (int ti = t_begin; ti < t_end && !*abort_flag; ti++) {
-        const OzProb &P = probs[find_prob(probs, nprobs, sched[ti])];
+        const OzProb &P = probs[sched[ti].x];
         if (P.ksteps == 0) continue;
         int buf = nt & 1;
         uint32_t use = (uint32_t)(nt >> 1);
@@ -511,9 +525,9 @@ __global__ void __launch_bounds__(OZ_THREADS, 1) k_oz_mma(const OzProb *__restri
     const int row = quad * 32 + lane;
     int nt = 0;
     for (int ti = t_begin; ti < t_end; ti++) {
-      int tile = sched[ti];
-      const OzProb &P = probs[find_prob(probs, nprobs, tile)];
-      int lt = tile - P.tile0;
+      const int2 slot = sched[ti];
+      const OzProb &P = probs[slot.x];
+      const int lt = slot.y;
       // problem fields in registers: the stores below could alias the problem
       // table as far as the compiler knows, which would force a reload per column
       const int Mp = P.M, Np = P.N, ldc = P.ldc, ksteps = P.ksteps, gA = P.gA, gB = P.gB;
@@ -628,6 +642,8 @@ int ozaki_prepare(imsrg_basis *b) {
       int g = add_group(src, o0, o1 - o0);
       for (int k = 0; k < 6; k++) add_matrix(src, g, b->gam_off[q * 6 + k], b->gam_n1[q * 6 + k], b->gam_n2[q * 6 + k]);
     }
+  pl->groups0 = ngroups;
+  pl->chunks0 = (int)chunks.size();
   for (int src = 2; src < 4; src++)
     for (int q1 = 0; q1 < b->ccblocks; q1++) {
       long len = (long)b->cc_rlen[q1] * b->cc_nph[q1];
@@ -684,6 +700,35 @@ int ozaki_prepare(imsrg_basis *b) {
   }
   pl->lines_r = lines_r;
   pl->lines_c = lines_c;
+  // first lines of part 1 (the first LCC matrix)
+  pl->lines_c0 = lines_c;
+  pl->lines_r0 = lines_r;
+  for (const OzMatrix &m : pl->mats)
+    if (m.src >= 2) {
+      pl->lines_c0 = m.line_c0;
+      pl->lines_r0 = m.line_r0;
+      break;
+    }
+  // per part: the matrix of each 256-line CTA's first line (C lines, then R lines)
+  std::vector<int> blk_mat;
+  for (int part = 0; part < 2; part++) {
+    const int c_lo = part ? pl->lines_c0 : 0, c_hi = part ? lines_c : pl->lines_c0;
+    const int r_lo = part ? pl->lines_r0 : 0, r_hi = part ? lines_r : pl->lines_r0;
+    pl->cblocks[part] = (c_hi - c_lo + 255) / 256;
+    pl->rblocks[part] = (r_hi - r_lo + 255) / 256;
+    pl->blk_off[part] = (int)blk_mat.size();
+    for (int cimg = 1; cimg >= 0; cimg--) {
+      const int nb = cimg ? pl->cblocks[part] : pl->rblocks[part];
+      const int lo = cimg ? c_lo : r_lo;
+      int mi = 0;
+      auto l0 = [&](int k) { return cimg ? pl->mats[k].line_c0 : pl->mats[k].line_r0; };
+      for (int bk = 0; bk < nb; bk++) {
+        const int t0 = lo + bk * 256;
+        while (mi + 1 < (int)pl->mats.size() && l0(mi + 1) <= t0) mi++;
+        blk_mat.push_back(mi);
+      }
+    }
+  }
   for (int s = 0; s < 4; s++) {
     pl->img_bytes[s] = std::max<long>(imgb[s], 256);
     void *p = nullptr;
@@ -695,6 +740,7 @@ int ozaki_prepare(imsrg_basis *b) {
   // problems: the FP64 grouped-GEMM list mapped onto images
   int tiles = 0;
   std::vector<int> tile_cost;
+  std::vector<int2> tile_slot;  // (problem, tile within the problem) of each tile
   for (const GemmProb &gp : b->probs) {
     OzProb p{};
     p.M = gp.M;
@@ -733,7 +779,13 @@ int ozaki_prepare(imsrg_basis *b) {
     p.tiles = p.tiles_m * ((p.N + TN - 1) / TN);
     p.tile0 = tiles;
     tiles += p.tiles;
-    for (int k = 0; k < p.tiles; k++) tile_cost.push_back(p.nterms * p.ksteps + 2);
+    for (int k = 0; k < p.tiles; k++) {
+      // cost in K steps: the products, plus the epilogue's conversions of
+      // the live part of the tile (a full tile costs about five K steps)
+      const int live_m = std::min(TM, p.M - (k % p.tiles_m) * TM), live_n = std::min(TN, p.N - (k / p.tiles_m) * TN);
+      tile_cost.push_back(4 * p.nterms * p.ksteps + (20 * live_m * live_n) / (TM * TN) + 4);
+      tile_slot.push_back(make_int2((int)pl->probs.size(), k));
+    }
     pl->probs.push_back(p);
   }
   pl->nmats = (int)pl->mats.size();
@@ -752,10 +804,11 @@ int ozaki_prepare(imsrg_basis *b) {
     load[best] += tile_cost[t];
     lists[best].push_back(t);
   }
-  std::vector<int> sched, sched_off(pl->grid + 1, 0);
+  std::vector<int2> sched;
+  std::vector<int> sched_off(pl->grid + 1, 0);
   for (int c = 0; c < pl->grid; c++) {
     sched_off[c] = (int)sched.size();
-    sched.insert(sched.end(), lists[c].begin(), lists[c].end());
+    for (int t : lists[c]) sched.push_back(tile_slot[t]);
   }
   sched_off[pl->grid] = (int)sched.size();
 
@@ -767,8 +820,9 @@ int ozaki_prepare(imsrg_basis *b) {
   IMSRG_TRY(up(pl->mats.data(), pl->mats.size() * sizeof(OzMatrix), (void **)&pl->d_mats));
   IMSRG_TRY(up(chunks.data(), chunks.size() * sizeof(OzChunk), (void **)&pl->d_chunks));
   IMSRG_TRY(up(pl->probs.data(), pl->probs.size() * sizeof(OzProb), (void **)&pl->d_probs));
-  IMSRG_TRY(up(sched.data(), sched.size() * sizeof(int), (void **)&pl->d_sched));
+  IMSRG_TRY(up(sched.data(), sched.size() * sizeof(int2), (void **)&pl->d_sched));
   IMSRG_TRY(up(sched_off.data(), sched_off.size() * sizeof(int), (void **)&pl->d_sched_off));
+  IMSRG_TRY(up(blk_mat.data(), blk_mat.size() * sizeof(int), (void **)&pl->d_blk_mat));
   IMSRG_CUDA_TRY(cudaMalloc((void **)&pl->d_exps, std::max(pl->ngroups, 1) * sizeof(int)));
   IMSRG_CUDA_TRY(cudaMalloc((void **)&pl->d_err, sizeof(int)));
   IMSRG_CUDA_TRY(cudaMemset(pl->d_err, 0, sizeof(int)));
@@ -778,29 +832,36 @@ int ozaki_prepare(imsrg_basis *b) {
   return IMSRG_OK;
 }
 
-int ozaki_gemm(imsrg_basis *b, const double *L, int hL, const double *R, int hR) {
-  IMSRG_TRY(ozaki_prepare(b));
+int ozaki_slice(imsrg_basis *b, const double *L, const double *R, int part, cudaStream_t st) {
   OzPlan *pl = plan_of(b);
-  {
-    ProfScope ps(b, IMSRG_KERNEL_OZAKI_SLICE);
-    IMSRG_CUDA_TRY(cudaMemsetAsync(pl->d_exps, 0, std::max(pl->ngroups, 1) * sizeof(int), b->stream));
-    if (pl->nchunks)
-      k_oz_exponents<<<pl->nchunks, 256, 0, b->stream>>>(pl->d_chunks, L, R, b->lcc, b->rcc, pl->d_exps);
-    int lines = pl->lines_c + pl->lines_r;
-    if (lines)
-      k_oz_slice<<<(lines + 255) / 256, 256, 0, b->stream>>>(pl->d_mats, pl->nmats, pl->lines_c, pl->lines_r, L, R,
-                                                              b->lcc, b->rcc, pl->d_exps, pl->img[0], pl->img[1],
-                                                              pl->img[2], pl->img[3]);
-    b->launches += 2;
-  }
-  IMSRG_CUDA_TRY(cudaGetLastError());
-  {
-    ProfScope ps(b, IMSRG_KERNEL_OZAKI_MMA);
-    int smem = STAGES * STAGE_BYTES + 1024 + 256;
-    k_oz_mma<<<pl->grid, OZ_THREADS, smem, b->stream>>>(pl->d_probs, pl->nprobs, pl->d_sched, pl->d_sched_off,
-                                                       pl->d_exps, hL, hR, pl->d_err);
+  if (!pl) return IMSRG_ERR_INVALID;
+  ProfScope ps(b, IMSRG_KERNEL_OZAKI_SLICE, st);
+  const int g0 = part ? pl->groups0 : 0, g1 = part ? pl->ngroups : pl->groups0;
+  const int k0 = part ? pl->chunks0 : 0, k1 = part ? pl->nchunks : pl->chunks0;
+  if (g1 > g0) IMSRG_CUDA_TRY(cudaMemsetAsync(pl->d_exps + g0, 0, (g1 - g0) * sizeof(int), st));
+  if (k1 > k0) {
+    k_oz_exponents<<<k1 - k0, 256, 0, st>>>(pl->d_chunks + k0, L, R, b->lcc, b->rcc, pl->d_exps);
     b->launches++;
   }
+  const int nblk = pl->cblocks[part] + pl->rblocks[part];
+  if (nblk) {
+    k_oz_slice<<<nblk, 256, 0, st>>>(pl->d_mats, pl->nmats, pl->d_blk_mat + pl->blk_off[part], pl->cblocks[part],
+                                     part ? pl->lines_c0 : 0, part ? pl->lines_c : pl->lines_c0,
+                                     part ? pl->lines_r0 : 0, part ? pl->lines_r : pl->lines_r0, L, R, b->lcc,
+                                     b->rcc, pl->d_exps, pl->img[0], pl->img[1], pl->img[2], pl->img[3]);
+    b->launches++;
+  }
+  return cuda_status(cudaGetLastError());
+}
+
+int ozaki_mma(imsrg_basis *b, int hL, int hR) {
+  OzPlan *pl = plan_of(b);
+  if (!pl) return IMSRG_ERR_INVALID;
+  ProfScope ps(b, IMSRG_KERNEL_OZAKI_MMA);
+  const int smem = STAGES * STAGE_BYTES + 1024 + 256;
+  k_oz_mma<<<pl->grid, OZ_THREADS, smem, b->stream>>>(pl->d_probs, pl->nprobs, pl->d_sched, pl->d_sched_off,
+                                                     pl->d_exps, hL, hR, pl->d_err);
+  b->launches++;
   return cuda_status(cudaGetLastError());
 }
 
@@ -826,6 +887,7 @@ void ozaki_free(imsrg_basis *b) {
   cudaFree(pl->d_probs);
   cudaFree(pl->d_sched);
   cudaFree(pl->d_sched_off);
+  cudaFree(pl->d_blk_mat);
   cudaFree(pl->d_exps);
   cudaFree(pl->d_err);
   delete pl;

@@ -17,10 +17,10 @@ cudaEvent_t get_event(imsrg_basis *b) {
 }
 }  // namespace
 
-ProfScope::ProfScope(imsrg_basis *b_, int kind_) : b(b_), kind(kind_) {
+ProfScope::ProfScope(imsrg_basis *b_, int kind_, cudaStream_t st_) : b(b_), kind(kind_), st(st_ ? st_ : b_->stream) {
   if (!b->prof.on) return;
   start = get_event(b);
-  if (start) cudaEventRecord(start, b->stream);
+  if (start) cudaEventRecord(start, st);
 }
 
 ProfScope::~ProfScope() {
@@ -30,7 +30,7 @@ ProfScope::~ProfScope() {
     b->prof.pool.push_back(start);
     return;
   }
-  cudaEventRecord(stop, b->stream);
+  cudaEventRecord(stop, st);
   b->prof.pending.push_back({kind, start, stop});
   if (b->prof.pending.size() > 8192) profile_collect(b);
 }
