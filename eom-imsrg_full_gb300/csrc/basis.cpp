@@ -13,6 +13,7 @@
 #include <cmath>
 #include <cstring>
 #include <algorithm>
+#include <map>
 
 #include "internal.h"
 
@@ -471,101 +472,122 @@ int build_basis(imsrg_basis *b) {
            (J6 >> 1);
   };
 
-  // --- two-body assembly: work order and gather lists (see Asm2Head)
+  // --- two-body assembly: work order, gather lists and the recoupling inputs
+  // shared by the elements of one orbit quadruple (see Asm2Head, PhTerm)
   {
     auto jpcount = [&](int lo, int hi) { return hi >= lo ? (hi - lo) / 2 + 1 : 0; };
     static const int c1tab[6] = {0, 0, 0, 1, 2, 1}, c2tab[6] = {0, 1, 2, 1, 2, 2};
-    std::vector<Asm2Head> heads;
-    std::vector<unsigned long long> terms;
-    std::vector<std::pair<long, int>> items;  // (signature, head)
-    std::vector<unsigned long long> tl;
+    // elements of each (a, b, c, d, category), in increasing J (blocks run J-major)
+    struct El {
+      int e, em, J2, IX, JX;
+    };
+    std::map<unsigned long long, std::vector<El>> qmap;
+    std::vector<unsigned long long> qorder;  // quadruples in first-seen order
     for (int qb = 0; qb < b->nblocks; qb++)
       for (int g = 0; g < 6; g++) {
-        int n1 = b->gam_n1[qb * 6 + g], n2 = b->gam_n2[qb * 6 + g];
-        const int J2 = blk_J2[qb];
+        const int n1 = b->gam_n1[qb * 6 + g], n2 = b->gam_n2[qb * 6 + g];
+        const std::vector<int> &qr = b->qn[qb * 3 + c1tab[g]], &qc = b->qn[qb * 3 + c2tab[g]];
         for (int JX = 0; JX < n2; JX++)
           for (int IX = 0; IX < n1; IX++) {
             if (sq[g] && IX > JX) continue;
-            const std::vector<int> &qr = b->qn[qb * 3 + c1tab[g]], &qc = b->qn[qb * 3 + c2tab[g]];
-            const int i = qr[2 * IX], j = qr[2 * IX + 1], k = qc[2 * JX], l = qc[2 * JX + 1];
-            const int ji = b->jj[i], jjv = b->jj[j], jk = b->jj[k], jl = b->jj[l];
-            Asm2Head h{};
-            h.e = (int)(b->gam_off[qb * 6 + g] + IX + (long)JX * n1);
-            h.em = sq[g] ? (int)(b->gam_off[qb * 6 + g] + JX + (long)IX * n1) : -1;
-            h.start = (int)terms.size();
-            h.J2 = J2;
-            tl.clear();
-            // commutator_122: one-body insertions on the four legs
-            auto add122 = [&](int leg_sign, int fa, int fb, const HLoc &v) {
-              if (v.idx < 0) return;
-              int ftr;
-              long fi = floc(fa, fb, &ftr);
-              tl.push_back((unsigned long long)v.idx | ((unsigned long long)fi << 28) |
-                           ((unsigned long long)(leg_sign ^ v.neg) << 48) | ((unsigned long long)v.nsq << 49) |
-                           ((unsigned long long)v.trans << 51) | ((unsigned long long)ftr << 52));
-            };
-            for (int t = 0; t < ljt_count[i]; t++) {
-              int x = ljt_list[ljt_start[i] + t];
-              add122(0, i, x, vloc(x, j, k, l, J2));
+            const unsigned long long key = ((((unsigned long long)qr[2 * IX] * 4096 + qr[2 * IX + 1]) * 4096 +
+                                             qc[2 * JX]) * 4096 + qc[2 * JX + 1]) * 8 + g;
+            auto it = qmap.find(key);
+            if (it == qmap.end()) {
+              it = qmap.emplace(key, std::vector<El>()).first;
+              qorder.push_back(key);
             }
-            for (int t = 0; t < ljt_count[j]; t++) {
-              int x = ljt_list[ljt_start[j] + t];
-              add122(0, j, x, vloc(i, x, k, l, J2));
-            }
-            for (int t = 0; t < ljt_count[k]; t++) {
-              int x = ljt_list[ljt_start[k] + t];
-              add122(1, x, k, vloc(i, j, x, l, J2));
-            }
-            for (int t = 0; t < ljt_count[l]; t++) {
-              int x = ljt_list[ljt_start[l] + t];
-              add122(1, x, l, vloc(i, j, k, x, J2));
-            }
-            const int n122 = (int)tl.size();
-            // commutator_222_ph recoupling, both exchange channels
-            const int JTM = jtm;
-            int Tz1 = std::abs(b->itzp[i] - b->itzp[k]) / 2, PAR1 = (b->ll[i] + b->ll[k]) & 1;
-            int Tz2 = std::abs(b->itzp[i] - b->itzp[l]) / 2, PAR2 = (b->ll[i] + b->ll[l]) & 1;
-            bool valid = std::abs(b->itzp[l] - b->itzp[j]) == Tz1 * 2 && ((b->ll[l] + b->ll[j]) & 1) == PAR1 &&
-                         std::abs(b->itzp[k] - b->itzp[j]) == Tz2 * 2 && ((b->ll[k] + b->ll[j]) & 1) == PAR2;
-            int n_in = 0, n_out = 0;
-            auto row16 = [](int r) -> unsigned long long { return r < 0 ? 0xFFFFull : (unsigned long long)r; };
-            if (valid) {
-              int jmin = std::max(std::abs(jjv - jl), std::abs(ji - jk)), jmax = std::min(jjv + jl, ji + jk);
-              for (int JP = jmin; JP <= jmax; JP += 2, n_in++) {
-                int qx = JP / 2 + Tz1 * (JTM + 1) + 2 * PAR1 * (JTM + 1);
-                if (JP == jmin) {
-                  h.qx = qx;
-                  h.six1 = (int)sixidx(ji, jjv, J2, jl, jk, JP);
-                }
-                tl.push_back(row16(ccr(qx, k, i)) | (row16(ccr(qx, j, l)) << 16) | (row16(ccr(qx, l, j)) << 32) |
-                             (row16(ccr(qx, i, k)) << 48));
-              }
-              jmin = std::max(std::abs(ji - jl), std::abs(jjv - jk));
-              jmax = std::min(ji + jl, jjv + jk);
-              for (int JP = jmin; JP <= jmax; JP += 2, n_out++) {
-                int qx = JP / 2 + Tz2 * (JTM + 1) + 2 * PAR2 * (JTM + 1);
-                if (JP == jmin) {
-                  h.qx |= qx << 16;
-                  h.six2 = (int)sixidx(ji, jjv, J2, jk, jl, JP);
-                }
-                tl.push_back(row16(ccr(qx, l, i)) | (row16(ccr(qx, j, k)) << 16) | (row16(ccr(qx, k, j)) << 32) |
-                             (row16(ccr(qx, i, l)) << 48));
-              }
-            }
-            if (n122 > 31 || n_in > 31 || n_out > 31) return IMSRG_ERR_TOO_LARGE;
-            const int nd = (i == j) + (k == l);
-            const int n2par = (((jl + jk + J2) >> 1) + 1) & 1;
-            const int nph = ((ji + jjv + jk + jl) >> 1) & 1;
-            h.meta = (unsigned)n122 | ((unsigned)n_in << 5) | ((unsigned)n_out << 10) | ((unsigned)valid << 15) |
-                     ((unsigned)n2par << 16) | ((unsigned)nph << 17) | ((unsigned)nd << 18) |
-                     ((unsigned)(sq[g] && IX == JX) << 20) | ((unsigned)sq[g] << 21) | ((unsigned)(g == 2) << 22);
-            terms.insert(terms.end(), tl.begin(), tl.end());
-            // warps run elements of one loop-trip signature
-            long sig = (((long)n_in * 32 + n_out) * 32 + n122) * 2 + (valid ? 1 : 0);
-            items.push_back({sig, (int)heads.size()});
-            heads.push_back(h);
+            El el{(int)(b->gam_off[qb * 6 + g] + IX + (long)JX * n1),
+                  sq[g] ? (int)(b->gam_off[qb * 6 + g] + JX + (long)IX * n1) : -1, blk_J2[qb], IX, JX};
+            it->second.push_back(el);
           }
       }
+    std::vector<Asm2Head> heads;
+    std::vector<PhTerm> zt;
+    std::vector<unsigned long long> terms;
+    std::vector<std::pair<long, int>> items;  // (signature, head)
+    auto row16 = [](int r) -> unsigned long long { return r < 0 ? 0xFFFFull : (unsigned long long)r; };
+    for (unsigned long long key : qorder) {
+      const std::vector<El> &els = qmap[key];
+      const int g = (int)(key & 7);
+      const int l = (int)((key >> 3) & 4095), k = (int)((key >> 15) & 4095), j = (int)((key >> 27) & 4095),
+                i = (int)((key >> 39) & 4095);
+      const int ji = b->jj[i], jjv = b->jj[j], jk = b->jj[k], jl = b->jj[l];
+      // commutator_222_ph recoupling inputs of both exchange channels (J independent)
+      const int JTM = jtm;
+      const int Tz1 = std::abs(b->itzp[i] - b->itzp[k]) / 2, PAR1 = (b->ll[i] + b->ll[k]) & 1;
+      const int Tz2 = std::abs(b->itzp[i] - b->itzp[l]) / 2, PAR2 = (b->ll[i] + b->ll[l]) & 1;
+      const bool valid = std::abs(b->itzp[l] - b->itzp[j]) == Tz1 * 2 && ((b->ll[l] + b->ll[j]) & 1) == PAR1 &&
+                         std::abs(b->itzp[k] - b->itzp[j]) == Tz2 * 2 && ((b->ll[k] + b->ll[j]) & 1) == PAR2;
+      const int nph = ((ji + jjv + jk + jl) >> 1) & 1;
+      const int zs = (int)zt.size();
+      const int jmin1 = std::max(std::abs(jjv - jl), std::abs(ji - jk)), jmax1 = std::min(jjv + jl, ji + jk);
+      const int jmin2 = std::max(std::abs(ji - jl), std::abs(jjv - jk)), jmax2 = std::min(ji + jl, jjv + jk);
+      int n_in = 0, n_out = 0;
+      if (valid) {
+        for (int JP = jmin1; JP <= jmax1; JP += 2, n_in++) {
+          const int qx = JP / 2 + Tz1 * (JTM + 1) + 2 * PAR1 * (JTM + 1);
+          zt.push_back({row16(ccr(qx, k, i)) | (row16(ccr(qx, j, l)) << 16) | (row16(ccr(qx, l, j)) << 32) |
+                            (row16(ccr(qx, i, k)) << 48),
+                        qx, nph});
+        }
+        for (int JP = jmin2; JP <= jmax2; JP += 2, n_out++) {
+          const int qx = JP / 2 + Tz2 * (JTM + 1) + 2 * PAR2 * (JTM + 1);
+          zt.push_back({row16(ccr(qx, l, i)) | (row16(ccr(qx, j, k)) << 16) | (row16(ccr(qx, k, j)) << 32) |
+                            (row16(ccr(qx, i, l)) << 48),
+                        qx, nph});
+        }
+      }
+      const int nd = (i == j) + (k == l);
+      for (const El &el : els) {
+        const int J2 = el.J2;
+        Asm2Head h{};
+        h.e = el.e;
+        h.em = el.em;
+        h.J2 = J2;
+        h.start = (int)terms.size();
+        h.zs = zs;
+        if (valid) {
+          h.six1 = (int)sixidx(ji, jjv, J2, jl, jk, jmin1);
+          h.six2 = (int)sixidx(ji, jjv, J2, jk, jl, jmin2);
+        }
+        // commutator_122: one-body insertions on the four legs
+        auto add122 = [&](int leg_sign, int fa, int fb, const HLoc &v) {
+          if (v.idx < 0) return;
+          int ftr;
+          long fi = floc(fa, fb, &ftr);
+          terms.push_back((unsigned long long)v.idx | ((unsigned long long)fi << 28) |
+                          ((unsigned long long)(leg_sign ^ v.neg) << 48) | ((unsigned long long)v.nsq << 49) |
+                          ((unsigned long long)v.trans << 51) | ((unsigned long long)ftr << 52));
+        };
+        for (int t = 0; t < ljt_count[i]; t++) {
+          const int x = ljt_list[ljt_start[i] + t];
+          add122(0, i, x, vloc(x, j, k, l, J2));
+        }
+        for (int t = 0; t < ljt_count[j]; t++) {
+          const int x = ljt_list[ljt_start[j] + t];
+          add122(0, j, x, vloc(i, x, k, l, J2));
+        }
+        for (int t = 0; t < ljt_count[k]; t++) {
+          const int x = ljt_list[ljt_start[k] + t];
+          add122(1, x, k, vloc(i, j, x, l, J2));
+        }
+        for (int t = 0; t < ljt_count[l]; t++) {
+          const int x = ljt_list[ljt_start[l] + t];
+          add122(1, x, l, vloc(i, j, k, x, J2));
+        }
+        const int n122 = (int)terms.size() - h.start;
+        if (n122 > 31 || n_in > 31 || n_out > 31) return IMSRG_ERR_TOO_LARGE;
+        const int n2par = (((jl + jk + J2) >> 1) + 1) & 1;
+        h.meta = (unsigned)n122 | ((unsigned)n_in << 5) | ((unsigned)n_out << 10) | ((unsigned)valid << 15) |
+                 ((unsigned)n2par << 16) | ((unsigned)nd << 18) | ((unsigned)(sq[g] && el.IX == el.JX) << 20) |
+                 ((unsigned)sq[g] << 21) | ((unsigned)(g == 2) << 22);
+        // warps run elements of one loop-trip signature
+        const long sig = (((long)n_in * 32 + n_out) * 32 + n122) * 2 + (valid ? 1 : 0);
+        items.push_back({sig, (int)heads.size()});
+        heads.push_back(h);
+      }
+    }
     if (b->nfull >= (1L << 28) || b->off_fpp + (long)P * P >= (1L << 20)) return IMSRG_ERR_TOO_LARGE;
     for (int q1 = 0; q1 < b->ccblocks; q1++)
       if (b->cc_rlen[q1] >= 0xFFFF) return IMSRG_ERR_TOO_LARGE;
@@ -574,8 +596,10 @@ int build_basis(imsrg_basis *b) {
     std::vector<Asm2Head> ordered(heads.size());
     for (size_t t = 0; t < items.size(); t++) ordered[t] = heads[items[t].second];
     T.n_asm2 = (int)ordered.size();
+    T.n_ph = (int)zt.size();
     IMSRG_TRY(dev_upload(b, ordered, &T.asm2_head));
     IMSRG_TRY(dev_upload(b, terms, &T.asm2_terms));
+    IMSRG_TRY(dev_upload(b, zt, &T.ph_terms));
 
     std::vector<std::pair<long, int>> cit;
     for (int q1 = 0; q1 < b->ccblocks; q1++) {
@@ -777,11 +801,13 @@ int build_basis(imsrg_basis *b) {
   b->rcc = (double *)p;
   IMSRG_TRY(dev_alloc(b, b->wcc_total * sizeof(double), &p));
   b->wcc = (double *)p;
+  IMSRG_TRY(dev_alloc(b, (size_t)T.n_ph * sizeof(double), &p));
+  b->zph = (double *)p;
   IMSRG_TRY(dev_alloc(b, (size_t)N * N * sizeof(double), &p));
   b->mono = (double *)p;
   IMSRG_TRY(dev_alloc(b, 64 * sizeof(double), &p));
   b->scal = (double *)p;
-  b->partials_len = std::max(std::max(b->nchunks, b->nblocks), (T.n_asm2 + 255) / 256) + 64;
+  b->partials_len = std::max(std::max(b->nchunks, b->nblocks), asm2_ctas(b)) + 64;
   IMSRG_TRY(dev_alloc(b, b->partials_len * sizeof(double), &p));
   b->partials = (double *)p;
   IMSRG_TRY(dev_alloc(b, std::max(b->nfull, b->neq) * sizeof(double), &p));

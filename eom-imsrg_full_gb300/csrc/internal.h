@@ -49,12 +49,16 @@ struct DevTables {
   // Work orders: elements grouped by identical loop-trip signatures so the
   // lanes of a warp run the same FP64 instruction sequence (GB300 issues an
   // FP64 warp instruction at full cost whatever the active lanes).
-  // Two-body elements (upper triangles only), each with its resolved gather
-  // list: asm2_head[w] for the w-th element of the work order, its terms in
-  // asm2_terms[head.start ..] (see Asm2Head).
+  // Two-body elements (upper triangles only): asm2_head[w] is the w-th
+  // element of the work order, its commutator_122 terms asm2_terms[head.start
+  // ..]; the 222_ph recoupling inputs Z (one per orbit quadruple, channel and
+  // J', shared by the quadruple's elements of every J) come from the ph_terms
+  // list (see Asm2Head, PhTerm).
   const struct Asm2Head *asm2_head;
   const unsigned long long *asm2_terms;
   int n_asm2;
+  const struct PhTerm *ph_terms;
+  int n_ph;
   const int *ccf_order;    // cross-coupled elements
   int n_ccf;
   // Gather lists of the Pandya transform: element e of every CC block is
@@ -87,29 +91,39 @@ struct OneBodyTerm {
   double coef;  // (2J+1) x phase x sqrt(2)^n
 };
 
+// One J'-term of the inverse Pandya recoupling of commutator_222_ph
+// (commutators.f90:855-910) for an orbit quadruple (a,b,c,d) and one exchange
+// channel: the kernel forms
+//   Z = herm_L (W(x1,y1) + e W(x2,y2)) - herm_R (e W(y2,x2) + W(y1,x1))
+// from four cross-coupled rows (16 bits each in `rows`: x1, y1, x2, y2;
+// 0xFFFF = absent) of WCC block qx, e = (-1)^((ja+jb+jc+jd)/2).  The
+// reference's four products per J' become sum_J' {6j} Z(J') per element, with
+// the inside channel's (-1)^n2(J) applied after the sum.
+struct __align__(16) PhTerm {
+  unsigned long long rows;
+  int qx;
+  int nph;  // the exponent of e
+};
+
 // One two-body element of the assembly kernel with its operator-independent
-// gather list, resolved once per basis on the host.  The list holds, in
-// order:
-//   * n122 commutator_122 terms (commutators.f90:283-396): bits 0-27 flat
-//     index of the two-body element V, bits 28-47 flat index of the one-body
-//     element f, bit 48 sign (leg sign x pair-reordering phase), bits 49-50
-//     number of sqrt(2) factors, bit 51 V read transposed, bit 52 f read
-//     transposed (each transposed read takes the operator's herm);
-//   * n_in + n_out commutator_222_ph recoupling terms (:855-910), one per J'
-//     of the 'inside' and 'outside' channel: four 16-bit cross-coupled rows
-//     x1, y1, x2, y2 (0xFFFF = absent) of WCC block qx, which the kernel reads
-//     as W(x1,y1), W(x2,y2), W(y2,x2), W(y1,x1).  Consecutive J' of a channel
-//     have consecutive qx and consecutive 6j-table entries.
+// gather list, resolved once per basis on the host: n122 commutator_122
+// terms (:283-396) at asm2_terms[start ..]: bits 0-27 flat index of the
+// two-body element V, bits 28-47 flat index of the one-body element f, bit 48
+// sign (leg sign x pair-reordering phase), bits 49-50 number of sqrt(2)
+// factors, bit 51 V read transposed, bit 52 f read transposed (each transposed
+// read takes the operator's herm).  Its recoupling reads Z[zs .. zs + n_in)
+// (inside channel) and Z[zs + n_in .. + n_out) (outside) against consecutive
+// 6j-table entries from six1 and six2.
 struct __align__(16) Asm2Head {
   int e;       // flat index of the element
   int em;      // flat index of its mirror (JX, IX) in a square array, else -1 (== e on the diagonal)
-  int start;   // first term in asm2_terms
+  int start;   // first commutator_122 term
+  int zs;      // first recoupling input
   int six1;    // 6j-table index of the first J' of each channel
   int six2;
-  int qx;      // WCC block of the first J': inside | outside << 16
   unsigned meta;  // bits 0-4 n122, 5-9 n_in, 10-14 n_out, 15 recoupling applies,
-                  // 16 inside phase, 17 (-1)^((ji+jj+jk+jl)/2) phase, 18-19 identical
-                  // orbit pairs, 20 diagonal, 21 square array, 22 pphh array
+                  // 16 inside phase n2, 18-19 identical orbit pairs, 20 diagonal,
+                  // 21 square array, 22 pphh array
   int J2;
 };
 
@@ -195,6 +209,7 @@ struct imsrg_basis {
   imsrg::Profiler prof;
   // commutator workspace
   double *w1 = nullptr, *w2 = nullptr, *lcc = nullptr, *rcc = nullptr, *wcc = nullptr;
+  double *zph = nullptr;        // 222_ph recoupling inputs (T.n_ph)
   double *mono = nullptr;       // norb x norb monopole table of the White generator
   double *scal = nullptr;       // small device scratch for reductions (E0, norms)
   double *partials = nullptr;   // norm/mbpt2 partial sums
@@ -231,6 +246,11 @@ int build_basis(imsrg_basis *b);            // host tables + device upload (basi
 void free_basis_device(imsrg_basis *b);
 int cuda_status(cudaError_t e);
 
+// Threads per CTA of the two-body assembly; its commutator_220 partials are
+// one per CTA.
+constexpr int ASM2_THREADS = 128;
+inline int asm2_ctas(const imsrg_basis *b) { return (b->T.n_asm2 + ASM2_THREADS - 1) / ASM2_THREADS; }
+
 // launchers (kernels_*.cu); all enqueue on b->stream and bump b->launches
 int launch_cc_forward(imsrg_basis *b, const double *L, int hL, const double *R, int hR);
 int launch_gemm_fp64(imsrg_basis *b, const double *L, int hL, const double *R, int hR);
@@ -250,7 +270,7 @@ int launch_check_finite(imsrg_basis *b, const double *op, int *d_flag);
 // Intermediates of one commutator: W1, W2 (flat operators), LCC, RCC (all
 // cross-coupled blocks) and WCC.
 struct Workspace {
-  double *w1, *w2, *lcc, *rcc, *wcc;
+  double *w1, *w2, *lcc, *rcc, *wcc, *zph;
   double *e0p;  // per-CTA commutator_220 partials of the two-body kernel
 };
 int launch_commutator_fp64_ws(imsrg_basis *b, const Workspace &ws, const double *L, int hL, const double *R, int hR,

@@ -148,38 +148,33 @@ __device__ __forceinline__ double wcc_at(const double *W, int rlen, unsigned r, 
   return W[r + (long)c * rlen];
 }
 
-// One exchange channel of the inverse Pandya recoupling of commutator_222_ph
-// (commutators.f90:855-910): the +-1 factors (herm, phases) become sign flips
-// of the 6j symbol, leaving four DFMAs per J'.
-__device__ __forceinline__ double c222ph_channel(const DevTables &T, const double *WCC,
-                                                 const unsigned long long *tm, int n, int qx, long six, int n2,
-                                                 int nL, int nR, int nph, double sm) {
-  for (int k = 0; k < n; k++, qx++, six++) {
-    const unsigned long long u = tm[k];
-    const unsigned x1 = (unsigned)(u & 0xFFFF), y1 = (unsigned)((u >> 16) & 0xFFFF);
-    const unsigned x2 = (unsigned)((u >> 32) & 0xFFFF), y2 = (unsigned)(u >> 48);
-    const double *W = WCC + T.wcc_off[qx];
-    const int rl = T.cc_rlen[qx];
-    const double s6 = T.six[six];
-    const double c1 = dflip(s6, n2 ^ nL), c4 = dflip(s6, n2 ^ nR ^ 1);
-    sm = fma(c1, wcc_at(W, rl, x1, y1), sm);
-    sm = fma(dflip(c1, nph), wcc_at(W, rl, x2, y2), sm);
-    sm = fma(dflip(c4, nph), wcc_at(W, rl, y2, x2), sm);
-    sm = fma(c4, wcc_at(W, rl, y1, x1), sm);
-  }
-  return sm;
+// Recoupling inputs Z of commutator_222_ph, one thread per PhTerm.
+__global__ void __launch_bounds__(256) k_ph_inputs(DevTables T, const double *__restrict__ WCC, int hL, int hR,
+                                                   double *__restrict__ Z) {
+  const long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= T.n_ph) return;
+  const PhTerm p = T.ph_terms[t];
+  const unsigned long long u = p.rows;
+  const unsigned x1 = (unsigned)(u & 0xFFFF), y1 = (unsigned)((u >> 16) & 0xFFFF);
+  const unsigned x2 = (unsigned)((u >> 32) & 0xFFFF), y2 = (unsigned)(u >> 48);
+  const double *W = WCC + T.wcc_off[p.qx];
+  const int rl = T.cc_rlen[p.qx];
+  const double a = wcc_at(W, rl, x1, y1) + dflip(wcc_at(W, rl, x2, y2), p.nph);
+  const double c = dflip(wcc_at(W, rl, y2, x2), p.nph) + wcc_at(W, rl, y1, x1);
+  Z[t] = dflip(a, hL < 0) - dflip(c, hR < 0);
 }
 
 // Every two-body element of RES once (upper triangles of square arrays, the
 // mirror written alongside): the one-body insertions of commutator_122, the
 // antisymmetrised ladder epilogue of 222_pp_hh (:658-764) and the 222_ph
-// recoupling.
-__global__ void __launch_bounds__(256) k_assemble_2body(DevTables T, const double *__restrict__ L, int hL,
-                                                        const double *__restrict__ R, int hR,
-                                                        const double *__restrict__ W1, const double *__restrict__ W2,
-                                                        const double *__restrict__ WCC, double *RES, int hRES,
-                                                        double *e0p) {
-  __shared__ double sh220[8];
+// recoupling sum over J' of {6j} Z(J').
+__global__ void __launch_bounds__(ASM2_THREADS) k_assemble_2body(DevTables T, const double *__restrict__ L, int hL,
+                                                                 const double *__restrict__ R, int hR,
+                                                                 const double *__restrict__ W1,
+                                                                 const double *__restrict__ W2,
+                                                                 const double *__restrict__ Z, double *RES, int hRES,
+                                                                 double *e0p) {
+  __shared__ double sh220[ASM2_THREADS / 32];
   const long w = (long)blockIdx.x * blockDim.x + threadIdx.x;
   double e220 = 0.0;  // this element's commutator_220 term (pphh arrays only)
   if (w < T.n_asm2) {
@@ -215,9 +210,11 @@ __global__ void __launch_bounds__(256) k_assemble_2body(DevTables T, const doubl
     if (square) t = t - dflip(W1[em] - W2[em], npm);
     if ((meta >> 15) & 1) {
       const int n_in = (meta >> 5) & 31, n_out = (meta >> 10) & 31;
-      const int n2 = (meta >> 16) & 1, nph = (meta >> 17) & 1;
-      double sm = c222ph_channel(T, WCC, tm + n122, n_in, h.qx & 0xFFFF, h.six1, n2, nL, nR, nph, 0.0);
-      sm = c222ph_channel(T, WCC, tm + n122 + n_in, n_out, h.qx >> 16, h.six2, 0, nL, nR, nph, sm);
+      const double *z = Z + h.zs, *s1 = T.six + h.six1, *s2 = T.six + h.six2;
+      double a1 = 0.0, a2 = 0.0;
+      for (int k = 0; k < n_in; k++) a1 = fma(s1[k], z[k], a1);
+      for (int k = 0; k < n_out; k++) a2 = fma(s2[k], z[n_in + k], a2);
+      double sm = dflip(a1, (meta >> 16) & 1) + a2;
       // the reference's truncated 1/sqrt(2) literal for identical orbits
       if (nd) sm = sm * (nd == 1 ? .70710678118 : .70710678118 * .70710678118);
       t = t + sm;
@@ -231,7 +228,7 @@ __global__ void __launch_bounds__(256) k_assemble_2body(DevTables T, const doubl
     // commutator_220 (commutators.f90:409-427): -(2J+1) L_pphh R_pphh herm_R
     if (e0p && ((meta >> 22) & 1)) e220 = -L[e] * R[e] * hR * (h.J2 + 1.0);
   }
-  if (e0p) {  // per-CTA partial in a fixed order; the one-body kernel sums them
+  if (e0p) {  // per-CTA partial in a fixed order; the energy kernel sums them
     e220 = warp_sum(e220);
     if ((threadIdx.x & 31) == 0) sh220[threadIdx.x >> 5] = e220;
     __syncthreads();
@@ -452,13 +449,18 @@ int launch_gemm_fp64(imsrg_basis *b, const double *L, int hL, const double *R, i
 
 int launch_assemble_2body(imsrg_basis *b, const double *L, int hL, const double *R, int hR, double *RES, int hRES,
                           int with_e0) {
-  long n = b->T.n_asm2;
-  if (n <= 0) return IMSRG_OK;
   ProfScope ps(b, IMSRG_KERNEL_ASSEMBLE_2BODY);
-  double *e0p = (with_e0 && hL * hR == -1) ? b->partials : nullptr;
-  k_assemble_2body<<<(unsigned)((n + 255) / 256), 256, 0, b->stream>>>(b->T, L, hL, R, hR, b->w1, b->w2, b->wcc, RES,
-                                                                      hRES, e0p);
-  b->launches++;
+  if (b->T.n_ph > 0) {
+    k_ph_inputs<<<(unsigned)((b->T.n_ph + 255) / 256), 256, 0, b->stream>>>(b->T, b->wcc, hL, hR, b->zph);
+    b->launches++;
+  }
+  const long n = b->T.n_asm2;
+  if (n > 0) {
+    double *e0p = (with_e0 && hL * hR == -1) ? b->partials : nullptr;
+    k_assemble_2body<<<(unsigned)((n + ASM2_THREADS - 1) / ASM2_THREADS), ASM2_THREADS, 0, b->stream>>>(
+        b->T, L, hL, R, hR, b->w1, b->w2, b->zph, RES, hRES, e0p);
+    b->launches++;
+  }
   return cuda_status(cudaGetLastError());
 }
 
@@ -474,7 +476,7 @@ int launch_assemble_1body(imsrg_basis *b, const double *L, int hL, const double 
 
 int launch_energy(imsrg_basis *b, const double *L, int hL, const double *R, int hR, double *RES, int e220) {
   ProfScope ps(b, IMSRG_KERNEL_ASSEMBLE_1BODY);
-  k_energy<<<1, 128, 0, b->stream>>>(b->T, L, hL, R, hR, RES, e220 ? b->partials : nullptr, (b->T.n_asm2 + 255) / 256);
+  k_energy<<<1, 128, 0, b->stream>>>(b->T, L, hL, R, hR, RES, e220 ? b->partials : nullptr, asm2_ctas(b));
   b->launches++;
   return cuda_status(cudaGetLastError());
 }
@@ -504,11 +506,15 @@ int launch_commutator_fp64_ws(imsrg_basis *b, const Workspace &ws, const double 
     k_gemm_fp64<<<b->ntiles, 256, 0, st>>>(b->d_probs, b->nprobs, ops, hL, hR);
     b->launches++;
   }
-  long n2 = b->T.n_asm2;
+  if (b->T.n_ph > 0) {
+    k_ph_inputs<<<(unsigned)((b->T.n_ph + 255) / 256), 256, 0, st>>>(b->T, ws.wcc, hL, hR, ws.zph);
+    b->launches++;
+  }
+  const long n2 = b->T.n_asm2;
   if (n2 > 0) {
     double *e0p = (with_e0 && hL * hR == -1) ? ws.e0p : nullptr;
-    k_assemble_2body<<<(unsigned)((n2 + 255) / 256), 256, 0, st>>>(b->T, L, hL, R, hR, ws.w1, ws.w2, ws.wcc, RES,
-                                                                   hRES, e0p);
+    k_assemble_2body<<<(unsigned)((n2 + ASM2_THREADS - 1) / ASM2_THREADS), ASM2_THREADS, 0, st>>>(
+        b->T, L, hL, R, hR, ws.w1, ws.w2, ws.zph, RES, hRES, e0p);
     b->launches++;
   }
   const int grid1 = b->T.n_asm1_heavy + (b->T.n_asm1_light + 3) / 4;
@@ -518,7 +524,7 @@ int launch_commutator_fp64_ws(imsrg_basis *b, const Workspace &ws, const double 
   }
   if (with_e0) {
     const bool e220 = hL * hR == -1;
-    k_energy<<<1, 128, 0, st>>>(b->T, L, hL, R, hR, RES, e220 ? ws.e0p : nullptr, (b->T.n_asm2 + 255) / 256);
+    k_energy<<<1, 128, 0, st>>>(b->T, L, hL, R, hR, RES, e220 ? ws.e0p : nullptr, asm2_ctas(b));
     b->launches++;
   }
   return cuda_status(cudaGetLastError());

@@ -48,8 +48,8 @@ extern "C" int imsrg_gpu_commutator_noalloc(imsrg_basis_t *b, const double *d_L,
   if (!b || !d_L || !d_R || !d_RES) return IMSRG_ERR_INVALID;
   if ((herm_L != 1 && herm_L != -1) || (herm_R != 1 && herm_R != -1)) return IMSRG_ERR_INVALID;
   if (d_RES == d_L || d_RES == d_R) return IMSRG_ERR_INVALID;
-  long ne0p = round_up((b->T.n_asm2 + 255) / 256);
-  long need = 2 * round_up(b->nfull) + 2 * round_up(b->cc_total) + round_up(b->wcc_total) + ne0p;
+  long ne0p = round_up(imsrg::asm2_ctas(b));
+  long need = 2 * round_up(b->nfull) + 2 * round_up(b->cc_total) + round_up(b->wcc_total) + round_up(b->T.n_ph) + ne0p;
   if (need > IMSRG_NOALLOC_SCRATCH_DOUBLES) return IMSRG_ERR_TOO_LARGE;
   int dev = -1;
   cudaError_t e = cudaGetDevice(&dev);
@@ -64,7 +64,8 @@ extern "C" int imsrg_gpu_commutator_noalloc(imsrg_basis_t *b, const double *d_L,
   ws.lcc = ws.w2 + round_up(b->nfull);
   ws.rcc = ws.lcc + round_up(b->cc_total);
   ws.wcc = ws.rcc + round_up(b->cc_total);
-  ws.e0p = ws.wcc + round_up(b->wcc_total);
+  ws.zph = ws.wcc + round_up(b->wcc_total);
+  ws.e0p = ws.zph + round_up(b->T.n_ph);
   cudaStream_t st = stream ? (cudaStream_t)stream : b->stream;
   return launch_commutator_fp64_ws(b, ws, d_L, herm_L, d_R, herm_R, d_RES, -herm_L * herm_R, with_e0 ? 1 : 0, st);
 }
