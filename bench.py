@@ -254,8 +254,9 @@ def run_gpu(args, world, rank, local):
     # FP64 path beside the split-precision one, and their difference
     extra = {}
     if precision != "fp64":
-        t64, _, prof64, _ = timed("fp64", max(args.steps // 2, 3), 3)
-        extra["fp64_value"] = max(args.steps // 2, 3) / (t64 / 1e3)
+        n64 = max(min(args.steps // 2, 500), 3)
+        t64, _, prof64, _ = timed("fp64", n64, 3)
+        extra["fp64_value"] = n64 / (t64 / 1e3)
         api.commutator(O, H, RES, precision=precision)
         api.commutator(O, H, RES64, precision="fp64")
         a, b_ = RES.download(), RES64.download()
@@ -289,6 +290,31 @@ def run_gpu(args, world, rank, local):
                 "unit": "GB/s", "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)"}
     roof["frac"] = roof["achieved"] / roof["peak"]
     roof["traffic"] = _traffic_from_profiles(kname)
+    roof["algorithmic_per_launch"] = work
+    # every kernel class against its own bound: the contraction kernel against
+    # the tensor peak (FP64-equivalent algorithmic flops, and the BF16 flops the
+    # 21 digit products execute), the others against HBM with the compulsory
+    # bytes of one commutator
+    hbm_peak = peaks.get("hbm_gbs", 6795.5)
+    bf16_peak = peaks.get("bf16_tflops", 1951.5)
+    comp = _compulsory_bytes(lay)
+    alg_flops = _workload_flops(lay) + _cc_flops(orb)
+    roof_all = {}
+    for k, (ms_k, n_k) in prof.items():
+        if not n_k:
+            continue
+        per = (ms_k / 1e3) / n_k
+        if k.startswith("ozaki_mma"):
+            roof_all[k] = {"bound": "tensor", "per_launch_us": per * 1e6,
+                           "achieved_fp64_equiv_tflops": alg_flops / per / 1e12,
+                           "executed_bf16_tflops": 21 * alg_flops / per / 1e12,
+                           "frac_executed_of_bf16_peak": 21 * alg_flops / per / 1e12 / bf16_peak}
+        elif k == "gemm_fp64":
+            roof_all[k] = {"bound": "fp64", "per_launch_us": per * 1e6, "achieved_tflops": alg_flops / per / 1e12}
+        else:
+            roof_all[k] = {"bound": "hbm", "per_launch_us": per * 1e6, "achieved_gbs": comp / per / 1e9,
+                           "frac": comp / per / 1e9 / hbm_peak, "traffic": _traffic_from_profiles(k)}
+    roof["all_kernels"] = roof_all
     roof["per_launch_us"] = per_launch_s * 1e6
     roof["kernel_share"] = {k: round(v[0] / max(sum(x[0] for x in prof.values()), 1e-12), 4)
                             for k, v in prof.items() if v[1]}
@@ -298,7 +324,7 @@ def run_gpu(args, world, rank, local):
     pin_h = torch.empty(lay.nfull, dtype=torch.float64, pin_memory=True).numpy()
     pin_r = torch.empty(lay.nfull, dtype=torch.float64, pin_memory=True).numpy()
     pin_o[:], pin_h[:] = Oh, Hh
-    n_e2e = max(args.steps // 2, 3)
+    n_e2e = max(min(args.steps // 2, 500), 3)
     for _ in range(2):
         O.upload(pin_o); H.upload(pin_h); api.commutator(O, H, RES, precision=precision)
         pin_r[:] = RES.download()
@@ -358,18 +384,22 @@ def _fp64_peak_tflops():
 
 
 def _traffic_from_profiles(kname):
-    """DRAM bytes per launch of a kernel from the committed ncu summary, or None."""
+    """DRAM bytes per launch of a kernel class from the committed ncu summary
+    (profiles/dram_traffic.md, a two-column markdown table), or None."""
     try:
-        d = json.load(open(os.path.join(ROOT, "profiles", "dram_traffic.json")))
-        return d.get(kname, {}).get("bytes_per_launch")
-    except (OSError, ValueError):
-        return None
+        for line in open(os.path.join(ROOT, "profiles", "dram_traffic.md")):
+            cells = [c.strip() for c in line.strip().strip("|").split("|")]
+            if len(cells) == 2 and cells[0] == kname and cells[1].isdigit():
+                return int(cells[1])
+    except OSError:
+        pass
+    return None
 
 
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=50)
+    ap.add_argument("--steps", type=int, default=2000)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--precision", default="auto", choices=["auto", "ozaki", "fp64"])

@@ -262,9 +262,9 @@ __device__ void cta_sum(double *v, double (*sh)[8]) {
 
 // E0 = commutator_110 + commutator_220 (commutators.f90:10-33, 399-432), one
 // CTA: the 220 sum arrives as the two-body kernel's per-CTA partials.
-__global__ void __launch_bounds__(128) k_energy(DevTables T, const double *L, int hL, const double *R, int hR,
-                                                double *RES, const double *e0p, int ne0p) {
-  __shared__ double sh[4][8];
+__global__ void __launch_bounds__(1024) k_energy(DevTables T, const double *L, int hL, const double *R, int hR,
+                                                 double *RES, const double *e0p, int ne0p) {
+  __shared__ double sh[32][8];
   const int A = T.A, P = T.P, tid = threadIdx.x, nt = blockDim.x;
   const double *Lph = L + T.off_fph, *Rph = R + T.off_fph;
   double v[2] = {0.0, 0.0};
@@ -476,7 +476,7 @@ int launch_assemble_1body(imsrg_basis *b, const double *L, int hL, const double 
 
 int launch_energy(imsrg_basis *b, const double *L, int hL, const double *R, int hR, double *RES, int e220) {
   ProfScope ps(b, IMSRG_KERNEL_ASSEMBLE_1BODY);
-  k_energy<<<1, 128, 0, b->stream>>>(b->T, L, hL, R, hR, RES, e220 ? b->partials : nullptr, asm2_ctas(b));
+  k_energy<<<1, 1024, 0, b->stream>>>(b->T, L, hL, R, hR, RES, e220 ? b->partials : nullptr, asm2_ctas(b));
   b->launches++;
   return cuda_status(cudaGetLastError());
 }
@@ -524,7 +524,7 @@ int launch_commutator_fp64_ws(imsrg_basis *b, const Workspace &ws, const double 
   }
   if (with_e0) {
     const bool e220 = hL * hR == -1;
-    k_energy<<<1, 128, 0, st>>>(b->T, L, hL, R, hR, RES, e220 ? ws.e0p : nullptr, asm2_ctas(b));
+    k_energy<<<1, 1024, 0, st>>>(b->T, L, hL, R, hR, RES, e220 ? ws.e0p : nullptr, asm2_ctas(b));
     b->launches++;
   }
   return cuda_status(cudaGetLastError());

@@ -25,8 +25,9 @@
 //      level l = s + t = 2, 3, 4 and one "tail" that sums levels 5, 6, 7 in
 //      units of level 7 (the pre-scaled B planes supply 128^(7 - l)).  The
 //      accumulators are double-buffered (2 x 4 x 64 = 512 columns) so the
-//      eight epilogue warps read one tile (tcgen05.ld), combine it in int64
-//      and write FP64 while the next tile's products run.
+//      sixteen epilogue warps read one tile (tcgen05.ld), combine it in int64
+//      and write FP64 while the next tile's products run.  Each CTA takes a
+//      host-built list of (problem, tile) slots, longest first.
 //
 // Exactness: the level sums of levels 2..4 are bounded by 5 * 2^12 per
 // product and term, so those accumulators hold exact integers below 2^24
@@ -621,7 +622,7 @@ int ozaki_prepare(imsrg_basis *b) {
   int ngroups = 0;
   auto add_group = [&](int src, long off, long len) {
     int g = ngroups++;
-    for (long s0 = 0; s0 < len; s0 += 4096) chunks.push_back({g, src, off + s0, (int)std::min<long>(4096, len - s0)});
+    for (long s0 = 0; s0 < len; s0 += 1024) chunks.push_back({g, src, off + s0, (int)std::min<long>(1024, len - s0)});
     return g;
   };
   auto add_matrix = [&](int src, int group, long off, int n1, int n2) {

@@ -61,3 +61,27 @@ def test_ozaki_magnus_flow_emax2(gpu_lib, oracle_mod):
     HS, G = gpu_lib.Operator(B, 1, Hh), gpu_lib.Operator(B, -1)
     out = gpu_lib.magnus_decouple(HS, G, s_max=50.0, ds=0.5, precision="ozaki")
     assert abs(out["trace"][-1, 2] - ref["trace"][-1, 2]) < 1e-6
+
+
+def test_ozaki_magnus_flow_emax6(gpu_lib, oracle_mod):
+    """emax = 6 Magnus flow to s = 50 with every two-body contraction in split
+    precision: E0 within 1e-6 MeV of the FP64 GPU flow, which itself follows
+    the FP64 oracle (checked here over the first steps, s <= 1)."""
+    from imsrg_gpu.synth import synth_hamiltonian
+    bas, lay = make_case(6)
+    B = gpu_lib.Basis.from_dict(bas)
+    orc = oracle_mod.Oracle(**bas)
+    Hh = orc.normal_order(synth_hamiltonian(lay, 13))
+    flows = {}
+    for prec in ("fp64", "ozaki"):
+        HS, G = gpu_lib.Operator(B, 1, Hh), gpu_lib.Operator(B, -1)
+        flows[prec] = gpu_lib.magnus_decouple(HS, G, s_max=50.0, ds=0.5, precision=prec)
+    t64, toz = flows["fp64"]["trace"], flows["ozaki"]["trace"]
+    assert flows["fp64"]["steps"] == flows["ozaki"]["steps"] > 2
+    assert abs(toz[-1, 2] - t64[-1, 2]) < 1e-6
+    assert np.max(np.abs(toz[:, 2] - t64[:, 2])) < 1e-6
+    ref = orc.magnus_decouple(Hh, s_max=1.0, ds=0.5)
+    HS, G = gpu_lib.Operator(B, 1, Hh), gpu_lib.Operator(B, -1)
+    short = gpu_lib.magnus_decouple(HS, G, s_max=1.0, ds=0.5, precision="fp64")
+    assert short["steps"] == ref["steps"]
+    assert np.max(np.abs(short["trace"][:, 2] - ref["trace"][:, 2])) < 1e-8
