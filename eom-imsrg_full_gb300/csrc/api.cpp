@@ -11,6 +11,7 @@
 #include <cmath>
 #include <cstring>
 #include <new>
+#include <vector>
 
 #include "internal.h"
 
@@ -93,6 +94,14 @@ int commutator_dev(imsrg_basis *b, const double *L, int hL, const double *R, int
   IMSRG_TRY(launch_assemble_2body(b, L, hL, R, hR, RES, hRES, with_e0));
   IMSRG_TRY(join(1));
   if (with_e0) IMSRG_TRY(launch_energy(b, L, hL, R, hR, RES, hL * hR == -1));
+  return IMSRG_OK;
+}
+
+int flow_tmp_ops(imsrg_basis *b, imsrg_op **H0, imsrg_op **DG, imsrg_op **X0, imsrg_op **X1) {
+  IMSRG_TRY(tmp_op(b, 0, X0));
+  IMSRG_TRY(tmp_op(b, 1, X1));
+  IMSRG_TRY(tmp_op(b, 2, H0));
+  IMSRG_TRY(tmp_op(b, 3, DG));
   return IMSRG_OK;
 }
 
@@ -524,6 +533,71 @@ int imsrg_gpu_magnus_decouple(imsrg_op_t *HS, imsrg_op_t *G, double s_max, doubl
   if (steps_out) *steps_out = steps;
   if (ncomm) *ncomm = nct;
   return IMSRG_OK;
+}
+
+int imsrg_gpu_magnus_decouple_batch(int n, imsrg_op_t *const *HS, imsrg_op_t *const *G, double s_max, double ds,
+                                    int max_steps, int precision, double *const *traces, int *steps_out, int *ncomm,
+                                    int *status) {
+  if (n <= 0 || !HS || !G || ds <= 0.0 || max_steps < 0) return IMSRG_ERR_INVALID;
+  if (precision != IMSRG_PREC_FP64 && precision != IMSRG_PREC_OZAKI) return IMSRG_ERR_INVALID;
+  for (int i = 0; i < n; i++) {
+    IMSRG_TRY(check_op(HS[i]));
+    IMSRG_TRY(check_op(G[i]));
+    if (HS[i]->b != G[i]->b) return IMSRG_ERR_MISMATCH;
+    for (int j = 0; j < i; j++)
+      if (HS[j]->b == HS[i]->b) return IMSRG_ERR_INVALID;  // instances need their own workspace
+  }
+  std::vector<double> s(n, 0.0), crit(n, 0.0);
+  std::vector<int> steps(n, 0), nct(n, 0), st(n, IMSRG_OK);
+  for (int i = 0; i < n; i++) {
+    double e0 = 0.0, emp2 = 0.0;
+    IMSRG_TRY(imsrg::flow_graph_begin(HS[i], G[i], precision, ds, &e0, &emp2));
+    crit[i] = std::fabs(emp2);
+    if (traces && traces[i]) {
+      double *t = traces[i];
+      t[0] = 0; t[1] = 0.0; t[2] = e0; t[3] = e0 + emp2; t[4] = crit[i];
+    }
+  }
+  auto active = [&](int i) { return st[i] == IMSRG_OK && crit[i] > 1e-6 && s[i] < s_max - 1e-12 && steps[i] < max_steps; };
+  for (;;) {
+    int nact = 0;
+    for (int i = 0; i < n; i++)
+      if (active(i)) {
+        IMSRG_TRY(imsrg::flow_graph_launch(HS[i]->b));
+        nact++;
+      }
+    if (!nact) break;
+    for (int i = 0; i < n; i++) {
+      if (!active(i)) continue;
+      double e0, emp2;
+      int nc, stat;
+      IMSRG_TRY(imsrg::flow_graph_finish(HS[i]->b, &s[i], &e0, &emp2, &nc, &stat));
+      steps[i]++;
+      nct[i] += nc;
+      if (stat == IMSRG_OK && (!std::isfinite(e0) || !std::isfinite(emp2))) stat = IMSRG_ERR_NONFINITE;
+      st[i] = stat;
+      crit[i] = std::fabs(emp2);
+      if (stat == IMSRG_OK && traces && traces[i]) {
+        double *t = traces[i] + 5 * steps[i];
+        t[0] = steps[i]; t[1] = s[i]; t[2] = e0; t[3] = e0 + emp2; t[4] = crit[i];
+      }
+    }
+  }
+  int worst = IMSRG_OK;
+  for (int i = 0; i < n; i++) {
+    if (steps_out) steps_out[i] = steps[i];
+    if (ncomm) ncomm[i] = nct[i];
+    if (status) status[i] = st[i];
+    if (st[i] != IMSRG_OK && worst == IMSRG_OK) worst = st[i];
+  }
+  return worst;
+}
+
+int imsrg_gpu_magnus_decouple_graph(imsrg_op_t *HS, imsrg_op_t *G, double s_max, double ds, int max_steps,
+                                    int precision, double *trace, int *steps_out, int *ncomm) {
+  double *traces[1] = {trace};
+  return imsrg_gpu_magnus_decouple_batch(1, &HS, &G, s_max, ds, max_steps, precision, traces, steps_out, ncomm,
+                                         nullptr);
 }
 
 }  // extern "C"

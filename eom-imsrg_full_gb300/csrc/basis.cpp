@@ -821,6 +821,7 @@ int build_basis(imsrg_basis *b) {
 void free_basis_device(imsrg_basis *b) {
   if (b->stream) cudaStreamSynchronize(b->stream);
   profile_free(b);
+  flow_graph_free(b);
   ozaki_free(b);
   for (void *p : b->dev_allocs) cudaFree(p);
   b->dev_allocs.clear();

@@ -232,6 +232,8 @@ struct imsrg_basis {
   long launches = 0;
   // Ozaki split-precision engine state (allocated on first use)
   void *ozaki = nullptr;
+  // Graph of one Magnus flow step (graph.cu), built on first use
+  void *flowgraph = nullptr;
 };
 
 struct imsrg_op {
@@ -260,6 +262,7 @@ int launch_assemble_1body(imsrg_basis *b, const double *L, int hL, const double 
                           cudaStream_t st);
 int launch_energy(imsrg_basis *b, const double *L, int hL, const double *R, int hR, double *RES, int e220);
 int launch_axpby(imsrg_basis *b, const double *A, double ax, const double *B, double bx, double *C);
+int launch_axpby_dev(imsrg_basis *b, const double *A, double ax, const double *B, const double *bx, double *C);
 int launch_norm(imsrg_basis *b, const double *op, double *d_out);
 int launch_mbpt2(imsrg_basis *b, const double *H, int herm, double *d_out);
 int launch_white(imsrg_basis *b, const double *H, int hH, double *ETA);
@@ -284,6 +287,13 @@ int ozaki_slice(imsrg_basis *b, const double *L, const double *R, int part, cuda
 int ozaki_mma(imsrg_basis *b, int hL, int hR);
 int ozaki_check_error(imsrg_basis *b);  // IMSRG_ERR_TIMEOUT if a bounded device wait gave up
 void ozaki_free(imsrg_basis *b);
+
+// Magnus flow step as a CUDA graph (graph.cu)
+int flow_tmp_ops(imsrg_basis *b, imsrg_op **H0, imsrg_op **DG, imsrg_op **X0, imsrg_op **X1);  // api.cpp
+int flow_graph_begin(imsrg_op *HS, imsrg_op *G, int precision, double ds, double *e0, double *emp2);
+int flow_graph_launch(imsrg_basis *b);
+int flow_graph_finish(imsrg_basis *b, double *s, double *e0, double *emp2, int *nc, int *status);
+void flow_graph_free(imsrg_basis *b);
 
 // Records CUDA events around the launches of one kernel class while profiling
 // is enabled (profile.cpp).

@@ -15,8 +15,11 @@ namespace imsrg {
 
 namespace {
 
+// C = ax A + bx B; bx_dev, when given, supplies bx from device memory (the
+// graph-captured flow), with the same arithmetic as the scalar form.
 __global__ void k_axpby(const double *__restrict__ A, double ax, const double *__restrict__ B, double bx,
-                        double *__restrict__ C, long n) {
+                        const double *bx_dev, double *__restrict__ C, long n) {
+  if (bx_dev) bx = *bx_dev;
   long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
   long stride = (long)gridDim.x * blockDim.x;
   for (; i < n; i += stride) C[i] = A[i] * ax + B[i] * bx;
@@ -174,7 +177,16 @@ int launch_axpby(imsrg_basis *b, const double *A, double ax, const double *B, do
   long n = b->nfull;
   int grid = (int)std::min<long>((n + 255) / 256, 152 * 8);
   ProfScope ps(b, IMSRG_KERNEL_OPS);
-  k_axpby<<<grid, 256, 0, b->stream>>>(A, ax, B, bx, C, n);
+  k_axpby<<<grid, 256, 0, b->stream>>>(A, ax, B, bx, nullptr, C, n);
+  b->launches++;
+  return cuda_status(cudaGetLastError());
+}
+
+int launch_axpby_dev(imsrg_basis *b, const double *A, double ax, const double *B, const double *bx, double *C) {
+  long n = b->nfull;
+  int grid = (int)std::min<long>((n + 255) / 256, 152 * 8);
+  ProfScope ps(b, IMSRG_KERNEL_OPS);
+  k_axpby<<<grid, 256, 0, b->stream>>>(A, ax, B, 0.0, bx, C, n);
   b->launches++;
   return cuda_status(cudaGetLastError());
 }

@@ -34,6 +34,7 @@ SYMBOLS = (
     "imsrg_gpu_magnus_decouple", "imsrg_gpu_strerror", "imsrg_gpu_launch_count",
     "imsrg_gpu_basis_get_stream", "imsrg_gpu_basis_set_stream", "imsrg_gpu_profile_enable",
     "imsrg_gpu_profile_read", "imsrg_gpu_profile_reset", "imsrg_gpu_commutator_noalloc",
+    "imsrg_gpu_magnus_decouple_graph", "imsrg_gpu_magnus_decouple_batch",
 )
 
 KERNELS = ("cc_forward", "gemm_fp64", "assemble_2body", "assemble_1body", "ozaki_slice", "ozaki_mma",
@@ -99,6 +100,9 @@ def lib():
             "imsrg_gpu_profile_read": [vp, i, dp, C.POINTER(C.c_long)],
             "imsrg_gpu_profile_reset": [vp],
             "imsrg_gpu_commutator_noalloc": [vp, vp, i, vp, i, vp, i, vp],
+            "imsrg_gpu_magnus_decouple_graph": [vp, vp, d, d, i, i, dp, ip, ip],
+            "imsrg_gpu_magnus_decouple_batch": [i, C.POINTER(vp), C.POINTER(vp), d, d, i, i, C.POINTER(dp), ip, ip,
+                                                ip],
         }
         for name, args in sig.items():
             f = getattr(L, name)
@@ -351,3 +355,36 @@ def magnus_decouple(HS: Operator, G: Operator, s_max: float = 50.0, ds: float = 
            "magnus_decouple")
     n = steps.value + 1
     return dict(steps=steps.value, ncomm=nc.value, trace=trace[:5 * n].reshape(n, 5))
+
+
+def magnus_decouple_graph(HS: Operator, G: Operator, s_max: float = 50.0, ds: float = 0.5, max_steps: int = 1000,
+                          precision: str = "fp64"):
+    """magnus_decouple with one CUDA graph launch per Magnus step."""
+    trace = np.zeros(5 * (max_steps + 1))
+    steps, nc = C.c_int(0), C.c_int(0)
+    _check(lib().imsrg_gpu_magnus_decouple_graph(HS.handle, G.handle, float(s_max), float(ds), int(max_steps),
+                                                 PREC[precision], _dp(trace), C.byref(steps), C.byref(nc)),
+           "magnus_decouple_graph")
+    n = steps.value + 1
+    return dict(steps=steps.value, ncomm=nc.value, trace=trace[:5 * n].reshape(n, 5))
+
+
+def magnus_decouple_batch(HS: list, G: list, s_max: float = 50.0, ds: float = 0.5, max_steps: int = 1000,
+                          precision: str = "fp64"):
+    """Independent flows (one basis each) advanced together: a list of dicts
+    as magnus_decouple returns, each with the instance's status."""
+    n = len(HS)
+    traces = [np.zeros(5 * (max_steps + 1)) for _ in range(n)]
+    tp = (C.POINTER(C.c_double) * n)(*[_dp(t) for t in traces])
+    hs = (C.c_void_p * n)(*[h.handle for h in HS])
+    gs = (C.c_void_p * n)(*[g.handle for g in G])
+    steps, nc, st = (C.c_int * n)(), (C.c_int * n)(), (C.c_int * n)()
+    rc = lib().imsrg_gpu_magnus_decouple_batch(n, hs, gs, float(s_max), float(ds), int(max_steps), PREC[precision],
+                                               tp, steps, nc, st)
+    out = []
+    for i in range(n):
+        k = steps[i] + 1
+        out.append(dict(steps=steps[i], ncomm=nc[i], status=st[i], trace=traces[i][:5 * k].reshape(k, 5)))
+    if rc != 0 and all(o["status"] == 0 for o in out):
+        _check(rc, "magnus_decouple_batch")
+    return out

@@ -154,6 +154,23 @@ int imsrg_gpu_euler_step(imsrg_op_t *G, const imsrg_op_t *DG, double *s, double 
  * *steps = Magnus steps taken, *ncomm = commutators evaluated. */
 int imsrg_gpu_magnus_decouple(imsrg_op_t *HS, imsrg_op_t *G, double s_max, double ds, int max_steps, int precision,
                               double *trace, int *steps, int *ncomm);
+/* The same flow with each Magnus step one CUDA graph launch: the Magnus and
+ * BCH series run as device-side conditional loops, and the host reads back
+ * only the step's scalars.  Results are bit-identical to
+ * imsrg_gpu_magnus_decouple.  (No reference counterpart: the reference's
+ * loop is the host-driven one.)  The graph is built on the first call for an
+ * (HS, G, precision, ds) set and reused. */
+int imsrg_gpu_magnus_decouple_graph(imsrg_op_t *HS, imsrg_op_t *G, double s_max, double ds, int max_steps,
+                                    int precision, double *trace, int *steps, int *ncomm);
+/* n independent flows advanced together: HS[i], G[i] on their own bases
+ * (each instance needs its own workspace; a shared basis is rejected).
+ * Every round launches one step graph per unfinished instance on its
+ * basis's stream, so instances overlap on the device; each result equals its
+ * unbatched flow bit for bit.  traces[i] (optional) as above; steps, ncomm and
+ * status (optional) are n-element arrays.  Returns the first non-OK status. */
+int imsrg_gpu_magnus_decouple_batch(int n, imsrg_op_t *const *HS, imsrg_op_t *const *G, double s_max, double ds,
+                                    int max_steps, int precision, double *const *traces, int *steps, int *ncomm,
+                                    int *status);
 
 const char *imsrg_gpu_strerror(int status);
 /* Number of library kernel launches issued so far on this basis. */
