@@ -535,6 +535,150 @@ int imsrg_gpu_magnus_decouple(imsrg_op_t *HS, imsrg_op_t *G, double s_max, doubl
   return IMSRG_OK;
 }
 
+// --- tangent-linear flow -------------------------------------------------
+// The Magnus flow together with its derivative along one direction dH of the
+// input Hamiltonian (forward mode): every nested commutator T_n = [G, T_n-1]
+// carries dT_n = [dG, T_n-1] + [G, dT_n-1], the White generator its tangent,
+// and the series keep the term counts and stops of the undifferentiated flow.
+// dtrace rows: (step, s, dE0 along dH, 0, 0).
+namespace {
+
+int tangent_commutator(imsrg_basis *b, const imsrg_op *G, const imsrg_op *dG, const imsrg_op *A, const imsrg_op *dA,
+                       imsrg_op *X, imsrg_op *dX, imsrg_op *T1, int precision, int with_e0) {
+  const int h = -G->herm * A->herm;
+  X->herm = dX->herm = T1->herm = h;
+  IMSRG_TRY(imsrg::commutator_dev(b, G->d, G->herm, A->d, A->herm, X->d, h, precision, with_e0));
+  IMSRG_TRY(imsrg::commutator_dev(b, dG->d, G->herm, A->d, A->herm, T1->d, h, precision, with_e0));
+  IMSRG_TRY(imsrg::commutator_dev(b, G->d, G->herm, dA->d, A->herm, dX->d, h, precision, with_e0));
+  return imsrg::launch_axpby(b, dX->d, 1.0, T1->d, 1.0, dX->d);
+}
+
+}  // namespace
+
+int imsrg_gpu_magnus_decouple_tangent(imsrg_op_t *HS, imsrg_op_t *dHS, imsrg_op_t *G, imsrg_op_t *dG, double s_max,
+                                      double ds, int max_steps, int precision, double *trace, double *dtrace,
+                                      int *steps_out, int *ncomm) {
+  IMSRG_TRY(check_op(HS));
+  IMSRG_TRY(check_op(dHS));
+  IMSRG_TRY(check_op(G));
+  IMSRG_TRY(check_op(dG));
+  imsrg_basis *b = HS->b;
+  if (dHS->b != b || G->b != b || dG->b != b) return IMSRG_ERR_MISMATCH;
+  if (ds <= 0.0 || max_steps < 0) return IMSRG_ERR_INVALID;
+  if (precision != IMSRG_PREC_FP64 && precision != IMSRG_PREC_OZAKI) return IMSRG_ERR_INVALID;
+  imsrg_op *A, *X, *H0, *DG, *dH0, *dDG, *dA, *dX, *T1;
+  IMSRG_TRY(tmp_op(b, 0, &A));
+  IMSRG_TRY(tmp_op(b, 1, &X));
+  IMSRG_TRY(tmp_op(b, 2, &H0));
+  IMSRG_TRY(tmp_op(b, 3, &DG));
+  IMSRG_TRY(tmp_op(b, 4, &dH0));
+  IMSRG_TRY(tmp_op(b, 5, &dDG));
+  IMSRG_TRY(tmp_op(b, 6, &dA));
+  IMSRG_TRY(tmp_op(b, 7, &dX));
+  IMSRG_TRY(tmp_op(b, 8, &T1));
+  const long nf = b->nfull;
+  const double conv = 1e-6;
+  IMSRG_CUDA_TRY(cudaMemsetAsync(G->d, 0, nf * sizeof(double), b->stream));
+  IMSRG_CUDA_TRY(cudaMemsetAsync(dG->d, 0, nf * sizeof(double), b->stream));
+  G->herm = dG->herm = DG->herm = dDG->herm = -1;
+  dHS->herm = HS->herm;
+  IMSRG_TRY(imsrg::launch_white(b, HS->d, HS->herm, DG->d));
+  IMSRG_TRY(imsrg::launch_white_tangent(b, HS->d, dHS->d, HS->herm, dDG->d));
+  IMSRG_TRY(copy_dev(b, HS->d, H0->d, nf));
+  IMSRG_TRY(copy_dev(b, dHS->d, dH0->d, nf));
+  H0->herm = dH0->herm = HS->herm;
+  double s = 0.0, e0 = 0.0, de0 = 0.0, emp2 = 0.0;
+  IMSRG_TRY(imsrg_gpu_op_mbpt2(HS, &emp2));
+  IMSRG_TRY(read_scalar(b, HS->d, &e0));
+  IMSRG_TRY(read_scalar(b, dHS->d, &de0));
+  double crit = std::fabs(emp2);
+  auto row = [&](int k) {
+    if (trace) {
+      double *t = trace + 5 * k;
+      t[0] = k; t[1] = s; t[2] = e0; t[3] = e0 + emp2; t[4] = crit;
+    }
+    if (dtrace) {
+      double *t = dtrace + 5 * k;
+      t[0] = k; t[1] = s; t[2] = de0; t[3] = 0.0; t[4] = 0.0;
+    }
+  };
+  row(0);
+  int steps = 0, nct = 0;
+  while (crit > 1e-6 && s < s_max - 1e-12 && steps < max_steps) {
+    steps++;
+    // MAGNUS_EXPAND and its tangent (IMSRG_MAGNUS.f90:622-693)
+    double advals[8] = {0}, fullnorm = 0.0;
+    IMSRG_TRY(copy_dev(b, DG->d, A->d, nf));
+    IMSRG_TRY(copy_dev(b, DG->d, X->d, 1));
+    IMSRG_TRY(copy_dev(b, dDG->d, dA->d, nf));
+    IMSRG_TRY(copy_dev(b, dDG->d, dX->d, 1));
+    IMSRG_CUDA_TRY(cudaMemsetAsync(T1->d, 0, sizeof(double), b->stream));
+    A->herm = dA->herm = -1;
+    IMSRG_TRY(op_norm(b, A->d, &advals[1]));
+    IMSRG_TRY(op_norm(b, G->d, &fullnorm));
+    if (!(fullnorm < 1e-9)) {
+      int q = 1;
+      for (int i = 2; i <= 7; i++) {
+        double adnorm = advals[i - q];
+        q = (std::fabs(kMagnusCof[i - 1]) > 1e-6) ? 1 : 2;
+        if (std::fabs(adnorm / fullnorm) < conv) break;
+        IMSRG_TRY(tangent_commutator(b, G, dG, A, dA, X, dX, T1, precision, 0));
+        nct += 3;
+        IMSRG_TRY(imsrg::launch_axpby(b, DG->d, 1.0, X->d, kMagnusCof[i - 1], DG->d));
+        IMSRG_TRY(imsrg::launch_axpby(b, dDG->d, 1.0, dX->d, kMagnusCof[i - 1], dDG->d));
+        double nrm = 0.0;
+        IMSRG_TRY(op_norm(b, X->d, &nrm));
+        if (!std::isfinite(nrm)) return IMSRG_ERR_NONFINITE;
+        advals[i] = nrm * std::fabs(kMagnusCof[i - 1]);
+        IMSRG_TRY(copy_dev(b, X->d, A->d, nf));
+        IMSRG_TRY(copy_dev(b, dX->d, dA->d, nf));
+      }
+    }
+    // euler_step
+    IMSRG_TRY(imsrg::launch_axpby(b, G->d, 1.0, DG->d, ds, G->d));
+    IMSRG_TRY(imsrg::launch_axpby(b, dG->d, 1.0, dDG->d, ds, dG->d));
+    s += ds;
+    // BCH_EXPAND and its tangent (IMSRG_MAGNUS.f90:149-234)
+    IMSRG_TRY(copy_dev(b, H0->d, HS->d, nf));
+    IMSRG_TRY(copy_dev(b, dH0->d, dHS->d, nf));
+    IMSRG_TRY(copy_dev(b, H0->d, A->d, nf));
+    IMSRG_TRY(copy_dev(b, dH0->d, dA->d, nf));
+    A->herm = dA->herm = H0->herm;
+    double coef = 1.0;
+    int iw;
+    for (iw = 2; iw <= 40; iw++) {
+      coef = coef / (iw - 1.0);
+      IMSRG_TRY(tangent_commutator(b, G, dG, A, dA, X, dX, T1, precision, 1));
+      nct += 3;
+      IMSRG_TRY(imsrg::launch_axpby(b, HS->d, 1.0, X->d, coef, HS->d));
+      IMSRG_TRY(imsrg::launch_axpby(b, dHS->d, 1.0, dX->d, coef, dHS->d));
+      double nrm = 0.0;
+      IMSRG_TRY(op_norm(b, X->d, &nrm));
+      if (!std::isfinite(nrm)) return IMSRG_ERR_NONFINITE;
+      IMSRG_TRY(copy_dev(b, X->d, A->d, nf));
+      IMSRG_TRY(copy_dev(b, dX->d, dA->d, nf));
+      A->herm = dA->herm = X->herm;
+      if (nrm * coef < conv) break;
+    }
+    if (iw > 40) {
+      if (steps_out) *steps_out = steps;
+      if (ncomm) *ncomm = nct;
+      return IMSRG_ERR_NOT_CONVERGED;
+    }
+    IMSRG_TRY(imsrg::launch_white(b, HS->d, HS->herm, DG->d));
+    IMSRG_TRY(imsrg::launch_white_tangent(b, HS->d, dHS->d, HS->herm, dDG->d));
+    IMSRG_TRY(imsrg_gpu_op_mbpt2(HS, &emp2));
+    IMSRG_TRY(read_scalar(b, HS->d, &e0));
+    IMSRG_TRY(read_scalar(b, dHS->d, &de0));
+    if (!std::isfinite(e0) || !std::isfinite(emp2) || !std::isfinite(de0)) return IMSRG_ERR_NONFINITE;
+    crit = std::fabs(emp2);
+    row(steps);
+  }
+  if (steps_out) *steps_out = steps;
+  if (ncomm) *ncomm = nct;
+  return IMSRG_OK;
+}
+
 int imsrg_gpu_magnus_decouple_batch(int n, imsrg_op_t *const *HS, imsrg_op_t *const *G, double s_max, double ds,
                                     int max_steps, int precision, double *const *traces, int *steps_out, int *ncomm,
                                     int *status) {

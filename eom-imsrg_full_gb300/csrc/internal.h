@@ -210,7 +210,7 @@ struct imsrg_basis {
   // commutator workspace
   double *w1 = nullptr, *w2 = nullptr, *lcc = nullptr, *rcc = nullptr, *wcc = nullptr;
   double *zph = nullptr;        // 222_ph recoupling inputs (T.n_ph)
-  double *mono = nullptr;       // norb x norb monopole table of the White generator
+  double *mono = nullptr;       // 2 x norb x norb monopole tables of the White generator (H, tangent dH)
   double *scal = nullptr;       // small device scratch for reductions (E0, norms)
   double *partials = nullptr;   // norm/mbpt2 partial sums
   double *h_scal = nullptr;     // pinned host mirror of scal
@@ -266,6 +266,7 @@ int launch_axpby_dev(imsrg_basis *b, const double *A, double ax, const double *B
 int launch_norm(imsrg_basis *b, const double *op, double *d_out);
 int launch_mbpt2(imsrg_basis *b, const double *H, int herm, double *d_out);
 int launch_white(imsrg_basis *b, const double *H, int hH, double *ETA);
+int launch_white_tangent(imsrg_basis *b, const double *H, const double *dH, int hH, double *dETA);
 int launch_pack(imsrg_basis *b, const double *flat, double *packed);
 int launch_unpack(imsrg_basis *b, const double *packed, int herm, double *flat);
 int launch_check_finite(imsrg_basis *b, const double *op, int *d_flag);

@@ -97,42 +97,42 @@ __global__ void k_monopole(DevTables T, const double *__restrict__ H, int herm, 
   mono[t] = sm / (ja + 1.0) / (jb + 1.0);
 }
 
-// ETA one-body (fph) and two-body (pphh) elements; everything else was zeroed.
-__global__ void __launch_bounds__(256) k_white(DevTables T, const double *__restrict__ H, int herm,
-                                               const double *__restrict__ mono, double *ETA) {
-  long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
-  long nph1 = (long)T.P * T.A;
+// Element t of the White generator's support (fph elements first, then the
+// pphh arrays of all blocks): its flat index, and its energy denominator
+// (generators.f90:18-95) evaluated on operator X -- linear in X, with X's
+// monopole table.  Returns -1 for an fph element of mismatched (l,j,tz),
+// which the reference leaves at zero.
+__device__ long white_den(const DevTables &T, const double *__restrict__ X, int herm, const double *__restrict__ mono,
+                          long t, double *den) {
+  const long nph1 = (long)T.P * T.A;
   if (t < nph1) {
-    int a = (int)(t % T.P), i = (int)(t / T.P);
-    int ak = T.part_orb[a], ik = T.hole_orb[i];
-    int4 oa = T.orb[ak], oi = T.orb[ik];
-    double v = 0.0;
-    if (oa.x == oi.x && oa.y == oi.y && oa.z == oi.z) {
-      int ji = oi.x;
-      double Eden = 0.0;
-      for (int JT = 0; JT <= 2 * ji; JT += 2) Eden = Eden - (JT + 1) * v_elem(T, H, herm, ak, ik, ak, ik, JT);
-      Eden = Eden / (ji + 1.0) / (ji + 1.0);
-      Eden = Eden + H[T.off_fpp + a + (long)a * T.P] - H[T.off_fhh + i + (long)i * T.A];
-      v = H[T.off_fph + t] / Eden;
-    }
-    ETA[T.off_fph + t] = v;
-    return;
+    const int a = (int)(t % T.P), i = (int)(t / T.P);
+    const int ak = T.part_orb[a], ik = T.hole_orb[i];
+    const int4 oa = T.orb[ak], oi = T.orb[ik];
+    if (!(oa.x == oi.x && oa.y == oi.y && oa.z == oi.z)) return -1;
+    const int ji = oi.x;
+    double Eden = 0.0;
+    for (int JT = 0; JT <= 2 * ji; JT += 2) Eden = Eden - (JT + 1) * v_elem(T, X, herm, ak, ik, ak, ik, JT);
+    Eden = Eden / (ji + 1.0) / (ji + 1.0);
+    Eden = Eden + X[T.off_fpp + a + (long)a * T.P] - X[T.off_fhh + i + (long)i * T.A];
+    *den = Eden;
+    return T.off_fph + t;
   }
   t -= nph1;
   // two-body: walk the pphh arrays of all blocks
   for (int q = 0; q < T.nblocks; q++) {
-    int s = q * 6 + 2;
-    long n = (long)T.gam_n1[s] * T.gam_n2[s];
+    const int s = q * 6 + 2;
+    const long n = (long)T.gam_n1[s] * T.gam_n2[s];
     if (t >= n) {
       t -= n;
       continue;
     }
-    int np = T.gam_n1[s];
-    int IX = (int)(t % np), JX = (int)(t / np);
+    const int np = T.gam_n1[s];
+    const int IX = (int)(t % np), JX = (int)(t / np);
     const int *qp = T.qn + T.qn_start[q * 3 + 0] + 2 * IX;
     const int *qh = T.qn + T.qn_start[q * 3 + 2] + 2 * JX;
-    int a = qp[0], b = qp[1], i = qh[0], j = qh[1];
-    int N = T.norb;
+    const int a = qp[0], b = qp[1], i = qh[0], j = qh[1];
+    const int N = T.norb;
     double Eden = 0.0;
     Eden = Eden + mono[a * N + b];
     Eden = Eden + mono[i * N + j];
@@ -140,11 +140,39 @@ __global__ void __launch_bounds__(256) k_white(DevTables T, const double *__rest
     Eden = Eden - mono[a * N + j];
     Eden = Eden - mono[i * N + b];
     Eden = Eden - mono[j * N + b];
-    Eden = Eden + f_elem(T, H, herm, a, a) + f_elem(T, H, herm, b, b) - f_elem(T, H, herm, i, i) -
-           f_elem(T, H, herm, j, j);
-    long e = T.gam_off[s] + t;
-    ETA[e] = H[e] / Eden;
-    return;
+    Eden = Eden + f_elem(T, X, herm, a, a) + f_elem(T, X, herm, b, b) - f_elem(T, X, herm, i, i) -
+           f_elem(T, X, herm, j, j);
+    *den = Eden;
+    return T.gam_off[s] + t;
+  }
+  return -2;
+}
+
+// ETA one-body (fph) and two-body (pphh) elements; everything else was zeroed.
+__global__ void __launch_bounds__(256) k_white(DevTables T, const double *__restrict__ H, int herm,
+                                               const double *__restrict__ mono, double *ETA) {
+  const long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  double den = 1.0;
+  const long e = white_den(T, H, herm, mono, t, &den);
+  if (e == -1) ETA[T.off_fph + t] = 0.0;
+  else if (e >= 0) ETA[e] = H[e] / den;
+}
+
+// Tangent of the White generator along dH: eta = N / D with N and D linear in
+// H, so d eta = (dN - eta dD) / D.
+__global__ void __launch_bounds__(256) k_white_tangent(DevTables T, const double *__restrict__ H,
+                                                       const double *__restrict__ dH, int herm,
+                                                       const double *__restrict__ mono,
+                                                       const double *__restrict__ dmono, double *dETA) {
+  const long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  double den = 1.0, dden = 0.0;
+  const long e = white_den(T, H, herm, mono, t, &den);
+  if (e == -1) {
+    dETA[T.off_fph + t] = 0.0;
+  } else if (e >= 0) {
+    white_den(T, dH, herm, dmono, t, &dden);
+    const double eta = H[e] / den;
+    dETA[e] = (dH[e] - eta * dden) / den;
   }
 }
 
@@ -218,6 +246,22 @@ int launch_white(imsrg_basis *b, const double *H, int hH, double *ETA) {
   long n = (long)b->P * b->A + n3;
   if (n > 0) k_white<<<(unsigned)((n + 255) / 256), 256, 0, b->stream>>>(b->T, H, hH, mono, ETA);
   b->launches += 2;
+  return cuda_status(cudaGetLastError());
+}
+
+int launch_white_tangent(imsrg_basis *b, const double *H, const double *dH, int hH, double *dETA) {
+  double *mono = b->mono, *dmono = b->mono + (long)b->norb * b->norb;
+  ProfScope ps(b, IMSRG_KERNEL_OPS);
+  IMSRG_CUDA_TRY(cudaMemsetAsync(dETA, 0, b->nfull * sizeof(double), b->stream));
+  int nn = b->norb * b->norb;
+  k_monopole<<<(nn + 127) / 128, 128, 0, b->stream>>>(b->T, H, hH, mono);
+  k_monopole<<<(nn + 127) / 128, 128, 0, b->stream>>>(b->T, dH, hH, dmono);
+  long n3 = 0;
+  for (int q = 0; q < b->nblocks; q++) n3 += (long)b->gam_n1[q * 6 + 2] * b->gam_n2[q * 6 + 2];
+  long n = (long)b->P * b->A + n3;
+  if (n > 0)
+    k_white_tangent<<<(unsigned)((n + 255) / 256), 256, 0, b->stream>>>(b->T, H, dH, hH, mono, dmono, dETA);
+  b->launches += 3;
   return cuda_status(cudaGetLastError());
 }
 

@@ -34,7 +34,7 @@ SYMBOLS = (
     "imsrg_gpu_magnus_decouple", "imsrg_gpu_strerror", "imsrg_gpu_launch_count",
     "imsrg_gpu_basis_get_stream", "imsrg_gpu_basis_set_stream", "imsrg_gpu_profile_enable",
     "imsrg_gpu_profile_read", "imsrg_gpu_profile_reset", "imsrg_gpu_commutator_noalloc",
-    "imsrg_gpu_magnus_decouple_graph", "imsrg_gpu_magnus_decouple_batch",
+    "imsrg_gpu_magnus_decouple_graph", "imsrg_gpu_magnus_decouple_batch", "imsrg_gpu_magnus_decouple_tangent",
 )
 
 KERNELS = ("cc_forward", "gemm_fp64", "assemble_2body", "assemble_1body", "ozaki_slice", "ozaki_mma",
@@ -103,6 +103,7 @@ def lib():
             "imsrg_gpu_magnus_decouple_graph": [vp, vp, d, d, i, i, dp, ip, ip],
             "imsrg_gpu_magnus_decouple_batch": [i, C.POINTER(vp), C.POINTER(vp), d, d, i, i, C.POINTER(dp), ip, ip,
                                                 ip],
+            "imsrg_gpu_magnus_decouple_tangent": [vp, vp, vp, vp, d, d, i, i, dp, dp, ip, ip],
         }
         for name, args in sig.items():
             f = getattr(L, name)
@@ -388,3 +389,17 @@ def magnus_decouple_batch(HS: list, G: list, s_max: float = 50.0, ds: float = 0.
     if rc != 0 and all(o["status"] == 0 for o in out):
         _check(rc, "magnus_decouple_batch")
     return out
+
+
+def magnus_decouple_tangent(HS: Operator, dHS: Operator, G: Operator, dG: Operator, s_max: float = 50.0,
+                            ds: float = 0.5, max_steps: int = 1000, precision: str = "fp64"):
+    """The flow of HS with its derivative along dHS; dtrace[:, 2] is dE0."""
+    trace, dtrace = np.zeros(5 * (max_steps + 1)), np.zeros(5 * (max_steps + 1))
+    steps, nc = C.c_int(0), C.c_int(0)
+    _check(lib().imsrg_gpu_magnus_decouple_tangent(HS.handle, dHS.handle, G.handle, dG.handle, float(s_max),
+                                                   float(ds), int(max_steps), PREC[precision], _dp(trace),
+                                                   _dp(dtrace), C.byref(steps), C.byref(nc)),
+           "magnus_decouple_tangent")
+    n = steps.value + 1
+    return dict(steps=steps.value, ncomm=nc.value, trace=trace[:5 * n].reshape(n, 5),
+                dtrace=dtrace[:5 * n].reshape(n, 5))

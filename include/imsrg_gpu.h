@@ -171,6 +171,18 @@ int imsrg_gpu_magnus_decouple_graph(imsrg_op_t *HS, imsrg_op_t *G, double s_max,
 int imsrg_gpu_magnus_decouple_batch(int n, imsrg_op_t *const *HS, imsrg_op_t *const *G, double s_max, double ds,
                                     int max_steps, int precision, double *const *traces, int *steps, int *ncomm,
                                     int *status);
+/* Derivative of the flow along one direction of the input Hamiltonian
+ * (forward mode; no reference counterpart).  dHS: in = dH(0) (for
+ * H(c) = T + sum_k c_k V_k, the normal-ordered V_k gives dE0/dc_k), out =
+ * dH(s).  dG: out = dOmega(s).  Every nested commutator T_n = [G, T_n-1] of
+ * the Magnus and BCH series carries dT_n = [dG, T_n-1] + [G, dT_n-1]; the
+ * White generator carries its tangent (d eta = (dN - eta dD)/D); term counts
+ * and stops follow the undifferentiated flow, which runs alongside in HS, G
+ * exactly as in imsrg_gpu_magnus_decouple.  dtrace (optional, as trace)
+ * receives (step, s, dE0, 0, 0). */
+int imsrg_gpu_magnus_decouple_tangent(imsrg_op_t *HS, imsrg_op_t *dHS, imsrg_op_t *G, imsrg_op_t *dG, double s_max,
+                                      double ds, int max_steps, int precision, double *trace, double *dtrace,
+                                      int *steps, int *ncomm);
 
 const char *imsrg_gpu_strerror(int status);
 /* Number of library kernel launches issued so far on this basis. */
