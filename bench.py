@@ -351,6 +351,9 @@ def run_gpu(args, world, rank, local):
                        "l2": "flushed between timed steps (256 MiB write)", "nfull": lay.nfull},
             "roofline": roof, "e2e": e2e, "gpu_launches": launches, "clocks": clocks,
         }
+        if precision == "ozaki":
+            choice, us = B.split_schedule()
+            line["split_schedule_autotune"] = {"chosen_model": choice, "candidate_us": us}
         line.update(extra)
         if not args.no_flows:
             line["flow"] = flow_emax6(api, orb, lay)

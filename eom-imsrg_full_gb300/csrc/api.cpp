@@ -744,4 +744,9 @@ int imsrg_gpu_magnus_decouple_graph(imsrg_op_t *HS, imsrg_op_t *G, double s_max,
                                          nullptr);
 }
 
+int imsrg_gpu_split_schedule(imsrg_basis_t *b, int *choice, int *ncand, double *us, int max) {
+  if (!b) return IMSRG_ERR_INVALID;
+  return imsrg::ozaki_schedule_info(b, choice, ncand, us, max);
+}
+
 }  // extern "C"

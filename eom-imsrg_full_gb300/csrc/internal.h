@@ -287,6 +287,7 @@ int ozaki_prepare(imsrg_basis *b);  // plans and allocates the engine once; erro
 int ozaki_slice(imsrg_basis *b, const double *L, const double *R, int part, cudaStream_t st);
 int ozaki_mma(imsrg_basis *b, int hL, int hR);
 int ozaki_check_error(imsrg_basis *b);  // IMSRG_ERR_TIMEOUT if a bounded device wait gave up
+int ozaki_schedule_info(imsrg_basis *b, int *choice, int *ncand, double *us, int max);
 void ozaki_free(imsrg_basis *b);
 
 // Magnus flow step as a CUDA graph (graph.cu)

@@ -27,7 +27,9 @@
 //      accumulators are double-buffered (2 x 4 x 64 = 512 columns) so the
 //      sixteen epilogue warps read one tile (tcgen05.ld), combine it in int64
 //      and write FP64 while the next tile's products run.  Each CTA takes a
-//      host-built list of (problem, tile) slots, longest first.
+//      host-built list of (problem, tile) slots, longest first under a cost
+//      model that an autotuner picks by timing the kernel when the plan is
+//      built.
 //
 // Exactness: the level sums of levels 2..4 are bounded by 5 * 2^12 per
 // product and term, so those accumulators hold exact integers below 2^24
@@ -101,6 +103,14 @@ struct OzProb {
   int tiles_m, tile0, tiles;
 };
 
+// Cost models of the CTA schedule tried by the autotuner (weights of K steps,
+// of the epilogue's live outputs, and a per-tile constant).
+struct SchedModel {
+  int kw, ew, base;
+};
+constexpr int kNumSchedModels = 5;
+constexpr SchedModel kSchedModels[kNumSchedModels] = {{4, 20, 4}, {4, 0, 1}, {4, 10, 2}, {4, 40, 4}, {1, 40, 8}};
+
 struct OzPlan {
   std::vector<OzMatrix> mats;
   std::vector<OzChunk> chunks;
@@ -123,6 +133,11 @@ struct OzPlan {
   int *d_blk_mat = nullptr;  // slicing grids: matrix of each CTA's first line
   int cblocks[2] = {0, 0}, rblocks[2] = {0, 0}, blk_off[2] = {0, 0};
   int grid = 0;
+  int tune_choice = 0;                   // the schedule model the autotuner kept
+  double tune_us[kNumSchedModels] = {};  // its timings of each model
+  bool tuned = false;
+  std::vector<int> tile_ksteps, tile_live;  // per tile: K steps x terms, live outputs / 64
+  std::vector<int2> tile_slot;
   bool ok = false;
 };
 
@@ -604,6 +619,92 @@ __global__ void __launch_bounds__(OZ_THREADS, 1) k_oz_mma(const OzProb *__restri
 
 OzPlan *plan_of(imsrg_basis *b) { return (OzPlan *)b->ozaki; }
 
+// CTA schedule: longest-processing-time-first assignment of tiles to the
+// persistent CTAs under the cost model cost = kw * (K steps x terms) + ew *
+// (live outputs / 64) + base.
+void build_sched(const OzPlan *pl, const SchedModel &md, std::vector<int2> &sched, std::vector<int> &sched_off) {
+  const int tiles = (int)pl->tile_slot.size();
+  std::vector<long> cost(tiles);
+  for (int i = 0; i < tiles; i++)
+    cost[i] = (long)md.kw * pl->tile_ksteps[i] + (long)md.ew * pl->tile_live[i] + md.base;
+  std::vector<int> order(tiles);
+  for (int i = 0; i < tiles; i++) order[i] = i;
+  std::stable_sort(order.begin(), order.end(), [&](int a, int c) { return cost[a] > cost[c]; });
+  std::vector<long> load(pl->grid, 0);
+  std::vector<std::vector<int>> lists(pl->grid);
+  for (int t : order) {
+    int best = (int)(std::min_element(load.begin(), load.end()) - load.begin());
+    load[best] += cost[t];
+    lists[best].push_back(t);
+  }
+  sched.clear();
+  sched_off.assign(pl->grid + 1, 0);
+  for (int c = 0; c < pl->grid; c++) {
+    sched_off[c] = (int)sched.size();
+    for (int t : lists[c]) sched.push_back(pl->tile_slot[t]);
+  }
+  sched_off[pl->grid] = (int)sched.size();
+}
+
+int use_model(imsrg_basis *b, OzPlan *pl, int c) {
+  std::vector<int2> sched;
+  std::vector<int> sched_off;
+  build_sched(pl, kSchedModels[c], sched, sched_off);
+  IMSRG_CUDA_TRY(cudaMemcpyAsync(pl->d_sched, sched.data(), sched.size() * sizeof(int2), cudaMemcpyHostToDevice,
+                                 b->stream));
+  IMSRG_CUDA_TRY(cudaMemcpyAsync(pl->d_sched_off, sched_off.data(), sched_off.size() * sizeof(int),
+                                 cudaMemcpyHostToDevice, b->stream));
+  return cuda_status(cudaStreamSynchronize(b->stream));
+}
+
+// Autotuning of the CTA schedule, on the first split-precision commutator
+// that is not being captured into a graph: with that commutator's own digit
+// images in place, every candidate cost model is timed on the real kernel
+// (warm-up first, as clocks ramp on an idle GPU; then two interleaved passes,
+// three launches each, a candidate's time being its fastest launch) and the
+// fastest is kept.  The kernel is deterministic per tile, so the schedule
+// never changes results.
+int autotune(imsrg_basis *b, OzPlan *pl, int hL, int hR) {
+  const int smem = STAGES * STAGE_BYTES + 1024 + 256;
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  IMSRG_CUDA_TRY(cudaEventCreate(&e0));
+  IMSRG_CUDA_TRY(cudaEventCreate(&e1));
+  auto launch_timed = [&](float *ms) -> int {
+    IMSRG_CUDA_TRY(cudaEventRecord(e0, b->stream));
+    k_oz_mma<<<pl->grid, OZ_THREADS, smem, b->stream>>>(pl->d_probs, pl->nprobs, pl->d_sched, pl->d_sched_off,
+                                                       pl->d_exps, hL, hR, pl->d_err);
+    b->launches++;
+    IMSRG_CUDA_TRY(cudaEventRecord(e1, b->stream));
+    IMSRG_CUDA_TRY(cudaEventSynchronize(e1));
+    IMSRG_CUDA_TRY(cudaEventElapsedTime(ms, e0, e1));
+    return IMSRG_OK;
+  };
+  int s = IMSRG_OK;
+  for (int w = 0; w < 8 && s == IMSRG_OK; w++) {
+    float ms;
+    s = launch_timed(&ms);
+  }
+  for (int c = 0; c < kNumSchedModels; c++) pl->tune_us[c] = 1e30;
+  for (int pass = 0; pass < 2 && s == IMSRG_OK; pass++)
+    for (int c = 0; c < kNumSchedModels && s == IMSRG_OK; c++) {
+      s = use_model(b, pl, c);
+      for (int rep = 0; rep < 3 && s == IMSRG_OK; rep++) {
+        float ms = 0.f;
+        s = launch_timed(&ms);
+        pl->tune_us[c] = std::min(pl->tune_us[c], 1e3 * (double)ms);
+      }
+    }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  IMSRG_TRY(s);
+  int best = 0;
+  for (int c = 1; c < kNumSchedModels; c++)
+    if (pl->tune_us[c] < pl->tune_us[best]) best = c;
+  pl->tune_choice = best;
+  pl->tuned = true;
+  return use_model(b, pl, best);
+}
+
 }  // namespace
 
 int ozaki_prepare(imsrg_basis *b) {
@@ -740,8 +841,8 @@ int ozaki_prepare(imsrg_basis *b) {
 
   // problems: the FP64 grouped-GEMM list mapped onto images
   int tiles = 0;
-  std::vector<int> tile_cost;
-  std::vector<int2> tile_slot;  // (problem, tile within the problem) of each tile
+  std::vector<int> &tile_ksteps = pl->tile_ksteps, &tile_live = pl->tile_live;
+  std::vector<int2> &tile_slot = pl->tile_slot;  // (problem, tile within the problem) of each tile
   for (const GemmProb &gp : b->probs) {
     OzProb p{};
     p.M = gp.M;
@@ -781,10 +882,9 @@ int ozaki_prepare(imsrg_basis *b) {
     p.tile0 = tiles;
     tiles += p.tiles;
     for (int k = 0; k < p.tiles; k++) {
-      // cost in K steps: the products, plus the epilogue's conversions of
-      // the live part of the tile (a full tile costs about five K steps)
       const int live_m = std::min(TM, p.M - (k % p.tiles_m) * TM), live_n = std::min(TN, p.N - (k / p.tiles_m) * TN);
-      tile_cost.push_back(4 * p.nterms * p.ksteps + (20 * live_m * live_n) / (TM * TN) + 4);
+      tile_ksteps.push_back(p.nterms * p.ksteps);
+      tile_live.push_back((64 * live_m * live_n) / (TM * TN));
       tile_slot.push_back(make_int2((int)pl->probs.size(), k));
     }
     pl->probs.push_back(p);
@@ -794,24 +894,9 @@ int ozaki_prepare(imsrg_basis *b) {
   pl->ntiles = tiles;
   pl->grid = std::min(nsm, std::max(tiles, 1));
 
-  // longest-processing-time-first assignment of tiles to the persistent CTAs
-  std::vector<int> order(tiles);
-  for (int i = 0; i < tiles; i++) order[i] = i;
-  std::stable_sort(order.begin(), order.end(), [&](int a, int c) { return tile_cost[a] > tile_cost[c]; });
-  std::vector<long> load(pl->grid, 0);
-  std::vector<std::vector<int>> lists(pl->grid);
-  for (int t : order) {
-    int best = (int)(std::min_element(load.begin(), load.end()) - load.begin());
-    load[best] += tile_cost[t];
-    lists[best].push_back(t);
-  }
   std::vector<int2> sched;
-  std::vector<int> sched_off(pl->grid + 1, 0);
-  for (int c = 0; c < pl->grid; c++) {
-    sched_off[c] = (int)sched.size();
-    for (int t : lists[c]) sched.push_back(tile_slot[t]);
-  }
-  sched_off[pl->grid] = (int)sched.size();
+  std::vector<int> sched_off;
+  build_sched(pl, kSchedModels[0], sched, sched_off);
 
   auto up = [&](const void *h, size_t bytes, void **d) -> int {
     IMSRG_CUDA_TRY(cudaMalloc(d, std::max<size_t>(bytes, 16)));
@@ -829,6 +914,10 @@ int ozaki_prepare(imsrg_basis *b) {
   IMSRG_CUDA_TRY(cudaMemset(pl->d_err, 0, sizeof(int)));
   int smem = STAGES * STAGE_BYTES + 1024 + 256;
   IMSRG_CUDA_TRY(cudaFuncSetAttribute(k_oz_mma, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+
+  int herr = 0;
+  IMSRG_CUDA_TRY(cudaMemcpy(&herr, pl->d_err, sizeof(int), cudaMemcpyDeviceToHost));
+  if (herr) return IMSRG_ERR_TIMEOUT;
   pl->ok = true;
   return IMSRG_OK;
 }
@@ -858,6 +947,11 @@ int ozaki_slice(imsrg_basis *b, const double *L, const double *R, int part, cuda
 int ozaki_mma(imsrg_basis *b, int hL, int hR) {
   OzPlan *pl = plan_of(b);
   if (!pl) return IMSRG_ERR_INVALID;
+  if (!pl->tuned) {
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    IMSRG_CUDA_TRY(cudaStreamIsCapturing(b->stream, &cs));
+    if (cs == cudaStreamCaptureStatusNone) IMSRG_TRY(autotune(b, pl, hL, hR));
+  }
   ProfScope ps(b, IMSRG_KERNEL_OZAKI_MMA);
   const int smem = STAGES * STAGE_BYTES + 1024 + 256;
   k_oz_mma<<<pl->grid, OZ_THREADS, smem, b->stream>>>(pl->d_probs, pl->nprobs, pl->d_sched, pl->d_sched_off,
@@ -876,6 +970,16 @@ int ozaki_check_error(imsrg_basis *b) {
     cudaMemsetAsync(pl->d_err, 0, sizeof(int), b->stream);
     return IMSRG_ERR_TIMEOUT;
   }
+  return IMSRG_OK;
+}
+
+int ozaki_schedule_info(imsrg_basis *b, int *choice, int *ncand, double *us, int max) {
+  OzPlan *pl = plan_of(b);
+  if (!pl || !pl->ok || !pl->tuned) return IMSRG_ERR_INVALID;
+  if (choice) *choice = pl->tune_choice;
+  if (ncand) *ncand = kNumSchedModels;
+  if (us)
+    for (int k = 0; k < kNumSchedModels && k < max; k++) us[k] = pl->tune_us[k];
   return IMSRG_OK;
 }
 

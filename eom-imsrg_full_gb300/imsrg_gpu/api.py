@@ -35,6 +35,7 @@ SYMBOLS = (
     "imsrg_gpu_basis_get_stream", "imsrg_gpu_basis_set_stream", "imsrg_gpu_profile_enable",
     "imsrg_gpu_profile_read", "imsrg_gpu_profile_reset", "imsrg_gpu_commutator_noalloc",
     "imsrg_gpu_magnus_decouple_graph", "imsrg_gpu_magnus_decouple_batch", "imsrg_gpu_magnus_decouple_tangent",
+    "imsrg_gpu_split_schedule",
 )
 
 KERNELS = ("cc_forward", "gemm_fp64", "assemble_2body", "assemble_1body", "ozaki_slice", "ozaki_mma",
@@ -104,6 +105,7 @@ def lib():
             "imsrg_gpu_magnus_decouple_batch": [i, C.POINTER(vp), C.POINTER(vp), d, d, i, i, C.POINTER(dp), ip, ip,
                                                 ip],
             "imsrg_gpu_magnus_decouple_tangent": [vp, vp, vp, vp, d, d, i, i, dp, dp, ip, ip],
+            "imsrg_gpu_split_schedule": [vp, ip, ip, dp, i],
         }
         for name, args in sig.items():
             f = getattr(L, name)
@@ -182,6 +184,14 @@ class Basis:
             _check(lib().imsrg_gpu_profile_read(self._h, k, C.byref(ms), C.byref(n)), "profile_read")
             out[name] = (ms.value, n.value)
         return out
+
+    def split_schedule(self):
+        """(chosen model, [time in us of each candidate]) of the split engine's
+        autotuned CTA schedule; available after the first split commutator."""
+        ch, nc = C.c_int(), C.c_int()
+        us = np.zeros(16)
+        _check(lib().imsrg_gpu_split_schedule(self._h, C.byref(ch), C.byref(nc), _dp(us), 16), "split_schedule")
+        return ch.value, us[:nc.value].tolist()
 
     def block_dims(self, q):
         a, b, c = C.c_int(), C.c_int(), C.c_int()

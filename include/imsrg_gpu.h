@@ -184,6 +184,15 @@ int imsrg_gpu_magnus_decouple_tangent(imsrg_op_t *HS, imsrg_op_t *dHS, imsrg_op_
                                       double ds, int max_steps, int precision, double *trace, double *dtrace,
                                       int *steps, int *ncomm);
 
+/* The split-precision engine's CTA schedule (no reference counterpart): when
+ * a basis first runs a split-precision commutator, the engine times its
+ * persistent tensor-core kernel under *ncand candidate tile-cost models and
+ * keeps the fastest (*choice); us[k] (up to max entries) receives each
+ * candidate's time in microseconds.  IMSRG_ERR_INVALID before that first
+ * use.  That first use allocates and synchronises, so it must not happen
+ * inside a stream capture. */
+int imsrg_gpu_split_schedule(imsrg_basis_t *b, int *choice, int *ncand, double *us, int max);
+
 const char *imsrg_gpu_strerror(int status);
 /* Number of library kernel launches issued so far on this basis. */
 int imsrg_gpu_launch_count(const imsrg_basis_t *b, long *count);

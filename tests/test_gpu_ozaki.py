@@ -85,3 +85,14 @@ def test_ozaki_magnus_flow_emax6(gpu_lib, oracle_mod):
     short = gpu_lib.magnus_decouple(HS, G, s_max=1.0, ds=0.5, precision="fp64")
     assert short["steps"] == ref["steps"]
     assert np.max(np.abs(short["trace"][:, 2] - ref["trace"][:, 2])) < 1e-8
+
+
+def test_split_schedule_is_autotuned(gpu_lib):
+    bas, lay, B, Hh, Oh = _pair(gpu_lib, 4)
+    with pytest.raises(gpu_lib.ImsrgError):
+        B.split_schedule()
+    O, H, R = gpu_lib.Operator(B, -1, Oh), gpu_lib.Operator(B, 1, Hh), gpu_lib.Operator(B, 1)
+    gpu_lib.commutator(O, H, R, precision="ozaki")
+    choice, us = B.split_schedule()
+    assert len(us) >= 2 and all(t > 0 for t in us)
+    assert us[choice] == min(us)
