@@ -60,11 +60,11 @@ int tmp_op(imsrg_basis *b, int k, imsrg_op **out) {
 
 namespace imsrg {
 
-int commutator_dev(imsrg_basis *b, const double *L, int hL, const double *R, int hR, double *RES, int hRES,
-                   int precision, int with_e0) {
-  if (precision != IMSRG_PREC_FP64 && precision != IMSRG_PREC_OZAKI) return IMSRG_ERR_INVALID;
-  // Independent launches run on the side stream, forked from and joined back
-  // into the basis stream, so the call stays one ordered unit on that stream.
+// The launch sequence of one commutator.  Independent launches run on the
+// side stream, forked from and joined back into the basis stream with events,
+// so the call stays one ordered unit on that stream.
+int commutator_launches(imsrg_basis *b, const double *L, int hL, const double *R, int hR, double *RES, int hRES,
+                        int precision, int with_e0) {
   auto fork = [&](int k) -> int {
     IMSRG_CUDA_TRY(cudaEventRecord(b->ev_fork[k], b->stream));
     IMSRG_CUDA_TRY(cudaStreamWaitEvent(b->side, b->ev_fork[k], 0));
@@ -76,7 +76,6 @@ int commutator_dev(imsrg_basis *b, const double *L, int hL, const double *R, int
     return IMSRG_OK;
   };
   if (precision == IMSRG_PREC_OZAKI) {
-    IMSRG_TRY(ozaki_prepare(b));
     // digit images of L and R beside the Pandya transform
     IMSRG_TRY(fork(0));
     IMSRG_TRY(ozaki_slice(b, L, R, 0, b->side));
@@ -95,6 +94,55 @@ int commutator_dev(imsrg_basis *b, const double *L, int hL, const double *R, int
   IMSRG_TRY(join(1));
   if (with_e0) IMSRG_TRY(launch_energy(b, L, hL, R, hR, RES, hL * hR == -1));
   return IMSRG_OK;
+}
+
+namespace {
+constexpr size_t kCommGraphs = 8;
+}
+
+// One commutator.  Outside profiling and outside a caller's stream capture,
+// the launch sequence of each argument set is captured once into a CUDA graph
+// and replayed (one launch instead of ~12, and no host work per kernel); the
+// graph runs the same kernels on the same data, so results are unchanged.
+int commutator_dev(imsrg_basis *b, const double *L, int hL, const double *R, int hR, double *RES, int hRES,
+                   int precision, int with_e0) {
+  if (precision != IMSRG_PREC_FP64 && precision != IMSRG_PREC_OZAKI) return IMSRG_ERR_INVALID;
+  if (precision == IMSRG_PREC_OZAKI) IMSRG_TRY(ozaki_prepare(b));
+  cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+  IMSRG_CUDA_TRY(cudaStreamIsCapturing(b->stream, &cs));
+  const bool graphable = !b->prof.on && cs == cudaStreamCaptureStatusNone &&
+                         (precision != IMSRG_PREC_OZAKI || ozaki_tuned(b));
+  if (!graphable) return commutator_launches(b, L, hL, R, hR, RES, hRES, precision, with_e0);
+  b->comm_calls++;
+  for (imsrg_basis::CommGraph &g : b->comm_graphs)
+    if (g.L == L && g.R == R && g.RES == RES && g.hL == hL && g.hR == hR && g.hRES == hRES &&
+        g.precision == precision && g.with_e0 == with_e0) {
+      g.last_use = b->comm_calls;
+      b->launches += g.nlaunch;
+      return cuda_status(cudaGraphLaunch(g.exec, b->stream));
+    }
+  // capture the sequence of this argument set
+  IMSRG_CUDA_TRY(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
+  const long launches0 = b->launches;
+  int s = commutator_launches(b, L, hL, R, hR, RES, hRES, precision, with_e0);
+  cudaGraph_t graph = nullptr;
+  cudaError_t e = cudaStreamEndCapture(b->stream, &graph);
+  IMSRG_TRY(s);
+  IMSRG_CUDA_TRY(e);
+  cudaGraphExec_t exec = nullptr;
+  e = cudaGraphInstantiate(&exec, graph, 0);
+  cudaGraphDestroy(graph);
+  IMSRG_CUDA_TRY(e);
+  if (b->comm_graphs.size() >= kCommGraphs) {  // evict the least recently used
+    size_t lru = 0;
+    for (size_t k = 1; k < b->comm_graphs.size(); k++)
+      if (b->comm_graphs[k].last_use < b->comm_graphs[lru].last_use) lru = k;
+    cudaGraphExecDestroy(b->comm_graphs[lru].exec);
+    b->comm_graphs.erase(b->comm_graphs.begin() + lru);
+  }
+  b->comm_graphs.push_back({L, R, RES, hL, hR, hRES, precision, with_e0, exec, b->comm_calls,
+                            b->launches - launches0});
+  return cuda_status(cudaGraphLaunch(exec, b->stream));
 }
 
 int flow_tmp_ops(imsrg_basis *b, imsrg_op **H0, imsrg_op **DG, imsrg_op **X0, imsrg_op **X1) {

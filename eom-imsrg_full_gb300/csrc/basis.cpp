@@ -822,6 +822,8 @@ void free_basis_device(imsrg_basis *b) {
   if (b->stream) cudaStreamSynchronize(b->stream);
   profile_free(b);
   flow_graph_free(b);
+  for (imsrg_basis::CommGraph &g : b->comm_graphs) cudaGraphExecDestroy(g.exec);
+  b->comm_graphs.clear();
   ozaki_free(b);
   for (void *p : b->dev_allocs) cudaFree(p);
   b->dev_allocs.clear();

@@ -234,6 +234,17 @@ struct imsrg_basis {
   void *ozaki = nullptr;
   // Graph of one Magnus flow step (graph.cu), built on first use
   void *flowgraph = nullptr;
+  // Captured commutator launch sequences, one per argument set (api.cpp)
+  struct CommGraph {
+    const double *L, *R;
+    double *RES;
+    int hL, hR, hRES, precision, with_e0;
+    cudaGraphExec_t exec;
+    long last_use;
+    long nlaunch;  // library kernel launches in the sequence
+  };
+  std::vector<CommGraph> comm_graphs;
+  long comm_calls = 0;
 };
 
 struct imsrg_op {
@@ -287,6 +298,7 @@ int ozaki_prepare(imsrg_basis *b);  // plans and allocates the engine once; erro
 int ozaki_slice(imsrg_basis *b, const double *L, const double *R, int part, cudaStream_t st);
 int ozaki_mma(imsrg_basis *b, int hL, int hR);
 int ozaki_check_error(imsrg_basis *b);  // IMSRG_ERR_TIMEOUT if a bounded device wait gave up
+bool ozaki_tuned(imsrg_basis *b);       // the CTA schedule has been autotuned
 int ozaki_schedule_info(imsrg_basis *b, int *choice, int *ncand, double *us, int max);
 void ozaki_free(imsrg_basis *b);
 

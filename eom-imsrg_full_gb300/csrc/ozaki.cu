@@ -973,6 +973,11 @@ int ozaki_check_error(imsrg_basis *b) {
   return IMSRG_OK;
 }
 
+bool ozaki_tuned(imsrg_basis *b) {
+  OzPlan *pl = plan_of(b);
+  return pl && pl->ok && pl->tuned;
+}
+
 int ozaki_schedule_info(imsrg_basis *b, int *choice, int *ncand, double *us, int max) {
   OzPlan *pl = plan_of(b);
   if (!pl || !pl->ok || !pl->tuned) return IMSRG_ERR_INVALID;

@@ -239,8 +239,11 @@ class Operator:
         assert flat.size == self.basis.nfull
         _check(lib().imsrg_gpu_op_upload_flat(self._h, _dp(flat)), "op_upload_flat")
 
-    def download(self) -> np.ndarray:
-        out = np.empty(self.basis.nfull)
+    def download(self, out: np.ndarray = None) -> np.ndarray:
+        """The flat layout; into `out` (e.g. a pinned buffer) when given."""
+        if out is None:
+            out = np.empty(self.basis.nfull)
+        assert out.dtype == np.float64 and out.flags.c_contiguous and out.size == self.basis.nfull
         _check(lib().imsrg_gpu_op_download_flat(self._h, _dp(out)), "op_download_flat")
         return out
 
