@@ -76,12 +76,17 @@ int commutator_launches(imsrg_basis *b, const double *L, int hL, const double *R
     return IMSRG_OK;
   };
   if (precision == IMSRG_PREC_OZAKI) {
-    // digit images of L and R beside the Pandya transform
+    // digit images of L and of R on the two side streams, beside the Pandya
+    // transform and the images of LCC and RCC
     IMSRG_TRY(fork(0));
+    IMSRG_CUDA_TRY(cudaStreamWaitEvent(b->side2, b->ev_fork[0], 0));
     IMSRG_TRY(ozaki_slice(b, L, R, 0, b->side));
+    IMSRG_TRY(ozaki_slice(b, L, R, 1, b->side2));
     IMSRG_TRY(launch_cc_forward(b, L, hL, R, hR));
-    IMSRG_TRY(ozaki_slice(b, L, R, 1, b->stream));
+    IMSRG_TRY(ozaki_slice(b, L, R, 2, b->stream));
     IMSRG_TRY(join(0));
+    IMSRG_CUDA_TRY(cudaEventRecord(b->ev_join2, b->side2));
+    IMSRG_CUDA_TRY(cudaStreamWaitEvent(b->stream, b->ev_join2, 0));
     IMSRG_TRY(ozaki_mma(b, hL, hR));
   } else {
     IMSRG_TRY(launch_cc_forward(b, L, hL, R, hR));

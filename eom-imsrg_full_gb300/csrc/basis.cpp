@@ -354,6 +354,8 @@ int build_basis(imsrg_basis *b) {
   IMSRG_CUDA_TRY(cudaStreamCreateWithFlags(&b->own_stream, cudaStreamNonBlocking));
   b->stream = b->own_stream;
   IMSRG_CUDA_TRY(cudaStreamCreateWithFlags(&b->side, cudaStreamNonBlocking));
+  IMSRG_CUDA_TRY(cudaStreamCreateWithFlags(&b->side2, cudaStreamNonBlocking));
+  IMSRG_CUDA_TRY(cudaEventCreateWithFlags(&b->ev_join2, cudaEventDisableTiming));
   for (int k = 0; k < 2; k++) {
     IMSRG_CUDA_TRY(cudaEventCreateWithFlags(&b->ev_fork[k], cudaEventDisableTiming));
     IMSRG_CUDA_TRY(cudaEventCreateWithFlags(&b->ev_join[k], cudaEventDisableTiming));
@@ -833,7 +835,10 @@ void free_basis_device(imsrg_basis *b) {
   if (b->own_stream) cudaStreamDestroy(b->own_stream);
   b->stream = b->own_stream = nullptr;
   if (b->side) cudaStreamDestroy(b->side);
-  b->side = nullptr;
+  if (b->side2) cudaStreamDestroy(b->side2);
+  b->side = b->side2 = nullptr;
+  if (b->ev_join2) cudaEventDestroy(b->ev_join2);
+  b->ev_join2 = nullptr;
   for (int k = 0; k < 2; k++) {
     if (b->ev_fork[k]) cudaEventDestroy(b->ev_fork[k]);
     if (b->ev_join[k]) cudaEventDestroy(b->ev_join[k]);

@@ -201,10 +201,10 @@ struct imsrg_basis {
   std::vector<void *> dev_allocs;
   cudaStream_t stream = nullptr;      // where all work is enqueued
   cudaStream_t own_stream = nullptr;  // the library's own stream
-  // A second library stream for independent launches inside one commutator,
-  // forked from and joined back into `stream` with events.
-  cudaStream_t side = nullptr;
-  cudaEvent_t ev_fork[2] = {nullptr, nullptr}, ev_join[2] = {nullptr, nullptr};
+  // Library streams for independent launches inside one commutator, forked
+  // from and joined back into `stream` with events.
+  cudaStream_t side = nullptr, side2 = nullptr;
+  cudaEvent_t ev_fork[2] = {nullptr, nullptr}, ev_join[2] = {nullptr, nullptr}, ev_join2 = nullptr;
   int device = 0;
   imsrg::Profiler prof;
   // commutator workspace
@@ -293,8 +293,8 @@ int launch_commutator_fp64_ws(imsrg_basis *b, const Workspace &ws, const double 
 
 // Ozaki split-precision contraction engine (ozaki.cu)
 int ozaki_prepare(imsrg_basis *b);  // plans and allocates the engine once; errors if unavailable
-// part 0: exponents and digit images of L and R; part 1: of LCC and RCC (after
-// the Pandya transform).  ozaki_mma then runs every contraction.
+// part 0: exponents and digit images of L; part 1: of R; part 2: of LCC and
+// RCC (after the Pandya transform).  ozaki_mma then runs every contraction.
 int ozaki_slice(imsrg_basis *b, const double *L, const double *R, int part, cudaStream_t st);
 int ozaki_mma(imsrg_basis *b, int hL, int hR);
 int ozaki_check_error(imsrg_basis *b);  // IMSRG_ERR_TIMEOUT if a bounded device wait gave up

@@ -126,12 +126,13 @@ struct OzPlan {
   long img_bytes[4] = {0, 0, 0, 0};
   int nmats = 0, ngroups = 0, nchunks = 0, nprobs = 0, ntiles = 0;
   int lines_r = 0, lines_c = 0;
-  // The operands fall in two parts that are sliced separately: part 0 = L and
-  // R (available at once), part 1 = LCC and RCC (after the Pandya transform).
-  // Groups, chunks and image lines of part 0 come first.
-  int groups0 = 0, chunks0 = 0, lines_c0 = 0, lines_r0 = 0;
+  // The operands fall in three parts that are sliced separately (and
+  // concurrently): part 0 = L, part 1 = R (both available at once), part 2 =
+  // LCC and RCC (after the Pandya transform).  Groups, chunks and image lines
+  // are numbered part by part; part k owns [x_lo[k], x_lo[k + 1]).
+  int group_lo[4] = {0, 0, 0, 0}, chunk_lo[4] = {0, 0, 0, 0}, linec_lo[4] = {0, 0, 0, 0}, liner_lo[4] = {0, 0, 0, 0};
   int *d_blk_mat = nullptr;  // slicing grids: matrix of each CTA's first line
-  int cblocks[2] = {0, 0}, rblocks[2] = {0, 0}, blk_off[2] = {0, 0};
+  int cblocks[3] = {0, 0, 0}, rblocks[3] = {0, 0, 0}, blk_off[3] = {0, 0, 0};
   int grid = 0;
   int tune_choice = 0;                   // the schedule model the autotuner kept
   double tune_us[kNumSchedModels] = {};  // its timings of each model
@@ -248,9 +249,13 @@ __global__ void __launch_bounds__(256) k_oz_exponents(const OzChunk *chunks, con
   __shared__ int sh[8];
   OzChunk c = chunks[blockIdx.x];
   const double *src = (c.src == 0 ? L : c.src == 1 ? R : c.src == 2 ? LCC : RCC) + c.off;
+  // chunks hold at most 4 x 256 elements: four independent loads per thread
   int m = 0;
-  for (int i = threadIdx.x; i < c.len; i += blockDim.x)
-    m = max(m, (int)((__double_as_longlong(src[i]) >> 52) & 0x7FF));
+#pragma unroll
+  for (int k = 0; k < 4; k++) {
+    const int i = threadIdx.x + k * 256;
+    if (i < c.len) m = max(m, (int)((__double_as_longlong(src[i]) >> 52) & 0x7FF));
+  }
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) m = max(m, __shfl_xor_sync(0xffffffffu, m, o));
   if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = m;
@@ -738,14 +743,17 @@ int ozaki_prepare(imsrg_basis *b) {
     mat_of[{src, off}] = (int)pl->mats.size();
     pl->mats.push_back(m);
   };
-  for (int src = 0; src < 2; src++)
+  for (int src = 0; src < 2; src++) {
+    pl->group_lo[src] = ngroups;
+    pl->chunk_lo[src] = (int)chunks.size();
     for (int q = 0; q < b->nblocks; q++) {
       long o0 = b->gam_off[q * 6], o1 = (q + 1 < b->nblocks) ? b->gam_off[q * 6 + 6] : b->nfull;
       int g = add_group(src, o0, o1 - o0);
       for (int k = 0; k < 6; k++) add_matrix(src, g, b->gam_off[q * 6 + k], b->gam_n1[q * 6 + k], b->gam_n2[q * 6 + k]);
     }
-  pl->groups0 = ngroups;
-  pl->chunks0 = (int)chunks.size();
+  }
+  pl->group_lo[2] = ngroups;
+  pl->chunk_lo[2] = (int)chunks.size();
   for (int src = 2; src < 4; src++)
     for (int q1 = 0; q1 < b->ccblocks; q1++) {
       long len = (long)b->cc_rlen[q1] * b->cc_nph[q1];
@@ -754,6 +762,8 @@ int ozaki_prepare(imsrg_basis *b) {
     }
   pl->ngroups = ngroups;
   pl->nchunks = (int)chunks.size();
+  pl->group_lo[3] = ngroups;
+  pl->chunk_lo[3] = (int)chunks.size();
 
   // which images each matrix needs: op(A) = X reads X's R image, X^T its C
   // image; op(B) = Y reads Y's C image, Y^T its R image.  An image read as a B
@@ -802,20 +812,24 @@ int ozaki_prepare(imsrg_basis *b) {
   }
   pl->lines_r = lines_r;
   pl->lines_c = lines_c;
-  // first lines of part 1 (the first LCC matrix)
-  pl->lines_c0 = lines_c;
-  pl->lines_r0 = lines_r;
-  for (const OzMatrix &m : pl->mats)
-    if (m.src >= 2) {
-      pl->lines_c0 = m.line_c0;
-      pl->lines_r0 = m.line_r0;
-      break;
-    }
+  // first lines of each part (matrices are ordered L, R, then LCC and RCC)
+  for (int part = 0; part < 3; part++) {
+    pl->linec_lo[part] = lines_c;
+    pl->liner_lo[part] = lines_r;
+    for (const OzMatrix &m : pl->mats)
+      if ((part < 2 && m.src == part) || (part == 2 && m.src >= 2)) {
+        pl->linec_lo[part] = m.line_c0;
+        pl->liner_lo[part] = m.line_r0;
+        break;
+      }
+  }
+  pl->linec_lo[3] = lines_c;
+  pl->liner_lo[3] = lines_r;
   // per part: the matrix of each 256-line CTA's first line (C lines, then R lines)
   std::vector<int> blk_mat;
-  for (int part = 0; part < 2; part++) {
-    const int c_lo = part ? pl->lines_c0 : 0, c_hi = part ? lines_c : pl->lines_c0;
-    const int r_lo = part ? pl->lines_r0 : 0, r_hi = part ? lines_r : pl->lines_r0;
+  for (int part = 0; part < 3; part++) {
+    const int c_lo = pl->linec_lo[part], c_hi = pl->linec_lo[part + 1];
+    const int r_lo = pl->liner_lo[part], r_hi = pl->liner_lo[part + 1];
     pl->cblocks[part] = (c_hi - c_lo + 255) / 256;
     pl->rblocks[part] = (r_hi - r_lo + 255) / 256;
     pl->blk_off[part] = (int)blk_mat.size();
@@ -926,8 +940,9 @@ int ozaki_slice(imsrg_basis *b, const double *L, const double *R, int part, cuda
   OzPlan *pl = plan_of(b);
   if (!pl) return IMSRG_ERR_INVALID;
   ProfScope ps(b, IMSRG_KERNEL_OZAKI_SLICE, st);
-  const int g0 = part ? pl->groups0 : 0, g1 = part ? pl->ngroups : pl->groups0;
-  const int k0 = part ? pl->chunks0 : 0, k1 = part ? pl->nchunks : pl->chunks0;
+  if (part < 0 || part > 2) return IMSRG_ERR_INVALID;
+  const int g0 = pl->group_lo[part], g1 = pl->group_lo[part + 1];
+  const int k0 = pl->chunk_lo[part], k1 = pl->chunk_lo[part + 1];
   if (g1 > g0) IMSRG_CUDA_TRY(cudaMemsetAsync(pl->d_exps + g0, 0, (g1 - g0) * sizeof(int), st));
   if (k1 > k0) {
     k_oz_exponents<<<k1 - k0, 256, 0, st>>>(pl->d_chunks + k0, L, R, b->lcc, b->rcc, pl->d_exps);
@@ -936,9 +951,9 @@ int ozaki_slice(imsrg_basis *b, const double *L, const double *R, int part, cuda
   const int nblk = pl->cblocks[part] + pl->rblocks[part];
   if (nblk) {
     k_oz_slice<<<nblk, 256, 0, st>>>(pl->d_mats, pl->nmats, pl->d_blk_mat + pl->blk_off[part], pl->cblocks[part],
-                                     part ? pl->lines_c0 : 0, part ? pl->lines_c : pl->lines_c0,
-                                     part ? pl->lines_r0 : 0, part ? pl->lines_r : pl->lines_r0, L, R, b->lcc,
-                                     b->rcc, pl->d_exps, pl->img[0], pl->img[1], pl->img[2], pl->img[3]);
+                                     pl->linec_lo[part], pl->linec_lo[part + 1], pl->liner_lo[part],
+                                     pl->liner_lo[part + 1], L, R, b->lcc, b->rcc, pl->d_exps, pl->img[0],
+                                     pl->img[1], pl->img[2], pl->img[3]);
     b->launches++;
   }
   return cuda_status(cudaGetLastError());
