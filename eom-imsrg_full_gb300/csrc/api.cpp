@@ -56,6 +56,27 @@ int tmp_op(imsrg_basis *b, int k, imsrg_op **out) {
   return IMSRG_OK;
 }
 
+// The generator of the flow from H into ETA (herm -1): build_gs_white
+// (generators.f90:4-106), build_gs_atan (:162-266) or build_gs_w2 (:109-159:
+// ETA = 1.5 atan(H) + 0.5 atanxx(H, [atan(H), H])).
+int generator_dev(imsrg_basis *b, const double *H, int hH, double *ETA, int generator, int precision) {
+  if (generator == IMSRG_GEN_WHITE) return imsrg::launch_white(b, H, hH, ETA);
+  if (generator == IMSRG_GEN_ATAN) return imsrg::launch_generator(b, H, hH, H, 1, ETA);
+  if (generator != IMSRG_GEN_W2) return IMSRG_ERR_INVALID;
+  imsrg_op *E1, *H2, *E2;
+  IMSRG_TRY(tmp_op(b, 9, &E1));
+  IMSRG_TRY(tmp_op(b, 10, &H2));
+  IMSRG_TRY(tmp_op(b, 11, &E2));
+  IMSRG_CUDA_TRY(cudaMemsetAsync(E1->d, 0, sizeof(double), b->stream));
+  IMSRG_CUDA_TRY(cudaMemsetAsync(E2->d, 0, sizeof(double), b->stream));
+  IMSRG_TRY(imsrg::launch_generator(b, H, hH, H, 1, E1->d));
+  E1->herm = E2->herm = -1;
+  H2->herm = hH;
+  IMSRG_TRY(imsrg::commutator_dev(b, E1->d, -1, H, hH, H2->d, hH, precision, 1));
+  IMSRG_TRY(imsrg::launch_generator(b, H, hH, H2->d, 1, E2->d));
+  return imsrg::launch_axpby(b, E1->d, 1.5, E2->d, 0.5, ETA);
+}
+
 }  // namespace
 
 namespace imsrg {
@@ -536,8 +557,35 @@ int imsrg_gpu_bch_expand(imsrg_op_t *HS, const imsrg_op_t *G, const imsrg_op_t *
   return (iw > 40) ? IMSRG_ERR_NOT_CONVERGED : IMSRG_OK;
 }
 
+int imsrg_gpu_build_gs_atan(const imsrg_op_t *H, imsrg_op_t *ETA) {
+  IMSRG_TRY(check_op(H));
+  IMSRG_TRY(check_op(ETA));
+  if (H->b != ETA->b) return IMSRG_ERR_MISMATCH;
+  if (H == ETA) return IMSRG_ERR_INVALID;
+  ETA->herm = -1;
+  return generator_dev(H->b, H->d, H->herm, ETA->d, IMSRG_GEN_ATAN, IMSRG_PREC_FP64);
+}
+
+int imsrg_gpu_build_gs_w2(const imsrg_op_t *H, imsrg_op_t *ETA, int precision) {
+  IMSRG_TRY(check_op(H));
+  IMSRG_TRY(check_op(ETA));
+  if (H->b != ETA->b) return IMSRG_ERR_MISMATCH;
+  if (H == ETA) return IMSRG_ERR_INVALID;
+  if (precision != IMSRG_PREC_FP64 && precision != IMSRG_PREC_OZAKI) return IMSRG_ERR_INVALID;
+  ETA->herm = -1;
+  return generator_dev(H->b, H->d, H->herm, ETA->d, IMSRG_GEN_W2, precision);
+}
+
 int imsrg_gpu_magnus_decouple(imsrg_op_t *HS, imsrg_op_t *G, double s_max, double ds, int max_steps, int precision,
                               double *trace, int *steps_out, int *ncomm) {
+  return imsrg_gpu_magnus_decouple_gen(HS, G, IMSRG_GEN_WHITE, s_max, ds, max_steps, precision, trace, steps_out,
+                                       ncomm);
+}
+
+int imsrg_gpu_magnus_decouple_gen(imsrg_op_t *HS, imsrg_op_t *G, int generator, double s_max, double ds,
+                                  int max_steps, int precision, double *trace, int *steps_out, int *ncomm) {
+  if (generator != IMSRG_GEN_WHITE && generator != IMSRG_GEN_ATAN && generator != IMSRG_GEN_W2)
+    return IMSRG_ERR_INVALID;
   IMSRG_TRY(check_op(HS));
   IMSRG_TRY(check_op(G));
   if (HS->b != G->b) return IMSRG_ERR_MISMATCH;
@@ -550,7 +598,7 @@ int imsrg_gpu_magnus_decouple(imsrg_op_t *HS, imsrg_op_t *G, double s_max, doubl
   IMSRG_CUDA_TRY(cudaMemsetAsync(DG->d, 0, b->nfull * sizeof(double), b->stream));
   G->herm = -1;
   DG->herm = -1;
-  IMSRG_TRY(imsrg::launch_white(b, HS->d, HS->herm, DG->d));
+  IMSRG_TRY(generator_dev(b, HS->d, HS->herm, DG->d, generator, precision));
   IMSRG_TRY(copy_dev(b, HS->d, H0->d, b->nfull));
   H0->herm = HS->herm;
   double s = 0.0, e0 = 0.0, emp2 = 0.0;
@@ -573,7 +621,7 @@ int imsrg_gpu_magnus_decouple(imsrg_op_t *HS, imsrg_op_t *G, double s_max, doubl
       if (ncomm) *ncomm = nct;
       return st;
     }
-    IMSRG_TRY(imsrg::launch_white(b, HS->d, HS->herm, DG->d));
+    IMSRG_TRY(generator_dev(b, HS->d, HS->herm, DG->d, generator, precision));
     IMSRG_TRY(imsrg_gpu_op_mbpt2(HS, &emp2));
     IMSRG_TRY(read_scalar(b, HS->d, &e0));
     if (!std::isfinite(e0) || !std::isfinite(emp2)) return IMSRG_ERR_NONFINITE;

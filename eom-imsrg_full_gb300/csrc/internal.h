@@ -277,6 +277,7 @@ int launch_axpby_dev(imsrg_basis *b, const double *A, double ax, const double *B
 int launch_norm(imsrg_basis *b, const double *op, double *d_out);
 int launch_mbpt2(imsrg_basis *b, const double *H, int herm, double *d_out);
 int launch_white(imsrg_basis *b, const double *H, int hH, double *ETA);
+int launch_generator(imsrg_basis *b, const double *Hden, int hH, const double *Hnum, int use_atan, double *ETA);
 int launch_white_tangent(imsrg_basis *b, const double *H, const double *dH, int hH, double *dETA);
 int launch_pack(imsrg_basis *b, const double *flat, double *packed);
 int launch_unpack(imsrg_basis *b, const double *packed, int herm, double *flat);

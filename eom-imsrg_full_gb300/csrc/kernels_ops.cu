@@ -149,13 +149,17 @@ __device__ long white_den(const DevTables &T, const double *__restrict__ X, int 
 }
 
 // ETA one-body (fph) and two-body (pphh) elements; everything else was zeroed.
-__global__ void __launch_bounds__(256) k_white(DevTables T, const double *__restrict__ H, int herm,
-                                               const double *__restrict__ mono, double *ETA) {
+// Denominators from Hden (and its monopoles), numerators from Hnum:
+//   White (generators.f90:4-106)          eta = N / D
+//   atan, atanxx (generators.f90:162-376)  eta = atan(2 N / D) * 0.5
+__global__ void __launch_bounds__(256) k_generator(DevTables T, const double *__restrict__ Hden, int herm,
+                                                   const double *__restrict__ mono,
+                                                   const double *__restrict__ Hnum, int use_atan, double *ETA) {
   const long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
   double den = 1.0;
-  const long e = white_den(T, H, herm, mono, t, &den);
+  const long e = white_den(T, Hden, herm, mono, t, &den);
   if (e == -1) ETA[T.off_fph + t] = 0.0;
-  else if (e >= 0) ETA[e] = H[e] / den;
+  else if (e >= 0) ETA[e] = use_atan ? atan(2 * Hnum[e] / den) * 0.5 : Hnum[e] / den;
 }
 
 // Tangent of the White generator along dH: eta = N / D with N and D linear in
@@ -235,18 +239,23 @@ int launch_mbpt2(imsrg_basis *b, const double *H, int herm, double *d_out) {
   return cuda_status(cudaGetLastError());
 }
 
-int launch_white(imsrg_basis *b, const double *H, int hH, double *ETA) {
+int launch_generator(imsrg_basis *b, const double *Hden, int hH, const double *Hnum, int use_atan, double *ETA) {
   double *mono = b->mono;
   ProfScope ps(b, IMSRG_KERNEL_OPS);
   IMSRG_CUDA_TRY(cudaMemsetAsync(ETA + 1, 0, (b->nfull - 1) * sizeof(double), b->stream));
   int nn = b->norb * b->norb;
-  k_monopole<<<(nn + 127) / 128, 128, 0, b->stream>>>(b->T, H, hH, mono);
+  k_monopole<<<(nn + 127) / 128, 128, 0, b->stream>>>(b->T, Hden, hH, mono);
   long n3 = 0;
   for (int q = 0; q < b->nblocks; q++) n3 += (long)b->gam_n1[q * 6 + 2] * b->gam_n2[q * 6 + 2];
   long n = (long)b->P * b->A + n3;
-  if (n > 0) k_white<<<(unsigned)((n + 255) / 256), 256, 0, b->stream>>>(b->T, H, hH, mono, ETA);
+  if (n > 0)
+    k_generator<<<(unsigned)((n + 255) / 256), 256, 0, b->stream>>>(b->T, Hden, hH, mono, Hnum, use_atan, ETA);
   b->launches += 2;
   return cuda_status(cudaGetLastError());
+}
+
+int launch_white(imsrg_basis *b, const double *H, int hH, double *ETA) {
+  return launch_generator(b, H, hH, H, 0, ETA);
 }
 
 int launch_white_tangent(imsrg_basis *b, const double *H, const double *dH, int hH, double *dETA) {

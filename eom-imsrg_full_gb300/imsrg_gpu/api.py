@@ -35,7 +35,7 @@ SYMBOLS = (
     "imsrg_gpu_basis_get_stream", "imsrg_gpu_basis_set_stream", "imsrg_gpu_profile_enable",
     "imsrg_gpu_profile_read", "imsrg_gpu_profile_reset", "imsrg_gpu_commutator_noalloc",
     "imsrg_gpu_magnus_decouple_graph", "imsrg_gpu_magnus_decouple_batch", "imsrg_gpu_magnus_decouple_tangent",
-    "imsrg_gpu_split_schedule",
+    "imsrg_gpu_split_schedule", "imsrg_gpu_build_gs_atan", "imsrg_gpu_build_gs_w2", "imsrg_gpu_magnus_decouple_gen",
 )
 
 KERNELS = ("cc_forward", "gemm_fp64", "assemble_2body", "assemble_1body", "ozaki_slice", "ozaki_mma",
@@ -106,6 +106,9 @@ def lib():
                                                 ip],
             "imsrg_gpu_magnus_decouple_tangent": [vp, vp, vp, vp, d, d, i, i, dp, dp, ip, ip],
             "imsrg_gpu_split_schedule": [vp, ip, ip, dp, i],
+            "imsrg_gpu_build_gs_atan": [vp, vp],
+            "imsrg_gpu_build_gs_w2": [vp, vp, i],
+            "imsrg_gpu_magnus_decouple_gen": [vp, vp, i, d, d, i, i, dp, ip, ip],
         }
         for name, args in sig.items():
             f = getattr(L, name)
@@ -416,3 +419,25 @@ def magnus_decouple_tangent(HS: Operator, dHS: Operator, G: Operator, dG: Operat
     n = steps.value + 1
     return dict(steps=steps.value, ncomm=nc.value, trace=trace[:5 * n].reshape(n, 5),
                 dtrace=dtrace[:5 * n].reshape(n, 5))
+
+
+GENERATORS = {"white": 0, "atan": 1, "w2": 2}
+
+
+def build_gs_atan(H: Operator, ETA: Operator):
+    _check(lib().imsrg_gpu_build_gs_atan(H.handle, ETA.handle), "build_gs_atan")
+
+
+def build_gs_w2(H: Operator, ETA: Operator, precision: str = "fp64"):
+    _check(lib().imsrg_gpu_build_gs_w2(H.handle, ETA.handle, PREC[precision]), "build_gs_w2")
+
+
+def magnus_decouple_gen(HS: Operator, G: Operator, generator: str = "white", s_max: float = 50.0, ds: float = 0.5,
+                        max_steps: int = 1000, precision: str = "fp64"):
+    trace = np.zeros(5 * (max_steps + 1))
+    steps, nc = C.c_int(0), C.c_int(0)
+    _check(lib().imsrg_gpu_magnus_decouple_gen(HS.handle, G.handle, GENERATORS[generator], float(s_max), float(ds),
+                                               int(max_steps), PREC[precision], _dp(trace), C.byref(steps),
+                                               C.byref(nc)), "magnus_decouple_gen")
+    n = steps.value + 1
+    return dict(steps=steps.value, ncomm=nc.value, trace=trace[:5 * n].reshape(n, 5))

@@ -63,6 +63,14 @@ enum {
                             recombined in FP64 */
 };
 
+/* Generators of the flow (the reference's magnus_decouple takes one as an
+ * external procedure, IMSRG_MAGNUS.f90:29, main_IMSRG.f90:216). */
+enum {
+  IMSRG_GEN_WHITE = 0,  /* build_gs_white (generators.f90:4-106) */
+  IMSRG_GEN_ATAN = 1,   /* build_gs_atan  (generators.f90:162-266) */
+  IMSRG_GEN_W2 = 2      /* build_gs_w2    (generators.f90:109-159) */
+};
+
 typedef struct imsrg_basis imsrg_basis_t;
 typedef struct imsrg_op imsrg_op_t;
 
@@ -137,6 +145,13 @@ int imsrg_gpu_commutator(const imsrg_op_t *L, const imsrg_op_t *R, imsrg_op_t *R
 /* build_gs_white (generators.f90:4-106): ETA (herm -1) from H.  ETA E0 is
  * left unchanged, as in the reference. */
 int imsrg_gpu_build_gs_white(const imsrg_op_t *H, imsrg_op_t *ETA);
+/* build_gs_atan (generators.f90:162-266): the White denominators with
+ * eta = atan(2 N / D) * 0.5. */
+int imsrg_gpu_build_gs_atan(const imsrg_op_t *H, imsrg_op_t *ETA);
+/* build_gs_w2 (generators.f90:109-159): ETA1 = atan(H), H2 = [ETA1, H],
+ * ETA2 = atanxx(H, H2) (denominators from H, numerators from H2,
+ * :271-376), ETA = 1.5 ETA1 + 0.5 ETA2; the commutator in `precision`. */
+int imsrg_gpu_build_gs_w2(const imsrg_op_t *H, imsrg_op_t *ETA, int precision);
 
 /* --- Magnus flow ------------------------------------------------------- */
 /* MAGNUS_EXPAND (IMSRG_MAGNUS.f90:622-693): DG in = eta, out = dOmega/ds.
@@ -154,6 +169,10 @@ int imsrg_gpu_euler_step(imsrg_op_t *G, const imsrg_op_t *DG, double *s, double 
  * *steps = Magnus steps taken, *ncomm = commutators evaluated. */
 int imsrg_gpu_magnus_decouple(imsrg_op_t *HS, imsrg_op_t *G, double s_max, double ds, int max_steps, int precision,
                               double *trace, int *steps, int *ncomm);
+/* The same flow with the generator IMSRG_GEN_* (imsrg_gpu_magnus_decouple
+ * is generator IMSRG_GEN_WHITE). */
+int imsrg_gpu_magnus_decouple_gen(imsrg_op_t *HS, imsrg_op_t *G, int generator, double s_max, double ds,
+                                  int max_steps, int precision, double *trace, int *steps, int *ncomm);
 /* The same flow with each Magnus step one CUDA graph launch: the Magnus and
  * BCH series run as device-side conditional loops, and the host reads back
  * only the step's scalars.  Results are bit-identical to

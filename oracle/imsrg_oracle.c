@@ -1062,9 +1062,10 @@ void orc_commutator_parts(const obasis *b, const double *L, int hL, const double
 }
 
 /* ------------------------------------------------------------------ */
-/* White generator, generators.f90:4-106                               */
+/* Generators: White (generators.f90:4-106), atan (:162-266), atanxx  */
+/* (:271-376; denominators from Hold, numerators from H), w2 (:109-159) */
 /* ------------------------------------------------------------------ */
-void orc_white(const obasis *b, const double *H, int hH, double *ETA) {
+static void gen_core(const obasis *b, const double *Hd, int hd, const double *Hn, double *ETA, int use_atan) {
   /* ETA%fpp = 0, ETA%fhh = 0; fph entries with mismatched (l,j,tz) keep
    * their previous value in the reference; callers pass a zeroed ETA. */
   for (long i = 0; i < (long)b->P * b->P; i++) ETA[b->off_fpp + i] = 0.0;
@@ -1077,10 +1078,10 @@ void orc_white(const obasis *b, const double *H, int hH, double *ETA) {
       int ji = b->jj[ik], li = b->ll[ik], ti = b->itzp[ik];
       if (ji != ja || li != la || ti != ta) continue;
       double Eden = 0.0;
-      for (int JT = 0; JT <= 2 * ji; JT += 2) Eden = Eden - (JT + 1) * v_elem(b, ak, ik, ak, ik, JT, H, hH);
+      for (int JT = 0; JT <= 2 * ji; JT += 2) Eden = Eden - (JT + 1) * v_elem(b, ak, ik, ak, ik, JT, Hd, hd);
       Eden = Eden / (ji + 1.0) / (ji + 1.0);
-      Eden = Eden + FPP(b, H, a, a) - FHH(b, H, i, i);
-      FPH(b, ETA, a, i) = FPH(b, H, a, i) / Eden;
+      Eden = Eden + FPP(b, Hd, a, a) - FHH(b, Hd, i, i);
+      FPH(b, ETA, a, i) = use_atan ? atan(2 * FPH(b, Hn, a, i) / Eden) * 0.5 : FPH(b, Hn, a, i) / Eden;
     }
   }
   for (int q = 1; q <= b->nblocks; q++) {
@@ -1093,18 +1094,46 @@ void orc_white(const obasis *b, const double *H, int hH, double *ETA) {
         int i = QN(b, q, 3, JX, 1), j = QN(b, q, 3, JX, 2);
         int ji = b->jj[i], jj = b->jj[j];
         double Eden = 0.0;
-        Eden = Eden + twobody_monopole(b, a, bb, ja, jb, H, hH);
-        Eden = Eden + twobody_monopole(b, i, j, ji, jj, H, hH);
-        Eden = Eden - twobody_monopole(b, a, i, ja, ji, H, hH);
-        Eden = Eden - twobody_monopole(b, a, j, ja, jj, H, hH);
-        Eden = Eden - twobody_monopole(b, i, bb, ji, jb, H, hH);
-        Eden = Eden - twobody_monopole(b, j, bb, jj, jb, H, hH);
-        Eden = Eden + f_elem(b, a, a, H, hH) + f_elem(b, bb, bb, H, hH) - f_elem(b, i, i, H, hH) -
-               f_elem(b, j, j, H, hH);
-        GX(b, ETA, q, 3, IX, JX) = GX(b, H, q, 3, IX, JX) / Eden;
+        Eden = Eden + twobody_monopole(b, a, bb, ja, jb, Hd, hd);
+        Eden = Eden + twobody_monopole(b, i, j, ji, jj, Hd, hd);
+        Eden = Eden - twobody_monopole(b, a, i, ja, ji, Hd, hd);
+        Eden = Eden - twobody_monopole(b, a, j, ja, jj, Hd, hd);
+        Eden = Eden - twobody_monopole(b, i, bb, ji, jb, Hd, hd);
+        Eden = Eden - twobody_monopole(b, j, bb, jj, jb, Hd, hd);
+        Eden = Eden + f_elem(b, a, a, Hd, hd) + f_elem(b, bb, bb, Hd, hd) - f_elem(b, i, i, Hd, hd) -
+               f_elem(b, j, j, Hd, hd);
+        GX(b, ETA, q, 3, IX, JX) =
+            use_atan ? 0.5 * atan(2 * GX(b, Hn, q, 3, IX, JX) / Eden) : GX(b, Hn, q, 3, IX, JX) / Eden;
       }
     }
   }
+}
+
+void orc_white(const obasis *b, const double *H, int hH, double *ETA) { gen_core(b, H, hH, H, ETA, 0); }
+
+void orc_atan(const obasis *b, const double *H, int hH, double *ETA) { gen_core(b, H, hH, H, ETA, 1); }
+
+void orc_atanxx(const obasis *b, const double *Hold, int hold, const double *H, double *ETA) {
+  gen_core(b, Hold, hold, H, ETA, 1);
+}
+
+/* build_gs_w2: ETA1 = atan(H); H2 = [ETA1, H]; ETA2 = atanxx(H, H2);
+ * ETA = 1.5 ETA1 + 0.5 ETA2 (fresh, zeroed work operators). */
+void orc_w2(const obasis *b, const double *H, int hH, double *ETA) {
+  double *E1 = calloc(b->nfull, sizeof(double)), *E2 = calloc(b->nfull, sizeof(double)),
+         *H2 = calloc(b->nfull, sizeof(double));
+  orc_atan(b, H, hH, E1);
+  orc_commutator(b, E1, -1, H, hH, H2);
+  orc_atanxx(b, H, hH, H2, E2);
+  orc_add(b, E1, 1.5, E2, 0.5, ETA);
+  free(E1); free(E2); free(H2);
+}
+
+static void generator(const obasis *b, int gen, const double *H, double *ETA) {
+  memset(ETA, 0, b->nfull * sizeof(double));
+  if (gen == 1) orc_atan(b, H, 1, ETA);
+  else if (gen == 2) orc_w2(b, H, 1, ETA);
+  else orc_white(b, H, 1, ETA);
 }
 
 /* ------------------------------------------------------------------ */
@@ -1263,11 +1292,11 @@ int orc_bch_expand(const obasis *b, double *HS, const double *G, const double *H
  * stop at s >= s_max.  trace[5*k..] = (step, s, E0, E0+mbpt2, |mbpt2|) for
  * k = 0..nsteps; returns the number of steps (or -1 on BCH clipping).
  * HS: in = normal-ordered H, out = H(s).  G: out = Omega(s). */
-int orc_magnus_decouple(const obasis *b, double *HS, double *G, double s_max, double ds, int max_steps,
-                        double *trace, int *ncomm_total) {
+int orc_magnus_decouple_gen(const obasis *b, int gen, double *HS, double *G, double s_max, double ds,
+                            int max_steps, double *trace, int *ncomm_total) {
   double *H = malloc(b->nfull * sizeof(double)), *DG = calloc(b->nfull, sizeof(double));
   memset(G, 0, b->nfull * sizeof(double));
-  orc_white(b, HS, 1, DG);
+  generator(b, gen, HS, DG);
   memcpy(H, HS, b->nfull * sizeof(double));
   double s = 0.0;
   double E_mbpt2 = orc_mbpt2(b, HS, 1);
@@ -1282,8 +1311,7 @@ int orc_magnus_decouple(const obasis *b, double *HS, double *G, double s_max, do
     int nb = orc_bch_expand(b, HS, G, H);
     if (nb < 0) { steps = -1; break; }
     nct += nb;
-    memset(DG, 0, b->nfull * sizeof(double));
-    orc_white(b, HS, 1, DG);
+    generator(b, gen, HS, DG);
     E_mbpt2 = orc_mbpt2(b, HS, 1);
     crit = fabs(E_mbpt2);
     double *t = trace + 5 * steps;
@@ -1292,6 +1320,11 @@ int orc_magnus_decouple(const obasis *b, double *HS, double *G, double s_max, do
   if (ncomm_total) *ncomm_total = nct;
   free(H); free(DG);
   return steps;
+}
+
+int orc_magnus_decouple(const obasis *b, double *HS, double *G, double s_max, double ds, int max_steps,
+                        double *trace, int *ncomm_total) {
+  return orc_magnus_decouple_gen(b, 0, HS, G, s_max, ds, max_steps, trace, ncomm_total);
 }
 
 /* ------------------------------------------------------------------ */

@@ -47,6 +47,10 @@ def lib():
             "orc_comm220": (d, [vp, dp, i, dp, i]),
             "orc_cross_coupled": (None, [vp, dp, i, dp]),
             "orc_white": (None, [vp, dp, i, dp]),
+            "orc_atan": (None, [vp, dp, i, dp]),
+            "orc_atanxx": (None, [vp, dp, i, dp, dp]),
+            "orc_w2": (None, [vp, dp, i, dp]),
+            "orc_magnus_decouple_gen": (i, [vp, i, dp, dp, d, d, i, dp, ip]),
             "orc_normal_order": (None, [vp, dp, i]),
             "orc_mbpt2": (d, [vp, dp, i]),
             "orc_norm": (d, [vp, dp]),
@@ -155,6 +159,24 @@ class Oracle:
         lib().orc_white(self.h, _dp(H), herm, _dp(eta))
         return eta
 
+    def atan_gen(self, H, herm=1):
+        """build_gs_atan (generators.f90:162-266)."""
+        eta = self.zeros()
+        lib().orc_atan(self.h, _dp(H), herm, _dp(eta))
+        return eta
+
+    def atanxx_gen(self, Hold, H, herm=1):
+        """build_gs_atanxx (generators.f90:271-376)."""
+        eta = self.zeros()
+        lib().orc_atanxx(self.h, _dp(Hold), herm, _dp(H), _dp(eta))
+        return eta
+
+    def w2_gen(self, H, herm=1):
+        """build_gs_w2 (generators.f90:109-159)."""
+        eta = self.zeros()
+        lib().orc_w2(self.h, _dp(H), herm, _dp(eta))
+        return eta
+
     def normal_order(self, H, herm=1):
         out = H.copy()
         lib().orc_normal_order(self.h, _dp(out), herm)
@@ -197,6 +219,17 @@ class Oracle:
         trace = np.zeros(5 * (max_steps + 1))
         nc = C.c_int(0)
         steps = lib().orc_magnus_decouple(self.h, _dp(hs), _dp(G), s_max, ds, max_steps, _dp(trace), C.byref(nc))
+        nrow = max(steps, 0) + 1
+        return dict(H=hs, Omega=G, steps=steps, trace=trace[:5 * nrow].reshape(nrow, 5), ncomm=nc.value)
+
+    def magnus_decouple_gen(self, H, generator="white", s_max=50.0, ds=0.5, max_steps=1000):
+        gen = {"white": 0, "atan": 1, "w2": 2}[generator]
+        hs = H.copy()
+        G = self.zeros()
+        trace = np.zeros(5 * (max_steps + 1))
+        nc = C.c_int(0)
+        steps = lib().orc_magnus_decouple_gen(self.h, gen, _dp(hs), _dp(G), s_max, ds, max_steps, _dp(trace),
+                                              C.byref(nc))
         nrow = max(steps, 0) + 1
         return dict(H=hs, Omega=G, steps=steps, trace=trace[:5 * nrow].reshape(nrow, 5), ncomm=nc.value)
 
