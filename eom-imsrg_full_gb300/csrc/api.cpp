@@ -8,7 +8,9 @@
 // back.  The reference allocates fresh work operators in every BCH/MAGNUS call
 // (:164-174, :633-643); here they are allocated once per basis and reused, and
 // the INT1/AD/INT2 copies become two alternating buffers.
+#include <algorithm>
 #include <cmath>
+#include <cstdio>
 #include <cstring>
 #include <new>
 #include <vector>
@@ -195,6 +197,7 @@ const char *imsrg_gpu_strerror(int s) {
     case IMSRG_ERR_MISMATCH: return "operators belong to different bases";
     case IMSRG_ERR_NO_DEVICE: return "no usable CUDA device";
     case IMSRG_ERR_TOO_LARGE: return "basis too large for a fixed-size table or workspace";
+    case IMSRG_ERR_IO: return "file could not be written or read (or has the wrong length)";
     default: return "unknown status";
   }
 }
@@ -555,6 +558,81 @@ int imsrg_gpu_bch_expand(imsrg_op_t *HS, const imsrg_op_t *G, const imsrg_op_t *
   }
   if (ncomm) *ncomm = nc;
   return (iw > 40) ? IMSRG_ERR_NOT_CONVERGED : IMSRG_OK;
+}
+
+int imsrg_gpu_normal_order(imsrg_op_t *H) {
+  IMSRG_TRY(check_op(H));
+  imsrg_basis *b = H->b;
+  imsrg_op *T;
+  IMSRG_TRY(tmp_op(b, 12, &T));
+  IMSRG_TRY(copy_dev(b, H->d, T->d, b->nfull));
+  return imsrg::launch_normal_order(b, T->d, H->herm, H->d);
+}
+
+int imsrg_gpu_transform_bch(imsrg_op_t *Op, const imsrg_op_t *G, int precision, int *ncomm) {
+  IMSRG_TRY(check_op(Op));
+  IMSRG_TRY(check_op(G));
+  if (Op->b != G->b) return IMSRG_ERR_MISMATCH;
+  imsrg_op *E;
+  IMSRG_TRY(tmp_op(Op->b, 13, &E));
+  IMSRG_TRY(imsrg_gpu_bch_expand(E, G, Op, precision, ncomm));
+  return imsrg_gpu_op_copy(E, Op);
+}
+
+int imsrg_gpu_dhds(const imsrg_op_t *HS, imsrg_op_t *DH, int generator, int precision) {
+  IMSRG_TRY(check_op(HS));
+  IMSRG_TRY(check_op(DH));
+  if (HS->b != DH->b) return IMSRG_ERR_MISMATCH;
+  if (HS == DH) return IMSRG_ERR_INVALID;
+  if (precision != IMSRG_PREC_FP64 && precision != IMSRG_PREC_OZAKI) return IMSRG_ERR_INVALID;
+  imsrg_basis *b = HS->b;
+  imsrg_op *ETA;
+  IMSRG_TRY(tmp_op(b, 14, &ETA));
+  IMSRG_CUDA_TRY(cudaMemsetAsync(ETA->d, 0, sizeof(double), b->stream));
+  ETA->herm = -1;
+  IMSRG_TRY(generator_dev(b, HS->d, HS->herm, ETA->d, generator, precision));
+  DH->herm = HS->herm;
+  return imsrg::commutator_dev(b, ETA->d, -1, HS->d, HS->herm, DH->d, HS->herm, precision, 1);
+}
+
+int imsrg_gpu_op_save(const imsrg_op_t *op, const char *path) {
+  IMSRG_TRY(check_op(op));
+  if (!path) return IMSRG_ERR_INVALID;
+  std::vector<double> v(op->b->neq);
+  IMSRG_TRY(imsrg_gpu_op_download_packed(op, v.data()));
+  FILE *f = std::fopen(path, "wb");
+  if (!f) return IMSRG_ERR_IO;
+  const size_t n = std::fwrite(v.data(), sizeof(double), v.size(), f);
+  const int c = std::fclose(f);
+  return (n == v.size() && c == 0) ? IMSRG_OK : IMSRG_ERR_IO;
+}
+
+int imsrg_gpu_op_load(imsrg_op_t *op, const char *path) {
+  IMSRG_TRY(check_op(op));
+  if (!path) return IMSRG_ERR_INVALID;
+  FILE *f = std::fopen(path, "rb");
+  if (!f) return IMSRG_ERR_IO;
+  std::vector<double> v(op->b->neq);
+  const size_t n = std::fread(v.data(), sizeof(double), v.size(), f);
+  const bool at_end = std::fgetc(f) == EOF;
+  std::fclose(f);
+  if (n != v.size() || !at_end) return IMSRG_ERR_IO;
+  return imsrg_gpu_op_upload_packed(op, v.data());
+}
+
+int imsrg_gpu_checkpoint_name(const char *dir, const char *prefix, double s, char *out, int outlen) {
+  if (!dir || !prefix || !out || outlen <= 0) return IMSRG_ERR_INVALID;
+  // the run prefix up to its 'hw' field and two characters after it
+  const char *hw = std::strstr(prefix, "hw");
+  const size_t keep = hw ? std::min(std::strlen(prefix), (size_t)(hw - prefix) + 4) : std::strlen(prefix);
+  // f6.3 of s, left-adjusted; a trailing 0 below s = 10 (the reference's
+  // character(8) slot then holds '_s' and six characters)
+  char num[32];
+  std::snprintf(num, sizeof(num), "%6.3f", s);
+  const char *p = num;
+  while (*p == ' ') p++;
+  const int len = std::snprintf(out, outlen, "%s%.*s_s%s%s.bin", dir, (int)keep, prefix, p, s < 10.0 ? "0" : "");
+  return (len > 0 && len < outlen) ? IMSRG_OK : IMSRG_ERR_INVALID;
 }
 
 int imsrg_gpu_build_gs_atan(const imsrg_op_t *H, imsrg_op_t *ETA) {

@@ -282,6 +282,7 @@ int launch_white_tangent(imsrg_basis *b, const double *H, const double *dH, int 
 int launch_pack(imsrg_basis *b, const double *flat, double *packed);
 int launch_unpack(imsrg_basis *b, const double *packed, int herm, double *flat);
 int launch_check_finite(imsrg_basis *b, const double *op, int *d_flag);
+int launch_normal_order(imsrg_basis *b, const double *Tin, int herm, double *H);
 
 // Intermediates of one commutator: W1, W2 (flat operators), LCC, RCC (all
 // cross-coupled blocks) and WCC.

@@ -180,6 +180,74 @@ __global__ void __launch_bounds__(256) k_white_tangent(DevTables T, const double
   }
 }
 
+// normal_order (basic_IMSRG.f90:2375-2506) from T (the operator before
+// normal ordering) into H.  Threads [0, A*A + P*A + P*P) take one one-body
+// element each (upper triangles of fhh and fpp, mirrored; fph whole):
+//   f_ab + sum_{i hole} sum_J (2J+1)/(2j_a+1) <a i|V|b i>_J  for (l,j,tz)-equal a, b.
+// The last CTA forms E0 = (2 sum_i (2j_i+1) f_ii + sum_{ij holes} sum_J (2J+1) <ij|V|ij>_J) / 2.
+__global__ void __launch_bounds__(256) k_normal_order(DevTables T, const double *__restrict__ Tin, int herm,
+                                                      double *H, int nel) {
+  __shared__ double sh[8];
+  const int A = T.A, P = T.P;
+  if ((int)blockIdx.x == (int)gridDim.x - 1) {
+    // E0: hole diagonal one-body, then hole-hole monopoles (fixed order)
+    double sm = 0.0;
+    for (int k = threadIdx.x; k < A * A; k += blockDim.x) {
+      const int i = T.hole_orb[k % A], j = T.hole_orb[k / A];
+      double v = 0.0;
+      if (k % A == k / A) v += 2.0 * f_elem(T, Tin, herm, i, i) * (T.orb[i].x + 1);
+      const int ji = T.orb[i].x, jj = T.orb[j].x;
+      for (int JT = abs(ji - jj); JT <= ji + jj; JT += 2) v += v_elem(T, Tin, herm, i, j, i, j, JT) * (JT + 1);
+      sm += v;
+    }
+    sm = block_sum_ops(sm, sh);
+    if (threadIdx.x == 0) H[0] = sm * 0.5;
+    return;
+  }
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= nel) return;
+  int ax, bx, pass, a, b;
+  if (t < A * A) {
+    pass = 0;
+    a = t % A;
+    b = t / A;
+    ax = T.hole_orb[a];
+    bx = T.hole_orb[b];
+  } else if (t < A * A + P * A) {
+    pass = 1;
+    a = (t - A * A) % P;
+    b = (t - A * A) / P;
+    ax = T.part_orb[a];
+    bx = T.hole_orb[b];
+  } else {
+    pass = 2;
+    a = (t - A * A - P * A) % P;
+    b = (t - A * A - P * A) / P;
+    ax = T.part_orb[a];
+    bx = T.part_orb[b];
+  }
+  if (pass != 1 && b < a) return;  // mirrored from the upper triangle
+  const int4 oa = T.orb[ax], ob = T.orb[bx];
+  if (oa.x != ob.x || oa.y != ob.y || oa.z != ob.z) return;  // the reference leaves these untouched
+  double s = 0.0;
+  for (int i = 0; i < A; i++) {
+    const int ix = T.hole_orb[i];
+    const int ji = T.orb[ix].x;
+    for (int JT = abs(ji - oa.x); JT <= ji + oa.x; JT += 2)
+      s += (JT + 1.0) / (oa.x + 1) * v_elem(T, Tin, herm, ax, ix, bx, ix, JT);
+  }
+  const double v = f_elem(T, Tin, herm, ax, bx) + s;
+  if (pass == 0) {
+    H[T.off_fhh + a + (long)b * A] = v;
+    H[T.off_fhh + b + (long)a * A] = v;
+  } else if (pass == 1) {
+    H[T.off_fph + a + (long)b * P] = v;
+  } else {
+    H[T.off_fpp + a + (long)b * P] = v;
+    H[T.off_fpp + b + (long)a * P] = v;
+  }
+}
+
 __global__ void k_pack(const double *__restrict__ flat, const long *__restrict__ src, double *packed, long n) {
   long k = (long)blockIdx.x * blockDim.x + threadIdx.x;
   if (k < n) packed[k] = flat[src[k]];
@@ -283,6 +351,14 @@ int launch_pack(imsrg_basis *b, const double *flat, double *packed) {
 int launch_unpack(imsrg_basis *b, const double *packed, int herm, double *flat) {
   k_unpack<<<(unsigned)((b->neq + 255) / 256), 256, 0, b->stream>>>(packed, b->d_pack_src, b->d_pack_mirror, herm,
                                                                       flat, b->neq);
+  b->launches++;
+  return cuda_status(cudaGetLastError());
+}
+
+int launch_normal_order(imsrg_basis *b, const double *Tin, int herm, double *H) {
+  const int nel = b->A * b->A + b->P * b->A + b->P * b->P;
+  ProfScope ps(b, IMSRG_KERNEL_OPS);
+  k_normal_order<<<(nel + 255) / 256 + 1, 256, 0, b->stream>>>(b->T, Tin, herm, H, nel);
   b->launches++;
   return cuda_status(cudaGetLastError());
 }

@@ -36,6 +36,8 @@ SYMBOLS = (
     "imsrg_gpu_profile_read", "imsrg_gpu_profile_reset", "imsrg_gpu_commutator_noalloc",
     "imsrg_gpu_magnus_decouple_graph", "imsrg_gpu_magnus_decouple_batch", "imsrg_gpu_magnus_decouple_tangent",
     "imsrg_gpu_split_schedule", "imsrg_gpu_build_gs_atan", "imsrg_gpu_build_gs_w2", "imsrg_gpu_magnus_decouple_gen",
+    "imsrg_gpu_op_save", "imsrg_gpu_op_load", "imsrg_gpu_checkpoint_name", "imsrg_gpu_normal_order",
+    "imsrg_gpu_dhds", "imsrg_gpu_transform_bch",
 )
 
 KERNELS = ("cc_forward", "gemm_fp64", "assemble_2body", "assemble_1body", "ozaki_slice", "ozaki_mma",
@@ -109,6 +111,12 @@ def lib():
             "imsrg_gpu_build_gs_atan": [vp, vp],
             "imsrg_gpu_build_gs_w2": [vp, vp, i],
             "imsrg_gpu_magnus_decouple_gen": [vp, vp, i, d, d, i, i, dp, ip, ip],
+            "imsrg_gpu_op_save": [vp, C.c_char_p],
+            "imsrg_gpu_op_load": [vp, C.c_char_p],
+            "imsrg_gpu_checkpoint_name": [C.c_char_p, C.c_char_p, d, C.c_char_p, i],
+            "imsrg_gpu_normal_order": [vp],
+            "imsrg_gpu_dhds": [vp, vp, i, i],
+            "imsrg_gpu_transform_bch": [vp, vp, i, ip],
         }
         for name, args in sig.items():
             f = getattr(L, name)
@@ -249,6 +257,13 @@ class Operator:
         assert out.dtype == np.float64 and out.flags.c_contiguous and out.size == self.basis.nfull
         _check(lib().imsrg_gpu_op_download_flat(self._h, _dp(out)), "op_download_flat")
         return out
+
+    def save(self, path: str):
+        """Checkpoint file: the packed (vectorize) vector as a raw stream."""
+        _check(lib().imsrg_gpu_op_save(self._h, str(path).encode()), "op_save")
+
+    def load(self, path: str):
+        _check(lib().imsrg_gpu_op_load(self._h, str(path).encode()), "op_load")
 
     def upload_packed(self, vec: np.ndarray):
         vec = np.ascontiguousarray(vec, np.float64)
@@ -441,3 +456,24 @@ def magnus_decouple_gen(HS: Operator, G: Operator, generator: str = "white", s_m
                                                C.byref(nc)), "magnus_decouple_gen")
     n = steps.value + 1
     return dict(steps=steps.value, ncomm=nc.value, trace=trace[:5 * n].reshape(n, 5))
+
+
+def checkpoint_name(directory: str, prefix: str, s: float) -> str:
+    """The reference's Omega checkpoint file name for flow parameter s."""
+    buf = C.create_string_buffer(512)
+    _check(lib().imsrg_gpu_checkpoint_name(directory.encode(), prefix.encode(), float(s), buf, 512), "checkpoint_name")
+    return buf.value.decode()
+
+
+def normal_order(H: Operator):
+    _check(lib().imsrg_gpu_normal_order(H.handle), "normal_order")
+
+
+def dhds(HS: Operator, DH: Operator, generator: str = "white", precision: str = "fp64"):
+    _check(lib().imsrg_gpu_dhds(HS.handle, DH.handle, GENERATORS[generator], PREC[precision]), "dhds")
+
+
+def transform_bch(Op: Operator, G: Operator, precision: str = "fp64") -> int:
+    n = C.c_int(0)
+    _check(lib().imsrg_gpu_transform_bch(Op.handle, G.handle, PREC[precision], C.byref(n)), "transform_bch")
+    return n.value

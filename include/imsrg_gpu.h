@@ -51,7 +51,8 @@ enum {
   IMSRG_ERR_TIMEOUT = 6,        /* a bounded device wait gave up */
   IMSRG_ERR_MISMATCH = 7,       /* operators of different bases */
   IMSRG_ERR_NO_DEVICE = 8,      /* no usable CUDA device */
-  IMSRG_ERR_TOO_LARGE = 9       /* basis exceeds a fixed workspace limit */
+  IMSRG_ERR_TOO_LARGE = 9,      /* basis exceeds a fixed workspace limit */
+  IMSRG_ERR_IO = 10             /* checkpoint file error */
 };
 
 /* Arithmetic of the dense two-body contractions (222_pp_hh ladders and the
@@ -116,6 +117,20 @@ int imsrg_gpu_op_download_packed(const imsrg_op_t *op, double *packed);
 /* Device address of the flat layout (nfull doubles), for callers that keep
  * their own device buffers in the same layout. */
 int imsrg_gpu_op_device_ptr(imsrg_op_t *op, double **dptr);
+/* Operator files of write_omega_checkpoint / read_omega_checkpoint and
+ * write_twobody_operator (basic_IMSRG.f90:3069-3312): the vectorize vector
+ * (neq doubles, native byte order) as an unformatted stream, no header.
+ * load requires exactly neq doubles and keeps the operator's herm. */
+int imsrg_gpu_op_save(const imsrg_op_t *op, const char *path);
+int imsrg_gpu_op_load(imsrg_op_t *op, const char *path);
+/* The reference's checkpoint file name: dir, the run prefix up to its 'hw'
+ * field plus two characters, '_s', s in f6.3 left-adjusted (a '0' appended
+ * below s = 10), '.bin' (basic_IMSRG.f90:3142-3160).  Host only. */
+int imsrg_gpu_checkpoint_name(const char *dir, const char *prefix, double s, char *out, int outlen);
+/* normal_order (basic_IMSRG.f90:2375-2506) in place: E0 and the one-body part
+ * of H become those of H normal-ordered with respect to the reference state;
+ * one-body elements of different (l,j,tz) are left as they are. */
+int imsrg_gpu_normal_order(imsrg_op_t *H);
 
 /* copy_sq_op (basic_IMSRG.f90:2942-2969): dst = src, herm included */
 int imsrg_gpu_op_copy(const imsrg_op_t *src, imsrg_op_t *dst);
@@ -153,6 +168,12 @@ int imsrg_gpu_build_gs_atan(const imsrg_op_t *H, imsrg_op_t *ETA);
  * :271-376), ETA = 1.5 ETA1 + 0.5 ETA2; the commutator in `precision`. */
 int imsrg_gpu_build_gs_w2(const imsrg_op_t *H, imsrg_op_t *ETA, int precision);
 
+/* dHds (IMSRG_ODE.f90:416-463): DH = [eta(HS), HS] with the generator
+ * IMSRG_GEN_*, the derivative the reference hands its Shampine-Gordon solver
+ * (the solver stays with the caller; DH in packed form via
+ * imsrg_gpu_op_download_packed is its yp vector). */
+int imsrg_gpu_dhds(const imsrg_op_t *HS, imsrg_op_t *DH, int generator, int precision);
+
 /* --- Magnus flow ------------------------------------------------------- */
 /* MAGNUS_EXPAND (IMSRG_MAGNUS.f90:622-693): DG in = eta, out = dOmega/ds.
  * *ncomm = commutators evaluated. */
@@ -160,6 +181,9 @@ int imsrg_gpu_magnus_expand(imsrg_op_t *DG, const imsrg_op_t *G, int precision, 
 /* BCH_EXPAND (IMSRG_MAGNUS.f90:149-234): HS = exp(G) H exp(-G).
  * Returns IMSRG_ERR_NOT_CONVERGED where the reference STOPs ('clipping BCH'). */
 int imsrg_gpu_bch_expand(imsrg_op_t *HS, const imsrg_op_t *G, const imsrg_op_t *H, int precision, int *ncomm);
+/* transform_sq_op_BCH (IMSRG_MAGNUS.f90:131-146), scalar operators:
+ * Op = exp(G) Op exp(-G) by BCH_EXPAND, in place. */
+int imsrg_gpu_transform_bch(imsrg_op_t *Op, const imsrg_op_t *G, int precision, int *ncomm);
 /* euler_step (IMSRG_MAGNUS.f90:756-766): G += ds*DG, *s += ds */
 int imsrg_gpu_euler_step(imsrg_op_t *G, const imsrg_op_t *DG, double *s, double ds);
 /* magnus_decouple (IMSRG_MAGNUS.f90:15-128) with build_gs_white and an added

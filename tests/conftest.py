@@ -40,6 +40,15 @@ def gpu_lib():
     return api
 
 
+@pytest.fixture(scope="session")
+def gpu_lib_cpu():
+    """The library's Python mirror for host-only entry points (no GPU used)."""
+    import build as pkg_build
+    pkg_build.build()
+    from imsrg_gpu import api
+    return api
+
+
 def make_case(emax, seed=1):
     from imsrg_gpu.layout import Layout, ho_basis
     bas = ho_basis(emax)
