@@ -118,7 +118,7 @@ int commutator_launches(imsrg_basis *b, const double *L, int hL, const double *R
   // one-body assembly beside the two-body one; E0 after both
   IMSRG_TRY(fork(1));
   IMSRG_TRY(launch_assemble_1body(b, L, hL, R, hR, RES, hRES, b->side));
-  IMSRG_TRY(launch_assemble_2body(b, L, hL, R, hR, RES, hRES, with_e0));
+  IMSRG_TRY(launch_assemble_2body(b, L, hL, R, hR, RES, hRES, with_e0, precision));
   IMSRG_TRY(join(1));
   if (with_e0) IMSRG_TRY(launch_energy(b, L, hL, R, hR, RES, hL * hR == -1));
   return IMSRG_OK;

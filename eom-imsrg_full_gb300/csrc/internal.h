@@ -268,7 +268,7 @@ inline int asm2_ctas(const imsrg_basis *b) { return (b->T.n_asm2 + ASM2_THREADS 
 int launch_cc_forward(imsrg_basis *b, const double *L, int hL, const double *R, int hR);
 int launch_gemm_fp64(imsrg_basis *b, const double *L, int hL, const double *R, int hR);
 int launch_assemble_2body(imsrg_basis *b, const double *L, int hL, const double *R, int hR, double *RES, int hRES,
-                          int with_e0);
+                          int with_e0, int precision);
 int launch_assemble_1body(imsrg_basis *b, const double *L, int hL, const double *R, int hR, double *RES, int hRES,
                           cudaStream_t st);
 int launch_energy(imsrg_basis *b, const double *L, int hL, const double *R, int hR, double *RES, int e220);
@@ -301,6 +301,10 @@ int ozaki_slice(imsrg_basis *b, const double *L, const double *R, int part, cuda
 int ozaki_mma(imsrg_basis *b, int hL, int hR);
 int ozaki_check_error(imsrg_basis *b);  // IMSRG_ERR_TIMEOUT if a bounded device wait gave up
 bool ozaki_tuned(imsrg_basis *b);       // the CTA schedule has been autotuned
+// After a split-precision product WCC holds exact int64 level sums v with
+// WCC = v 2^k, k = (exps[g.x] - 1022) + (exps[g.y] - 1022) - 49 for the
+// groups g = ccgroups[q1] of cross-coupled block q1.
+int ozaki_wcc_scale(imsrg_basis *b, const int **exps, const int2 **ccgroups);
 int ozaki_schedule_info(imsrg_basis *b, int *choice, int *ncand, double *us, int max);
 void ozaki_free(imsrg_basis *b);
 

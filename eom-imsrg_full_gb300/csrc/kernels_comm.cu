@@ -148,8 +148,17 @@ __device__ __forceinline__ double wcc_at(const double *W, int rlen, unsigned r, 
   return W[r + (long)c * rlen];
 }
 
-// Recoupling inputs Z of commutator_222_ph, one thread per PhTerm.
+__device__ __forceinline__ long long wcc_at_int(const long long *W, int rlen, unsigned r, unsigned c) {
+  if (r == 0xFFFFu || c == 0xFFFFu) return 0;
+  return W[r + (long)c * rlen];
+}
+
+// Recoupling inputs Z of commutator_222_ph, one thread per PhTerm.  With
+// exps == nullptr WCC holds FP64 (the FP64 path); otherwise it holds the
+// split engine's exact int64 level sums, WCC = v 2^k per cross-coupled block,
+// and the four entries are combined exactly in int64 before one conversion.
 __global__ void __launch_bounds__(256) k_ph_inputs(DevTables T, const double *__restrict__ WCC, int hL, int hR,
+                                                   const int *__restrict__ exps, const int2 *__restrict__ ccg,
                                                    double *__restrict__ Z) {
   const long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= T.n_ph) return;
@@ -157,8 +166,18 @@ __global__ void __launch_bounds__(256) k_ph_inputs(DevTables T, const double *__
   const unsigned long long u = p.rows;
   const unsigned x1 = (unsigned)(u & 0xFFFF), y1 = (unsigned)((u >> 16) & 0xFFFF);
   const unsigned x2 = (unsigned)((u >> 32) & 0xFFFF), y2 = (unsigned)(u >> 48);
-  const double *W = WCC + T.wcc_off[p.qx];
   const int rl = T.cc_rlen[p.qx];
+  if (exps) {
+    const long long *W = reinterpret_cast<const long long *>(WCC) + T.wcc_off[p.qx];
+    const long long w2 = wcc_at_int(W, rl, x2, y2), w3 = wcc_at_int(W, rl, y2, x2);
+    const long long a = wcc_at_int(W, rl, x1, y1) + (p.nph ? -w2 : w2);
+    const long long c = (p.nph ? -w3 : w3) + wcc_at_int(W, rl, y1, x1);
+    const long long z = (hL < 0 ? -a : a) - (hR < 0 ? -c : c);
+    const int2 g = ccg[p.qx];
+    Z[t] = ldexp((double)z, (exps[g.x] - 1022) + (exps[g.y] - 1022) - 49);
+    return;
+  }
+  const double *W = WCC + T.wcc_off[p.qx];
   const double a = wcc_at(W, rl, x1, y1) + dflip(wcc_at(W, rl, x2, y2), p.nph);
   const double c = dflip(wcc_at(W, rl, y2, x2), p.nph) + wcc_at(W, rl, y1, x1);
   Z[t] = dflip(a, hL < 0) - dflip(c, hR < 0);
@@ -448,10 +467,14 @@ int launch_gemm_fp64(imsrg_basis *b, const double *L, int hL, const double *R, i
 }
 
 int launch_assemble_2body(imsrg_basis *b, const double *L, int hL, const double *R, int hR, double *RES, int hRES,
-                          int with_e0) {
+                          int with_e0, int precision) {
   ProfScope ps(b, IMSRG_KERNEL_ASSEMBLE_2BODY);
+  const int *exps = nullptr;
+  const int2 *ccg = nullptr;
+  if (precision == IMSRG_PREC_OZAKI) IMSRG_TRY(ozaki_wcc_scale(b, &exps, &ccg));
   if (b->T.n_ph > 0) {
-    k_ph_inputs<<<(unsigned)((b->T.n_ph + 255) / 256), 256, 0, b->stream>>>(b->T, b->wcc, hL, hR, b->zph);
+    k_ph_inputs<<<(unsigned)((b->T.n_ph + 255) / 256), 256, 0, b->stream>>>(b->T, b->wcc, hL, hR, exps, ccg,
+                                                                            b->zph);
     b->launches++;
   }
   const long n = b->T.n_asm2;
@@ -507,7 +530,8 @@ int launch_commutator_fp64_ws(imsrg_basis *b, const Workspace &ws, const double 
     b->launches++;
   }
   if (b->T.n_ph > 0) {
-    k_ph_inputs<<<(unsigned)((b->T.n_ph + 255) / 256), 256, 0, st>>>(b->T, ws.wcc, hL, hR, ws.zph);
+    k_ph_inputs<<<(unsigned)((b->T.n_ph + 255) / 256), 256, 0, st>>>(b->T, ws.wcc, hL, hR, nullptr, nullptr,
+                                                                       ws.zph);
     b->launches++;
   }
   const long n2 = b->T.n_asm2;

@@ -101,6 +101,7 @@ struct OzProb {
   int ldc;
   int gA, gB;
   int tiles_m, tile0, tiles;
+  int raw;  // store the exact int64 level sum v (result = v 2^k) instead of FP64: the WCC products
 };
 
 // Cost models of the CTA schedule tried by the autotuner (weights of K steps,
@@ -132,6 +133,7 @@ struct OzPlan {
   // are numbered part by part; part k owns [x_lo[k], x_lo[k + 1]).
   int group_lo[4] = {0, 0, 0, 0}, chunk_lo[4] = {0, 0, 0, 0}, linec_lo[4] = {0, 0, 0, 0}, liner_lo[4] = {0, 0, 0, 0};
   int *d_blk_mat = nullptr;  // slicing grids: matrix of each CTA's first line
+  int2 *d_ccgroups = nullptr;  // [ccblocks]: exponent groups of LCC and RCC block q1
   int cblocks[3] = {0, 0, 0}, rblocks[3] = {0, 0, 0}, blk_off[3] = {0, 0, 0};
   int grid = 0;
   int tune_choice = 0;                   // the schedule model the autotuner kept
@@ -589,6 +591,22 @@ __global__ void __launch_bounds__(OZ_THREADS, 1) k_oz_mma(const OzProb *__restri
       __syncwarp();
       if (lane == 0) mbar_arrive(&acc_empty[buf]);
       if (!live) continue;
+      if (P.raw) {
+        // WCC: the exact level sum stays an integer (the 222_ph recoupling
+        // combines four entries of one block, which share 2^k, before its one
+        // conversion to FP64)
+        long long *irow = reinterpret_cast<long long *>(crow);
+#pragma unroll
+        for (int c = 0; c < 16; c++) {
+          const long long v = ((long long)__float2int_rn(__uint_as_float(acc[0][c])) << 35) +
+                              ((long long)__float2int_rn(__uint_as_float(acc[1][c])) << 28) +
+                              ((long long)__float2int_rn(__uint_as_float(acc[2][c])) << 21) +
+                              __float2ll_rn(__uint_as_float(acc[3][c]));
+          const int n = n0 + c;
+          if (row_ok && n < Np) irow[(long)n * ldc] = v;
+        }
+        continue;
+      }
       const int k = (exps[gA] - 1022) + (exps[gB] - 1022) - 7 * OZ_LMAX;  // result = v * 2^k
 #pragma unroll
       for (int c = 0; c < 16; c++) {
@@ -866,6 +884,7 @@ int ozaki_prepare(imsrg_basis *b) {
     p.nterms = gp.nterms;
     double *dst = gp.c_dst == SRC_W1 ? b->w1 : gp.c_dst == SRC_W2 ? b->w2 : b->wcc;
     p.C = dst + gp.c_off;
+    p.raw = gp.c_dst == SRC_WCC;
     p.ldc = gp.ldc;
     for (int it = 0; it < gp.nterms; it++) {
       const GemmTerm &t = gp.t[it];
@@ -923,6 +942,10 @@ int ozaki_prepare(imsrg_basis *b) {
   IMSRG_TRY(up(sched.data(), sched.size() * sizeof(int2), (void **)&pl->d_sched));
   IMSRG_TRY(up(sched_off.data(), sched_off.size() * sizeof(int), (void **)&pl->d_sched_off));
   IMSRG_TRY(up(blk_mat.data(), blk_mat.size() * sizeof(int), (void **)&pl->d_blk_mat));
+  std::vector<int2> ccg(b->ccblocks);
+  for (int q1 = 0; q1 < b->ccblocks; q1++)
+    ccg[q1] = make_int2(pl->group_lo[2] + q1, pl->group_lo[2] + b->ccblocks + q1);
+  IMSRG_TRY(up(ccg.data(), ccg.size() * sizeof(int2), (void **)&pl->d_ccgroups));
   IMSRG_CUDA_TRY(cudaMalloc((void **)&pl->d_exps, std::max(pl->ngroups, 1) * sizeof(int)));
   IMSRG_CUDA_TRY(cudaMalloc((void **)&pl->d_err, sizeof(int)));
   IMSRG_CUDA_TRY(cudaMemset(pl->d_err, 0, sizeof(int)));
@@ -988,6 +1011,14 @@ int ozaki_check_error(imsrg_basis *b) {
   return IMSRG_OK;
 }
 
+int ozaki_wcc_scale(imsrg_basis *b, const int **exps, const int2 **ccgroups) {
+  OzPlan *pl = plan_of(b);
+  if (!pl || !pl->ok) return IMSRG_ERR_INVALID;
+  *exps = pl->d_exps;
+  *ccgroups = pl->d_ccgroups;
+  return IMSRG_OK;
+}
+
 bool ozaki_tuned(imsrg_basis *b) {
   OzPlan *pl = plan_of(b);
   return pl && pl->ok && pl->tuned;
@@ -1013,6 +1044,7 @@ void ozaki_free(imsrg_basis *b) {
   cudaFree(pl->d_sched);
   cudaFree(pl->d_sched_off);
   cudaFree(pl->d_blk_mat);
+  cudaFree(pl->d_ccgroups);
   cudaFree(pl->d_exps);
   cudaFree(pl->d_err);
   delete pl;
