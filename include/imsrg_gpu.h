@@ -273,9 +273,10 @@ int imsrg_gpu_profile_reset(imsrg_basis_t *b);
  * doubles each; herm_L, herm_R = +1 or -1; RES herm is -herm_L*herm_R).  The
  * intermediates live in one fixed array of IMSRG_NOALLOC_SCRATCH_DOUBLES
  * doubles (8 MiB) that the library holds on every device that loads it, so
- * the call allocates nothing.  Bases whose intermediates
- * (2*nfull + 2*cc_total + wcc_total doubles) do not fit are rejected with
- * IMSRG_ERR_TOO_LARGE (emax <= 4 fits; emax = 6 does not).
+ * the call allocates nothing.  Bases whose intermediates (two flat
+ * operators, the cross-coupled LCC and RCC, WCC, the 222_ph recoupling inputs
+ * and the E0 partials) do not fit are rejected with IMSRG_ERR_TOO_LARGE
+ * (emax <= 4 fits; emax = 6 does not).
  *  - The basis must have been created beforehand (creating it allocates the
  *    device tables once) and its device must be current.
  *  - The first call on each device looks up the array's device address; make
