@@ -211,6 +211,8 @@ def run_gpu(args, world, rank, local):
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
 
     precision = args.precision
+    if args.split_schedule is not None and precision != "fp64":
+        B.set_split_schedule(args.split_schedule)
     if precision == "auto":
         try:
             api.commutator(O, H, RES, precision="ozaki")
@@ -242,7 +244,13 @@ def run_gpu(args, world, rank, local):
         B.profile_reset()
         B.profile(True)
         for _ in range(min(steps, 200)):
-            flush.fill_(1.0)
+            # the flush runs on the library's stream, in order with the
+            # commutators (overlapping none of their kernels); while it runs
+            # the host enqueues the commutator's launches, so the kernel times
+            # carry no host launch latency (profiling replays launches one by
+            # one instead of the cached graph)
+            with torch.cuda.stream(stream):
+                flush.fill_(1.0)
             api.commutator(O, H, RES, precision=prec)
         B.synchronize()
         prof = B.profile_read()
@@ -272,59 +280,56 @@ def run_gpu(args, world, rank, local):
     else:
         extra["fp64_value"] = value
 
-    # roofline of the dominant kernel (measured live with events on the library stream)
-    kname, (kms, kn) = max(prof.items(), key=lambda kv: kv[1][0])
-    per_launch_s = (kms / 1e3) / max(kn, 1)
+    # roofline of the dominant kernel class: the class with the most device
+    # time per commutator, timed live with CUDA events on the library's stream
+    # (the profiled pass issues every launch on that one stream, so each event
+    # pair times its kernels alone).  A class may launch more than one kernel
+    # per commutator (slicing: three parts; two-body assembly: recoupling
+    # inputs + assembly), so times and work are per commutator.
+    n_prof = min(args.steps, 200)
     peaks = {}
     try:
         peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
     except (OSError, ValueError):
         pass
-    if kname in ("gemm_fp64",):
-        work = _workload_flops(lay) + _cc_flops(orb)
-        fp64_peak = _fp64_peak_tflops()
-        roof = {"kernel": kname, "bound": "fp64", "achieved": work / per_launch_s / 1e12, "peak": fp64_peak,
-                "unit": "TFLOP/s", "peak_source": "cuBLAS DGEMM 8192^3 measured in this run (FP64 pipe)"}
-    elif kname.startswith("ozaki_mma"):
-        work = prof_work_ozaki(lay, orb)
-        peak = peaks.get("bf16_tflops", 1951.5)
-        roof = {"kernel": kname, "bound": "tensor", "achieved": work / per_launch_s / 1e12, "peak": peak,
-                "unit": "TFLOP/s", "peak_source": "MEASURED_PEAKS.json bf16_tflops (of measured)"}
-    else:
-        work = _compulsory_bytes(lay)
-        peak = peaks.get("hbm_gbs", 6795.5)
-        roof = {"kernel": kname, "bound": "hbm", "achieved": work / per_launch_s / 1e9, "peak": peak,
-                "unit": "GB/s", "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)"}
-    roof["frac"] = roof["achieved"] / roof["peak"]
-    roof["traffic"] = _traffic_from_profiles(kname)
-    roof["algorithmic_per_launch"] = work
-    # every kernel class against its own bound: the contraction kernel against
-    # the tensor peak (FP64-equivalent algorithmic flops, and the BF16 flops the
-    # 21 digit products execute), the others against HBM with the compulsory
-    # bytes of one commutator
     hbm_peak = peaks.get("hbm_gbs", 6795.5)
     bf16_peak = peaks.get("bf16_tflops", 1951.5)
     comp = _compulsory_bytes(lay)
     alg_flops = _workload_flops(lay) + _cc_flops(orb)
-    roof_all = {}
-    for k, (ms_k, n_k) in prof.items():
-        if not n_k:
-            continue
-        per = (ms_k / 1e3) / n_k
+
+    def roof_of(k, per):
+        """One class against its bound: the contraction kernel against the
+        tensor peak with the BF16 flops its 21 digit products execute (and the
+        FP64-equivalent algorithmic flops beside them), the gather kernels
+        against HBM with the compulsory bytes of one commutator."""
         if k.startswith("ozaki_mma"):
-            roof_all[k] = {"bound": "tensor", "per_launch_us": per * 1e6,
-                           "achieved_fp64_equiv_tflops": alg_flops / per / 1e12,
-                           "executed_bf16_tflops": 21 * alg_flops / per / 1e12,
-                           "frac_executed_of_bf16_peak": 21 * alg_flops / per / 1e12 / bf16_peak}
-        elif k == "gemm_fp64":
-            roof_all[k] = {"bound": "fp64", "per_launch_us": per * 1e6, "achieved_tflops": alg_flops / per / 1e12}
-        else:
-            roof_all[k] = {"bound": "hbm", "per_launch_us": per * 1e6, "achieved_gbs": comp / per / 1e9,
-                           "frac": comp / per / 1e9 / hbm_peak, "traffic": _traffic_from_profiles(k)}
-    roof["all_kernels"] = roof_all
-    roof["per_launch_us"] = per_launch_s * 1e6
-    roof["kernel_share"] = {k: round(v[0] / max(sum(x[0] for x in prof.values()), 1e-12), 4)
-                            for k, v in prof.items() if v[1]}
+            return {"bound": "tensor", "achieved": 21 * alg_flops / per / 1e12, "peak": bf16_peak,
+                    "unit": "TFLOP/s", "peak_source": "MEASURED_PEAKS.json bf16_tflops (of measured)",
+                    "achieved_fp64_equiv_tflops": alg_flops / per / 1e12,
+                    "algorithmic_per_launch": 21 * alg_flops,
+                    "work_note": "executed BF16 flops = 21 digit products x 5.83e8 FP64-equivalent flop"}
+        if k == "gemm_fp64":
+            return {"bound": "fp64", "achieved": alg_flops / per / 1e12, "peak": _fp64_peak_tflops(),
+                    "unit": "TFLOP/s", "peak_source": "cuBLAS DGEMM 8192^3 measured in this run (FP64 pipe)",
+                    "algorithmic_per_launch": alg_flops}
+        return {"bound": "hbm", "achieved": comp / per / 1e9, "peak": hbm_peak, "unit": "GB/s",
+                "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)", "algorithmic_per_launch": comp,
+                "work_note": "compulsory bytes of one commutator: read L and R, write RES"}
+
+    per_comm = {k: (ms_k / 1e3) / n_prof for k, (ms_k, n_k) in prof.items() if n_k}
+    kname = max(per_comm, key=per_comm.get)
+    roof = {"kernel": kname}
+    roof.update(roof_of(kname, per_comm[kname]))
+    roof["frac"] = roof["achieved"] / roof["peak"]
+    roof["traffic"] = _traffic_from_profiles(kname)
+    roof["per_launch_us"] = per_comm[kname] * 1e6
+    roof["all_kernels"] = {}
+    for k, per in per_comm.items():
+        r = roof_of(k, per)
+        roof["all_kernels"][k] = {"bound": r["bound"], "per_launch_us": per * 1e6, "event_pairs_per_commutator":
+                                  prof[k][1] / n_prof, "achieved": r["achieved"], "unit": r["unit"],
+                                  "frac": r["achieved"] / r["peak"], "traffic": _traffic_from_profiles(k)}
+    roof["kernel_share"] = {k: round(v / max(sum(per_comm.values()), 1e-12), 4) for k, v in per_comm.items()}
 
     # end to end through the C ABI with pinned host buffers
     pin_o = torch.empty(lay.nfull, dtype=torch.float64, pin_memory=True).numpy()
@@ -360,7 +365,8 @@ def run_gpu(args, world, rank, local):
         }
         if precision == "ozaki":
             choice, us = B.split_schedule()
-            line["split_schedule_autotune"] = {"chosen_model": choice, "candidate_us": us}
+            line["split_schedule_autotune"] = {"chosen_model": choice, "candidate_us": us,
+                                               "pinned": args.split_schedule is not None}
         line.update(extra)
         if not args.no_flows:
             line["flow"] = flow_emax6(api, orb, lay)
@@ -473,6 +479,9 @@ def main():
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--no-flows", action="store_true", help="skip the flow and batched-flow extras")
     ap.add_argument("--batch", type=int, default=16, help="instances of the batched-flow extra")
+    ap.add_argument("--split-schedule", type=int, default=None,
+                    help="pin the split engine's CTA schedule model instead of autotuning it "
+                         "(for profiler runs, whose serialised launches distort the tuner's timings)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     world, rank, local = dist_setup()

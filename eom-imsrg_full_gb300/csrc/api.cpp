@@ -88,12 +88,18 @@ namespace imsrg {
 // so the call stays one ordered unit on that stream.
 int commutator_launches(imsrg_basis *b, const double *L, int hL, const double *R, int hR, double *RES, int hRES,
                         int precision, int with_e0) {
+  // While kernel timing is on, every launch goes to the basis stream in the
+  // same order, so each kernel class's event pair times that kernel alone.
+  const bool serial = b->prof.on;
+  cudaStream_t side = serial ? b->stream : b->side, side2 = serial ? b->stream : b->side2;
   auto fork = [&](int k) -> int {
+    if (serial) return IMSRG_OK;
     IMSRG_CUDA_TRY(cudaEventRecord(b->ev_fork[k], b->stream));
     IMSRG_CUDA_TRY(cudaStreamWaitEvent(b->side, b->ev_fork[k], 0));
     return IMSRG_OK;
   };
   auto join = [&](int k) -> int {
+    if (serial) return IMSRG_OK;
     IMSRG_CUDA_TRY(cudaEventRecord(b->ev_join[k], b->side));
     IMSRG_CUDA_TRY(cudaStreamWaitEvent(b->stream, b->ev_join[k], 0));
     return IMSRG_OK;
@@ -102,25 +108,27 @@ int commutator_launches(imsrg_basis *b, const double *L, int hL, const double *R
     // digit images of L and of R on the two side streams, beside the Pandya
     // transform and the images of LCC and RCC
     IMSRG_TRY(fork(0));
-    IMSRG_CUDA_TRY(cudaStreamWaitEvent(b->side2, b->ev_fork[0], 0));
-    IMSRG_TRY(ozaki_slice(b, L, R, 0, b->side));
-    IMSRG_TRY(ozaki_slice(b, L, R, 1, b->side2));
+    if (!serial) IMSRG_CUDA_TRY(cudaStreamWaitEvent(b->side2, b->ev_fork[0], 0));
+    IMSRG_TRY(ozaki_slice(b, L, R, 0, side));
+    IMSRG_TRY(ozaki_slice(b, L, R, 1, side2));
     IMSRG_TRY(launch_cc_forward(b, L, hL, R, hR));
     IMSRG_TRY(ozaki_slice(b, L, R, 2, b->stream));
     IMSRG_TRY(join(0));
-    IMSRG_CUDA_TRY(cudaEventRecord(b->ev_join2, b->side2));
-    IMSRG_CUDA_TRY(cudaStreamWaitEvent(b->stream, b->ev_join2, 0));
+    if (!serial) {
+      IMSRG_CUDA_TRY(cudaEventRecord(b->ev_join2, b->side2));
+      IMSRG_CUDA_TRY(cudaStreamWaitEvent(b->stream, b->ev_join2, 0));
+    }
     IMSRG_TRY(ozaki_mma(b, hL, hR));
   } else {
     IMSRG_TRY(launch_cc_forward(b, L, hL, R, hR));
     IMSRG_TRY(launch_gemm_fp64(b, L, hL, R, hR));
   }
-  // one-body assembly beside the two-body one; E0 after both
+  // one-body assembly and E0 beside the two-body assembly
   IMSRG_TRY(fork(1));
-  IMSRG_TRY(launch_assemble_1body(b, L, hL, R, hR, RES, hRES, b->side));
-  IMSRG_TRY(launch_assemble_2body(b, L, hL, R, hR, RES, hRES, with_e0, precision));
+  IMSRG_TRY(launch_assemble_1body(b, L, hL, R, hR, RES, hRES, side));
+  if (with_e0) IMSRG_TRY(launch_e0(b, L, hL, R, hR, RES, side));
+  IMSRG_TRY(launch_assemble_2body(b, L, hL, R, hR, RES, hRES, precision));
   IMSRG_TRY(join(1));
-  if (with_e0) IMSRG_TRY(launch_energy(b, L, hL, R, hR, RES, hL * hR == -1));
   return IMSRG_OK;
 }
 
@@ -926,6 +934,14 @@ int imsrg_gpu_magnus_decouple_graph(imsrg_op_t *HS, imsrg_op_t *G, double s_max,
 int imsrg_gpu_split_schedule(imsrg_basis_t *b, int *choice, int *ncand, double *us, int max) {
   if (!b) return IMSRG_ERR_INVALID;
   return imsrg::ozaki_schedule_info(b, choice, ncand, us, max);
+}
+
+int imsrg_gpu_split_schedule_set(imsrg_basis_t *b, int model) {
+  if (!b) return IMSRG_ERR_INVALID;
+  cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+  IMSRG_CUDA_TRY(cudaStreamIsCapturing(b->stream, &cs));
+  if (cs != cudaStreamCaptureStatusNone) return IMSRG_ERR_INVALID;
+  return imsrg::ozaki_set_schedule(b, model);
 }
 
 }  // extern "C"

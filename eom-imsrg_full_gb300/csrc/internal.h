@@ -268,10 +268,11 @@ inline int asm2_ctas(const imsrg_basis *b) { return (b->T.n_asm2 + ASM2_THREADS 
 int launch_cc_forward(imsrg_basis *b, const double *L, int hL, const double *R, int hR);
 int launch_gemm_fp64(imsrg_basis *b, const double *L, int hL, const double *R, int hR);
 int launch_assemble_2body(imsrg_basis *b, const double *L, int hL, const double *R, int hR, double *RES, int hRES,
-                          int with_e0, int precision);
+                          int precision);
 int launch_assemble_1body(imsrg_basis *b, const double *L, int hL, const double *R, int hR, double *RES, int hRES,
                           cudaStream_t st);
-int launch_energy(imsrg_basis *b, const double *L, int hL, const double *R, int hR, double *RES, int e220);
+// E0 of [L, R] into RES[0] on stream st (independent of the assembly kernels)
+int launch_e0(imsrg_basis *b, const double *L, int hL, const double *R, int hR, double *RES, cudaStream_t st);
 int launch_axpby(imsrg_basis *b, const double *A, double ax, const double *B, double bx, double *C);
 int launch_axpby_dev(imsrg_basis *b, const double *A, double ax, const double *B, const double *bx, double *C);
 int launch_norm(imsrg_basis *b, const double *op, double *d_out);
@@ -306,6 +307,7 @@ bool ozaki_tuned(imsrg_basis *b);       // the CTA schedule has been autotuned
 // groups g = ccgroups[q1] of cross-coupled block q1.
 int ozaki_wcc_scale(imsrg_basis *b, const int **exps, const int2 **ccgroups);
 int ozaki_schedule_info(imsrg_basis *b, int *choice, int *ncand, double *us, int max);
+int ozaki_set_schedule(imsrg_basis *b, int model);  // pin one cost model, no timing
 void ozaki_free(imsrg_basis *b);
 
 // Magnus flow step as a CUDA graph (graph.cu)

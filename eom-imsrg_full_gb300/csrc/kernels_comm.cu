@@ -1,6 +1,7 @@
 // kernels_comm.cu -- FP64 kernels of one scalar-scalar commutator [L, R].
 //
-// One commutator is four launches on the basis stream:
+// One commutator is these launches on the basis stream (4 and 5 on a side
+// stream beside 3):
 //   1. cc_forward      Pandya transform of L and R into LCC, RCC
 //                      (calculate_cross_coupled, cross_coupled.f90:1190-1300)
 //   2. gemm_fp64       every dense contraction as one grouped GEMM: the 12
@@ -8,14 +9,15 @@
 //                      commutator_222_pp_hh (commutators.f90:596-766) and the
 //                      WCC = LCC RCC^T products of commutator_222_ph (:792-802)
 //                      (the split-precision path replaces this launch)
-//   3. assemble_2body  every two-body element of RES in one pass: the
-//                      one-body insertions of commutator_122 (:283-396), the
+//   3. ph_inputs +     every two-body element of RES in one pass: the
+//      assemble_2body  one-body insertions of commutator_122 (:283-396), the
 //                      antisymmetrised ladder epilogue of 222_pp_hh
 //                      (:658-764) and the inverse Pandya recoupling of
 //                      222_ph (:804-923); RES is written once
 //   4. assemble_1body  every one-body element: commutator_111 (:36-80),
-//                      121 (:83-280) and 221 (:435-578), plus E0 from
-//                      110 + 220 (:10-33, :399-432)
+//                      121 (:83-280) and 221 (:435-578)
+//   5. e0              E0 from 110 + 220 (:10-33, :399-432), which need only
+//                      L and R
 // No float atomics: every reduction has a fixed order, so results are
 // bit-reproducible run to run.
 #include "device.cuh"
@@ -174,7 +176,19 @@ __global__ void __launch_bounds__(256) k_ph_inputs(DevTables T, const double *__
     const long long c = (p.nph ? -w3 : w3) + wcc_at_int(W, rl, y1, x1);
     const long long z = (hL < 0 ? -a : a) - (hR < 0 ? -c : c);
     const int2 g = ccg[p.qx];
-    Z[t] = ldexp((double)z, (exps[g.x] - 1022) + (exps[g.y] - 1022) - 49);
+    const int k = (exps[g.x] - 1022) + (exps[g.y] - 1022) - 49;
+    // z 2^k: add k to the exponent field on the integer pipe when the result
+    // stays normal (exactly ldexp's value), else ldexp
+    double d = (double)z;
+    unsigned long long bits = (unsigned long long)__double_as_longlong(d);
+    const int E = (int)((bits >> 52) & 0x7FF);
+    if (E != 0 && E + k > 0 && E + k < 2047) {
+      bits += (unsigned long long)(long long)k << 52;
+      d = __longlong_as_double((long long)bits);
+    } else if (E != 0) {
+      d = ldexp(d, k);
+    }
+    Z[t] = d;
     return;
   }
   const double *W = WCC + T.wcc_off[p.qx];
@@ -183,16 +197,82 @@ __global__ void __launch_bounds__(256) k_ph_inputs(DevTables T, const double *__
   Z[t] = dflip(a, hL < 0) - dflip(c, hR < 0);
 }
 
+// E0 = commutator_110 + commutator_220 (commutators.f90:10-33, 399-432) by one
+// CTA of NT threads; the 220 sum arrives as the two-body kernel's per-CTA
+// partials (e0p == nullptr: no 220 term).  Fixed order: strided per-thread
+// sums, warp shuffles, then thread 0 adds the warp totals in index order.
+// The partials were written by other CTAs, so they are read past L1.
+constexpr int ENERGY_THREADS = 256;
+
+template <int NT>
+__device__ void energy_block(const DevTables &T, const double *L, int hL, const double *R, int hR, double *RES,
+                             const double *e0p, int ne0p) {
+  __shared__ double sh[2][NT / 32];
+  const int A = T.A, P = T.P, tid = threadIdx.x;
+  const double *Lph = L + T.off_fph, *Rph = R + T.off_fph;
+  double v0 = 0.0, v1[4] = {0.0, 0.0, 0.0, 0.0};
+  for (int k = tid; k < P * A; k += NT) {
+    int ji = T.orb[T.hole_orb[k / P]].x;
+    v0 += (Lph[k] * Rph[k] * hL - Rph[k] * Lph[k] * hR) * (ji + 1);
+  }
+  if (e0p) {  // four independent chains, so the partials' loads overlap
+    int k = tid;
+    for (; k + 3 * NT < ne0p; k += 4 * NT) {
+#pragma unroll
+      for (int u = 0; u < 4; u++) v1[u] += __ldcg(e0p + k + u * NT);
+    }
+    for (; k < ne0p; k += NT) v1[0] += __ldcg(e0p + k);
+  }
+  v0 = warp_sum(v0);
+  const double s1 = warp_sum((v1[0] + v1[1]) + (v1[2] + v1[3]));
+  if ((tid & 31) == 0) {
+    sh[0][tid >> 5] = v0;
+    sh[1][tid >> 5] = s1;
+  }
+  __syncthreads();
+  if (tid == 0) {
+    double a = 0.0, c = 0.0;
+    for (int w = 0; w < NT / 32; w++) {
+      a += sh[0][w];
+      c += sh[1][w];
+    }
+    RES[0] = a + c * 2.0;
+  }
+}
+
+// commutator_122 (commutators.f90:283-396) of one element: f_L V_R - f_R V_L
+// over its leg terms
+__device__ __forceinline__ double sum122(const unsigned long long *tm, int n122, const double *L, int nL,
+                                              const double *R, int nR) {
+  double t = 0.0;
+  for (int k = 0; k < n122; k++) {
+    const unsigned long long u = tm[k];
+    const long vi = (long)(u & 0xFFFFFFFull), fi = (long)((u >> 28) & 0xFFFFFull);
+    const int sg = (int)(u >> 48) & 1, nsq = (int)(u >> 49) & 3, tr = (int)(u >> 51) & 1, ftr = (int)(u >> 52) & 1;
+    double vR = dflip(R[vi], tr & nR), vL = dflip(L[vi], tr & nL);
+    if (nsq) {
+      const double c = nsq == 1 ? IMSRG_SQRT2 : 2.0000000000000004;
+      vR = vR * c;
+      vL = vL * c;
+    }
+    const double fL = dflip(L[fi], (ftr & nL) ^ sg), fR = dflip(R[fi], (ftr & nR) ^ sg ^ 1);
+    t = fma(fL, vR, t);
+    t = fma(fR, vL, t);
+  }
+  return t;
+}
+
 // Every two-body element of RES once (upper triangles of square arrays, the
 // mirror written alongside): the one-body insertions of commutator_122, the
 // antisymmetrised ladder epilogue of 222_pp_hh (:658-764) and the 222_ph
-// recoupling sum over J' of {6j} Z(J').
+// recoupling sum over J' of {6j} Z(J').  has220 (the allocation-free path):
+// each CTA leaves its commutator_220 partial in e0p for k_energy.
 __global__ void __launch_bounds__(ASM2_THREADS) k_assemble_2body(DevTables T, const double *__restrict__ L, int hL,
                                                                  const double *__restrict__ R, int hR,
                                                                  const double *__restrict__ W1,
                                                                  const double *__restrict__ W2,
                                                                  const double *__restrict__ Z, double *RES, int hRES,
-                                                                 double *e0p) {
+                                                                 int has220, double *e0p) {
   __shared__ double sh220[ASM2_THREADS / 32];
   const long w = (long)blockIdx.x * blockDim.x + threadIdx.x;
   double e220 = 0.0;  // this element's commutator_220 term (pphh arrays only)
@@ -201,23 +281,7 @@ __global__ void __launch_bounds__(ASM2_THREADS) k_assemble_2body(DevTables T, co
     const unsigned long long *tm = T.asm2_terms + h.start;
     const unsigned meta = h.meta;
     const int nL = hL < 0, nR = hR < 0, nres = hRES < 0, npm = (hL * hR) < 0;
-    // commutator_122 (commutators.f90:283-396): f_L V_R - f_R V_L per leg term
-    const int n122 = meta & 31;
-    double t = 0.0;
-    for (int k = 0; k < n122; k++) {
-      const unsigned long long u = tm[k];
-      const long vi = (long)(u & 0xFFFFFFFull), fi = (long)((u >> 28) & 0xFFFFFull);
-      const int sg = (int)(u >> 48) & 1, nsq = (int)(u >> 49) & 3, tr = (int)(u >> 51) & 1, ftr = (int)(u >> 52) & 1;
-      double vR = dflip(R[vi], tr & nR), vL = dflip(L[vi], tr & nL);
-      if (nsq) {
-        const double c = nsq == 1 ? IMSRG_SQRT2 : 2.0000000000000004;
-        vR = vR * c;
-        vL = vL * c;
-      }
-      const double fL = dflip(L[fi], (ftr & nL) ^ sg), fR = dflip(R[fi], (ftr & nR) ^ sg ^ 1);
-      t = fma(fL, vR, t);
-      t = fma(fR, vL, t);
-    }
+    double t = sum122(tm, meta & 31, L, nL, R, nR);
     // / sqrt(1 + delta_ab) / sqrt(1 + delta_cd)
     const int nd = (meta >> 18) & 3;
     if (nd) t = t * (nd == 1 ? 0.7071067811865476 : 0.5);
@@ -245,9 +309,9 @@ __global__ void __launch_bounds__(ASM2_THREADS) k_assemble_2body(DevTables T, co
       if (square) RES[em] = dflip(t, nres);
     }
     // commutator_220 (commutators.f90:409-427): -(2J+1) L_pphh R_pphh herm_R
-    if (e0p && ((meta >> 22) & 1)) e220 = -L[e] * R[e] * hR * (h.J2 + 1.0);
+    if (has220 && ((meta >> 22) & 1)) e220 = -L[e] * R[e] * hR * (h.J2 + 1.0);
   }
-  if (e0p) {  // per-CTA partial in a fixed order; the energy kernel sums them
+  if (has220) {  // per-CTA partial in a fixed order
     e220 = warp_sum(e220);
     if ((threadIdx.x & 31) == 0) sh220[threadIdx.x >> 5] = e220;
     __syncthreads();
@@ -259,42 +323,52 @@ __global__ void __launch_bounds__(ASM2_THREADS) k_assemble_2body(DevTables T, co
   }
 }
 
-// Sum of NV values over the CTA (fixed order: warp shuffles, then warps in
-// index order), returned to every thread.
-template <int NV>
-__device__ void cta_sum(double *v, double (*sh)[8]) {
-  int w = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
-#pragma unroll
-  for (int i = 0; i < NV; i++) v[i] = warp_sum(v[i]);
-  if (lane == 0)
-#pragma unroll
-    for (int i = 0; i < NV; i++) sh[w][i] = v[i];
-  __syncthreads();
-#pragma unroll
-  for (int i = 0; i < NV; i++) {
-    double t = 0.0;
-    for (int k = 0; k < nw; k++) t += sh[k][i];
-    v[i] = t;
-  }
-  __syncthreads();
+// E0 for the allocation-free path: one CTA over the two-body kernel's partials.
+__global__ void __launch_bounds__(ENERGY_THREADS) k_energy(DevTables T, const double *L, int hL, const double *R,
+                                                           int hR, double *RES, const double *e0p, int ne0p) {
+  energy_block<ENERGY_THREADS>(T, L, hL, R, hR, RES, e0p, ne0p);
 }
 
-// E0 = commutator_110 + commutator_220 (commutators.f90:10-33, 399-432), one
-// CTA: the 220 sum arrives as the two-body kernel's per-CTA partials.
-__global__ void __launch_bounds__(1024) k_energy(DevTables T, const double *L, int hL, const double *R, int hR,
-                                                 double *RES, const double *e0p, int ne0p) {
-  __shared__ double sh[32][8];
-  const int A = T.A, P = T.P, tid = threadIdx.x, nt = blockDim.x;
+// E0 = commutator_110 + commutator_220 (commutators.f90:10-33, 399-432)
+// straight from L and R: the 220 sum needs only their pphh arrays, so E0 runs
+// beside the assembly kernels instead of after them.  One CTA; warp w takes
+// the (2J,Tz,pi) blocks w, w + 16, ... in turn; fixed summation order.
+constexpr int E0_THREADS = 512;
+
+__global__ void __launch_bounds__(E0_THREADS) k_e0(DevTables T, const double *__restrict__ L, int hL,
+                                                   const double *__restrict__ R, int hR, double *RES, int has220) {
+  __shared__ double sh[2][E0_THREADS / 32];
+  const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
+  const int A = T.A, P = T.P;
   const double *Lph = L + T.off_fph, *Rph = R + T.off_fph;
-  double v[2] = {0.0, 0.0};
-  for (int k = tid; k < P * A; k += nt) {
-    int ji = T.orb[T.hole_orb[k / P]].x;
-    v[0] += (Lph[k] * Rph[k] * hL - Rph[k] * Lph[k] * hR) * (ji + 1);
+  double v0 = 0.0, c = 0.0;
+  for (int k = tid; k < P * A; k += E0_THREADS) {
+    const int ji = T.orb[T.hole_orb[k / P]].x;
+    v0 += (Lph[k] * Rph[k] * hL - Rph[k] * Lph[k] * hR) * (ji + 1);
   }
-  if (e0p)
-    for (int k = tid; k < ne0p; k += nt) v[1] += e0p[k];
-  cta_sum<2>(v, sh);
-  if (tid == 0) RES[0] = v[0] + v[1] * 2.0;
+  if (has220)
+    for (int q = wid; q < T.nblocks; q += E0_THREADS / 32) {
+      const int n = T.gam_n1[q * 6 + 2] * T.gam_n2[q * 6 + 2];
+      const double *Lq = L + T.gam_off[q * 6 + 2], *Rq = R + T.gam_off[q * 6 + 2];
+      double s = 0.0;
+      for (int k = lane; k < n; k += 32) s = fma(Lq[k], Rq[k], s);
+      c += (T.blk_J2[q] + 1.0) * warp_sum(s);
+    }
+  v0 = warp_sum(v0);
+  if (lane == 0) {
+    sh[0][wid] = v0;
+    sh[1][wid] = c;
+  }
+  __syncthreads();
+  if (tid == 0) {
+    double a = 0.0, cc = 0.0;
+    for (int w = 0; w < E0_THREADS / 32; w++) {
+      a += sh[0][w];
+      cc += sh[1][w];
+    }
+    // 2 sum_q (2J+1) sum -L_pphh R_pphh herm_R
+    RES[0] = a - 2.0 * hR * cc;
+  }
 }
 
 // One-body assembly.  The (l,j,tz)-allowed upper-triangle elements carry the
@@ -467,7 +541,7 @@ int launch_gemm_fp64(imsrg_basis *b, const double *L, int hL, const double *R, i
 }
 
 int launch_assemble_2body(imsrg_basis *b, const double *L, int hL, const double *R, int hR, double *RES, int hRES,
-                          int with_e0, int precision) {
+                          int precision) {
   ProfScope ps(b, IMSRG_KERNEL_ASSEMBLE_2BODY);
   const int *exps = nullptr;
   const int2 *ccg = nullptr;
@@ -479,11 +553,17 @@ int launch_assemble_2body(imsrg_basis *b, const double *L, int hL, const double 
   }
   const long n = b->T.n_asm2;
   if (n > 0) {
-    double *e0p = (with_e0 && hL * hR == -1) ? b->partials : nullptr;
     k_assemble_2body<<<(unsigned)((n + ASM2_THREADS - 1) / ASM2_THREADS), ASM2_THREADS, 0, b->stream>>>(
-        b->T, L, hL, R, hR, b->w1, b->w2, b->zph, RES, hRES, e0p);
+        b->T, L, hL, R, hR, b->w1, b->w2, b->zph, RES, hRES, 0, nullptr);
     b->launches++;
   }
+  return cuda_status(cudaGetLastError());
+}
+
+int launch_e0(imsrg_basis *b, const double *L, int hL, const double *R, int hR, double *RES, cudaStream_t st) {
+  ProfScope ps(b, IMSRG_KERNEL_ASSEMBLE_1BODY, st);
+  k_e0<<<1, E0_THREADS, 0, st>>>(b->T, L, hL, R, hR, RES, hL * hR == -1);
+  b->launches++;
   return cuda_status(cudaGetLastError());
 }
 
@@ -497,12 +577,6 @@ int launch_assemble_1body(imsrg_basis *b, const double *L, int hL, const double 
   return cuda_status(cudaGetLastError());
 }
 
-int launch_energy(imsrg_basis *b, const double *L, int hL, const double *R, int hR, double *RES, int e220) {
-  ProfScope ps(b, IMSRG_KERNEL_ASSEMBLE_1BODY);
-  k_energy<<<1, 1024, 0, b->stream>>>(b->T, L, hL, R, hR, RES, e220 ? b->partials : nullptr, asm2_ctas(b));
-  b->launches++;
-  return cuda_status(cudaGetLastError());
-}
 
 // The four FP64 launches of one commutator with caller-chosen workspace and
 // stream; used by the allocation-free entry point (noalloc.cu).  Allocates
@@ -536,9 +610,9 @@ int launch_commutator_fp64_ws(imsrg_basis *b, const Workspace &ws, const double 
   }
   const long n2 = b->T.n_asm2;
   if (n2 > 0) {
-    double *e0p = (with_e0 && hL * hR == -1) ? ws.e0p : nullptr;
+    const int has220 = with_e0 && hL * hR == -1;
     k_assemble_2body<<<(unsigned)((n2 + ASM2_THREADS - 1) / ASM2_THREADS), ASM2_THREADS, 0, st>>>(
-        b->T, L, hL, R, hR, ws.w1, ws.w2, ws.zph, RES, hRES, e0p);
+        b->T, L, hL, R, hR, ws.w1, ws.w2, ws.zph, RES, hRES, has220, ws.e0p);
     b->launches++;
   }
   const int grid1 = b->T.n_asm1_heavy + (b->T.n_asm1_light + 3) / 4;
@@ -548,7 +622,7 @@ int launch_commutator_fp64_ws(imsrg_basis *b, const Workspace &ws, const double 
   }
   if (with_e0) {
     const bool e220 = hL * hR == -1;
-    k_energy<<<1, 1024, 0, st>>>(b->T, L, hL, R, hR, RES, e220 ? ws.e0p : nullptr, asm2_ctas(b));
+    k_energy<<<1, ENERGY_THREADS, 0, st>>>(b->T, L, hL, R, hR, RES, e220 ? ws.e0p : nullptr, asm2_ctas(b));
     b->launches++;
   }
   return cuda_status(cudaGetLastError());

@@ -1024,6 +1024,21 @@ bool ozaki_tuned(imsrg_basis *b) {
   return pl && pl->ok && pl->tuned;
 }
 
+// Pins the CTA schedule to one cost model instead of timing them all (for
+// runs whose event timings are distorted, e.g. under a profiler that
+// serialises launches).  Timings read back as 0 for a pinned schedule.
+int ozaki_set_schedule(imsrg_basis *b, int model) {
+  if (model < 0 || model >= kNumSchedModels) return IMSRG_ERR_INVALID;
+  IMSRG_TRY(ozaki_prepare(b));
+  OzPlan *pl = plan_of(b);
+  if (!pl || !pl->ok) return IMSRG_ERR_INVALID;
+  IMSRG_TRY(use_model(b, pl, model));
+  for (int c = 0; c < kNumSchedModels; c++) pl->tune_us[c] = 0.0;
+  pl->tune_choice = model;
+  pl->tuned = true;
+  return IMSRG_OK;
+}
+
 int ozaki_schedule_info(imsrg_basis *b, int *choice, int *ncand, double *us, int max) {
   OzPlan *pl = plan_of(b);
   if (!pl || !pl->ok || !pl->tuned) return IMSRG_ERR_INVALID;

@@ -35,7 +35,7 @@ SYMBOLS = (
     "imsrg_gpu_basis_get_stream", "imsrg_gpu_basis_set_stream", "imsrg_gpu_profile_enable",
     "imsrg_gpu_profile_read", "imsrg_gpu_profile_reset", "imsrg_gpu_commutator_noalloc",
     "imsrg_gpu_magnus_decouple_graph", "imsrg_gpu_magnus_decouple_batch", "imsrg_gpu_magnus_decouple_tangent",
-    "imsrg_gpu_split_schedule", "imsrg_gpu_build_gs_atan", "imsrg_gpu_build_gs_w2", "imsrg_gpu_magnus_decouple_gen",
+    "imsrg_gpu_split_schedule", "imsrg_gpu_split_schedule_set", "imsrg_gpu_build_gs_atan", "imsrg_gpu_build_gs_w2", "imsrg_gpu_magnus_decouple_gen",
     "imsrg_gpu_op_save", "imsrg_gpu_op_load", "imsrg_gpu_checkpoint_name", "imsrg_gpu_normal_order",
     "imsrg_gpu_dhds", "imsrg_gpu_transform_bch",
 )
@@ -108,6 +108,7 @@ def lib():
                                                 ip],
             "imsrg_gpu_magnus_decouple_tangent": [vp, vp, vp, vp, d, d, i, i, dp, dp, ip, ip],
             "imsrg_gpu_split_schedule": [vp, ip, ip, dp, i],
+            "imsrg_gpu_split_schedule_set": [vp, i],
             "imsrg_gpu_build_gs_atan": [vp, vp],
             "imsrg_gpu_build_gs_w2": [vp, vp, i],
             "imsrg_gpu_magnus_decouple_gen": [vp, vp, i, d, d, i, i, dp, ip, ip],
@@ -203,6 +204,12 @@ class Basis:
         us = np.zeros(16)
         _check(lib().imsrg_gpu_split_schedule(self._h, C.byref(ch), C.byref(nc), _dp(us), 16), "split_schedule")
         return ch.value, us[:nc.value].tolist()
+
+    def set_split_schedule(self, model: int):
+        """Pin the split engine's CTA schedule to candidate `model` without
+        timing (e.g. under a profiler whose serialised launches distort the
+        autotuner's event timings); results do not depend on the schedule."""
+        _check(lib().imsrg_gpu_split_schedule_set(self._h, int(model)), "split_schedule_set")
 
     def block_dims(self, q):
         a, b, c = C.c_int(), C.c_int(), C.c_int()

@@ -235,6 +235,11 @@ int imsrg_gpu_magnus_decouple_tangent(imsrg_op_t *HS, imsrg_op_t *dHS, imsrg_op_
  * use.  That first use allocates and synchronises, so it must not happen
  * inside a stream capture. */
 int imsrg_gpu_split_schedule(imsrg_basis_t *b, int *choice, int *ncand, double *us, int max);
+/* Pins that schedule to candidate model (0 <= model < ncand) without timing
+ * (no reference counterpart): for runs whose event timings do not reflect
+ * the kernel alone, such as under a profiler that serialises launches.  The
+ * schedule never changes results.  Allocates and synchronises on first use. */
+int imsrg_gpu_split_schedule_set(imsrg_basis_t *b, int model);
 
 const char *imsrg_gpu_strerror(int status);
 /* Number of library kernel launches issued so far on this basis. */

@@ -96,3 +96,36 @@ def test_split_schedule_is_autotuned(gpu_lib):
     choice, us = B.split_schedule()
     assert len(us) >= 2 and all(t > 0 for t in us)
     assert us[choice] == min(us)
+
+
+def test_pinned_split_schedule_gives_identical_results(gpu_lib):
+    """Each CTA schedule computes every tile the same way, so a commutator is
+    bit-identical whichever candidate schedule is pinned."""
+    bas, lay, B, Hh, Oh = _pair(gpu_lib, 4)
+    O, H = gpu_lib.Operator(B, -1, Oh), gpu_lib.Operator(B, 1, Hh)
+    R = gpu_lib.Operator(B, 1)
+    gpu_lib.commutator(O, H, R, precision="ozaki")
+    ref = R.download()
+    _, us = B.split_schedule()
+    for model in range(len(us)):
+        B.set_split_schedule(model)
+        assert B.split_schedule()[0] == model
+        gpu_lib.commutator(O, H, R, precision="ozaki")
+        assert np.array_equal(R.download(), ref), model
+    with pytest.raises(gpu_lib.ImsrgError):
+        B.set_split_schedule(len(us))
+
+
+@pytest.mark.parametrize("scale", [2.0 ** -40, 2.0 ** 70, 2.0 ** 200])
+def test_ozaki_any_magnitude_matches_fp64(gpu_lib, scale):
+    """Operands far from MeV magnitudes: the digit scales follow each block's
+    exponent, so the split path matches the FP64 path at any magnitude (a
+    diverging BCH series must end as in FP64)."""
+    bas, lay, B, Hh, Oh = _pair(gpu_lib, 4)
+    O, H = gpu_lib.Operator(B, -1, Oh), gpu_lib.Operator(B, 1, Hh * scale)
+    R64, Roz = gpu_lib.Operator(B, 1), gpu_lib.Operator(B, 1)
+    gpu_lib.commutator(O, H, R64, precision="fp64")
+    gpu_lib.commutator(O, H, Roz, precision="ozaki")
+    a, b = Roz.download(), R64.download()
+    assert np.all(np.isfinite(a))
+    assert rel_err(a, b) <= 1e-9
