@@ -111,8 +111,11 @@ int commutator_launches(imsrg_basis *b, const double *L, int hL, const double *R
     if (!serial) IMSRG_CUDA_TRY(cudaStreamWaitEvent(b->side2, b->ev_fork[0], 0));
     IMSRG_TRY(ozaki_slice(b, L, R, 0, side));
     IMSRG_TRY(ozaki_slice(b, L, R, 1, side2));
-    IMSRG_TRY(launch_cc_forward(b, L, hL, R, hR));
-    IMSRG_TRY(ozaki_slice(b, L, R, 2, b->stream));
+    // the transform also reduces the LCC/RCC block exponents
+    int *cc_exps = nullptr, gL = 0, gR = 0;
+    IMSRG_TRY(ozaki_cc_exponents(b, b->stream, &cc_exps, &gL, &gR));
+    IMSRG_TRY(launch_cc_forward(b, L, hL, R, hR, cc_exps, gL, gR));
+    IMSRG_TRY(ozaki_slice(b, L, R, 2, b->stream, cc_exps != nullptr));
     IMSRG_TRY(join(0));
     if (!serial) {
       IMSRG_CUDA_TRY(cudaEventRecord(b->ev_join2, b->side2));

@@ -604,6 +604,7 @@ int build_basis(imsrg_basis *b) {
     IMSRG_TRY(dev_upload(b, zt, &T.ph_terms));
 
     std::vector<std::pair<long, int>> cit;
+    T.ccf_packed = b->cc_total < (1L << 24) && b->ccblocks <= 128;
     for (int q1 = 0; q1 < b->ccblocks; q1++) {
       int rlen = b->cc_rlen[q1], nph = b->cc_nph[q1], JC = b->cc_J2[q1];
       const int *rows = cc_rowpair.data() + cc_rowstart[q1];
@@ -616,9 +617,14 @@ int build_basis(imsrg_basis *b) {
             n = jpcount(std::max(std::abs(b->jj[p] - b->jj[bb]), std::abs(b->jj[a] - b->jj[h])),
                         std::min(b->jj[p] + b->jj[bb], b->jj[a] + b->jj[h]));
           (void)JC;
-          cit.push_back({n, (int)(b->cc_off[q1] + r + (long)nb * rlen)});
+          // the block id rides in bits 24-30 when it fits (the transform
+          // then also reduces each block's largest exponent)
+          const int packed = T.ccf_packed ? q1 << 24 : 0;
+          cit.push_back({n, (int)(b->cc_off[q1] + r + (long)nb * rlen) | packed});
         }
     }
+    // stable: within one term count the elements stay in block order, so the
+    // lanes of a warp mostly share a block
     std::stable_sort(cit.begin(), cit.end(),
                      [](const std::pair<long, int> &x, const std::pair<long, int> &y) { return x.first < y.first; });
     std::vector<int> corder(cit.size());

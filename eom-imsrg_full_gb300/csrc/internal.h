@@ -59,8 +59,9 @@ struct DevTables {
   int n_asm2;
   const struct PhTerm *ph_terms;
   int n_ph;
-  const int *ccf_order;    // cross-coupled elements
+  const int *ccf_order;    // cross-coupled elements (bits 0-23), with their block in bits 24-30 if ccf_packed
   int n_ccf;
+  int ccf_packed;
   // Gather lists of the Pandya transform: element e of every CC block is
   // sum_k cct_coef[k] * op[cct_idx[k] & 0x7fffffff] (bit 31: read transposed,
   // times herm), k in [cct_start[e], cct_start[e + 1]).
@@ -265,7 +266,10 @@ constexpr int ASM2_THREADS = 128;
 inline int asm2_ctas(const imsrg_basis *b) { return (b->T.n_asm2 + ASM2_THREADS - 1) / ASM2_THREADS; }
 
 // launchers (kernels_*.cu); all enqueue on b->stream and bump b->launches
-int launch_cc_forward(imsrg_basis *b, const double *L, int hL, const double *R, int hR);
+// Pandya transform into b->lcc, b->rcc; exps != nullptr: also the largest
+// exponent of each LCC block q1 into exps[gL + q1] and RCC block into exps[gR + q1]
+int launch_cc_forward(imsrg_basis *b, const double *L, int hL, const double *R, int hR, int *exps = nullptr,
+                      int gL = 0, int gR = 0);
 int launch_gemm_fp64(imsrg_basis *b, const double *L, int hL, const double *R, int hR);
 int launch_assemble_2body(imsrg_basis *b, const double *L, int hL, const double *R, int hR, double *RES, int hRES,
                           int precision);
@@ -298,7 +302,13 @@ int launch_commutator_fp64_ws(imsrg_basis *b, const Workspace &ws, const double 
 int ozaki_prepare(imsrg_basis *b);  // plans and allocates the engine once; errors if unavailable
 // part 0: exponents and digit images of L; part 1: of R; part 2: of LCC and
 // RCC (after the Pandya transform).  ozaki_mma then runs every contraction.
-int ozaki_slice(imsrg_basis *b, const double *L, const double *R, int part, cudaStream_t st);
+// exps_ready: the part's block exponents are already in place (part 2: the
+// Pandya transform reduced them, see ozaki_cc_exponents).
+int ozaki_slice(imsrg_basis *b, const double *L, const double *R, int part, cudaStream_t st,
+                bool exps_ready = false);
+// Where the Pandya transform may leave the LCC/RCC block exponents (zeroed on
+// st here): exps[gL + q1], exps[gR + q1]; *exps = nullptr if it cannot.
+int ozaki_cc_exponents(imsrg_basis *b, cudaStream_t st, int **exps, int *gL, int *gR);
 int ozaki_mma(imsrg_basis *b, int hL, int hR);
 int ozaki_check_error(imsrg_basis *b);  // IMSRG_ERR_TIMEOUT if a bounded device wait gave up
 bool ozaki_tuned(imsrg_basis *b);       // the CTA schedule has been autotuned

@@ -29,23 +29,42 @@ namespace {
 // ---------------------------------------------------------------------------
 // 1. Pandya transform: CCX(r(a,b), nb(p,h)) of cross_coupled.f90:1247-1291.
 // ---------------------------------------------------------------------------
+// exps != nullptr (split-precision path, ccf_packed): also the largest IEEE
+// exponent of every LCC block (into exps[gL + block]) and RCC block (exps[gR +
+// block]) for the digit slicing: lanes of a warp that share a block combine
+// theirs, one integer atomicMax per block and warp (order-independent).
 __global__ void __launch_bounds__(256) k_cc_forward(DevTables T, const double *__restrict__ L, int hL,
-                                                    const double *__restrict__ R, int hR, double *LCC, double *RCC) {
-  long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= T.cc_total) return;
-  const long e = T.ccf_order[t];  // elements grouped by term count
-  const int k0 = T.cct_start[e], k1 = T.cct_start[e + 1];
-  const int nL = hL < 0, nR = hR < 0;
-  double sl = 0.0, sr = 0.0;
-  for (int k = k0; k < k1; k++) {
-    const int ix = T.cct_idx[k];
-    const int tr = (int)((unsigned)ix >> 31), idx = ix & 0x7fffffff;
-    const double c = T.cct_coef[k];
-    sl = fma(c, dflip(L[idx], tr & nL), sl);
-    sr = fma(c, dflip(R[idx], tr & nR), sr);
+                                                    const double *__restrict__ R, int hR, double *LCC, double *RCC,
+                                                    int *exps, int gL, int gR) {
+  const long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  int q1 = -1, xL = 0, xR = 0;
+  if (t < T.cc_total) {
+    const int v = T.ccf_order[t];  // elements grouped by term count
+    const long e = T.ccf_packed ? (v & 0xFFFFFF) : v;
+    if (T.ccf_packed) q1 = v >> 24;
+    const int k0 = T.cct_start[e], k1 = T.cct_start[e + 1];
+    const int nL = hL < 0, nR = hR < 0;
+    double sl = 0.0, sr = 0.0;
+    for (int k = k0; k < k1; k++) {
+      const int ix = T.cct_idx[k];
+      const int tr = (int)((unsigned)ix >> 31), idx = ix & 0x7fffffff;
+      const double c = T.cct_coef[k];
+      sl = fma(c, dflip(L[idx], tr & nL), sl);
+      sr = fma(c, dflip(R[idx], tr & nR), sr);
+    }
+    LCC[e] = sl;
+    RCC[e] = sr;
+    xL = (int)((__double_as_longlong(sl) >> 52) & 0x7FF);
+    xR = (int)((__double_as_longlong(sr) >> 52) & 0x7FF);
   }
-  LCC[e] = sl;
-  RCC[e] = sr;
+  if (exps) {  // every lane of the warp takes part (no early exit above)
+    const unsigned peers = __match_any_sync(0xffffffffu, q1);
+    const int mL = __reduce_max_sync(peers, xL), mR = __reduce_max_sync(peers, xR);
+    if (q1 >= 0 && (int)(threadIdx.x & 31) == __ffs(peers) - 1) {
+      atomicMax(exps + gL + q1, mL);
+      atomicMax(exps + gR + q1, mR);
+    }
+  }
 }
 
 // ---------------------------------------------------------------------------
@@ -512,11 +531,12 @@ __global__ void __launch_bounds__(128) k_assemble_1body(DevTables T, const doubl
 
 }  // namespace
 
-int launch_cc_forward(imsrg_basis *b, const double *L, int hL, const double *R, int hR) {
+int launch_cc_forward(imsrg_basis *b, const double *L, int hL, const double *R, int hR, int *exps, int gL, int gR) {
   long n = b->cc_total;
   if (n == 0) return IMSRG_OK;
   ProfScope ps(b, IMSRG_KERNEL_CC_FORWARD);
-  k_cc_forward<<<(unsigned)((n + 255) / 256), 256, 0, b->stream>>>(b->T, L, hL, R, hR, b->lcc, b->rcc);
+  k_cc_forward<<<(unsigned)((n + 255) / 256), 256, 0, b->stream>>>(b->T, L, hL, R, hR, b->lcc, b->rcc, exps, gL,
+                                                                   gR);
   b->launches++;
   return cuda_status(cudaGetLastError());
 }
@@ -585,7 +605,8 @@ int launch_commutator_fp64_ws(imsrg_basis *b, const Workspace &ws, const double 
                               double *RES, int hRES, int with_e0, cudaStream_t st) {
   long ncc = b->cc_total;
   if (ncc > 0) {
-    k_cc_forward<<<(unsigned)((ncc + 255) / 256), 256, 0, st>>>(b->T, L, hL, R, hR, ws.lcc, ws.rcc);
+    k_cc_forward<<<(unsigned)((ncc + 255) / 256), 256, 0, st>>>(b->T, L, hL, R, hR, ws.lcc, ws.rcc, nullptr, 0,
+                                                                 0);
     b->launches++;
   }
   if (b->ntiles > 0) {

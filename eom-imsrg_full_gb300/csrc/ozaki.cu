@@ -959,15 +959,27 @@ int ozaki_prepare(imsrg_basis *b) {
   return IMSRG_OK;
 }
 
-int ozaki_slice(imsrg_basis *b, const double *L, const double *R, int part, cudaStream_t st) {
+int ozaki_cc_exponents(imsrg_basis *b, cudaStream_t st, int **exps, int *gL, int *gR) {
+  OzPlan *pl = plan_of(b);
+  *exps = nullptr;
+  if (!pl || !pl->ok || !b->T.ccf_packed) return IMSRG_OK;
+  const int g0 = pl->group_lo[2], g1 = pl->group_lo[3];
+  if (g1 > g0) IMSRG_CUDA_TRY(cudaMemsetAsync(pl->d_exps + g0, 0, (g1 - g0) * sizeof(int), st));
+  *exps = pl->d_exps;
+  *gL = g0;
+  *gR = g0 + b->ccblocks;
+  return IMSRG_OK;
+}
+
+int ozaki_slice(imsrg_basis *b, const double *L, const double *R, int part, cudaStream_t st, bool exps_ready) {
   OzPlan *pl = plan_of(b);
   if (!pl) return IMSRG_ERR_INVALID;
   ProfScope ps(b, IMSRG_KERNEL_OZAKI_SLICE, st);
   if (part < 0 || part > 2) return IMSRG_ERR_INVALID;
   const int g0 = pl->group_lo[part], g1 = pl->group_lo[part + 1];
   const int k0 = pl->chunk_lo[part], k1 = pl->chunk_lo[part + 1];
-  if (g1 > g0) IMSRG_CUDA_TRY(cudaMemsetAsync(pl->d_exps + g0, 0, (g1 - g0) * sizeof(int), st));
-  if (k1 > k0) {
+  if (g1 > g0 && !exps_ready) IMSRG_CUDA_TRY(cudaMemsetAsync(pl->d_exps + g0, 0, (g1 - g0) * sizeof(int), st));
+  if (k1 > k0 && !exps_ready) {
     k_oz_exponents<<<k1 - k0, 256, 0, st>>>(pl->d_chunks + k0, L, R, b->lcc, b->rcc, pl->d_exps);
     b->launches++;
   }
