@@ -83,6 +83,18 @@ int generator_dev(imsrg_basis *b, const double *H, int hH, double *ETA, int gene
 
 namespace imsrg {
 
+int work_op(imsrg_basis *b, int k, imsrg_op **out) { return tmp_op(b, k, out); }
+
+// dHds (IMSRG_ODE.f90:416-463) on device buffers: DH = [eta(HS), HS].
+int dhds_dev(imsrg_basis *b, const double *HS, int hH, double *DH, int generator, int precision) {
+  imsrg_op *ETA;
+  IMSRG_TRY(tmp_op(b, 14, &ETA));
+  IMSRG_CUDA_TRY(cudaMemsetAsync(ETA->d, 0, sizeof(double), b->stream));
+  ETA->herm = -1;
+  IMSRG_TRY(generator_dev(b, HS, hH, ETA->d, generator, precision));
+  return commutator_dev(b, ETA->d, -1, HS, hH, DH, hH, precision, 1);
+}
+
 // The launch sequence of one commutator.  Independent launches run on the
 // side stream, forked from and joined back into the basis stream with events,
 // so the call stays one ordered unit on that stream.
@@ -596,14 +608,8 @@ int imsrg_gpu_dhds(const imsrg_op_t *HS, imsrg_op_t *DH, int generator, int prec
   if (HS->b != DH->b) return IMSRG_ERR_MISMATCH;
   if (HS == DH) return IMSRG_ERR_INVALID;
   if (precision != IMSRG_PREC_FP64 && precision != IMSRG_PREC_OZAKI) return IMSRG_ERR_INVALID;
-  imsrg_basis *b = HS->b;
-  imsrg_op *ETA;
-  IMSRG_TRY(tmp_op(b, 14, &ETA));
-  IMSRG_CUDA_TRY(cudaMemsetAsync(ETA->d, 0, sizeof(double), b->stream));
-  ETA->herm = -1;
-  IMSRG_TRY(generator_dev(b, HS->d, HS->herm, ETA->d, generator, precision));
   DH->herm = HS->herm;
-  return imsrg::commutator_dev(b, ETA->d, -1, HS->d, HS->herm, DH->d, HS->herm, precision, 1);
+  return imsrg::dhds_dev(HS->b, HS->d, HS->herm, DH->d, generator, precision);
 }
 
 int imsrg_gpu_op_save(const imsrg_op_t *op, const char *path) {

@@ -322,6 +322,10 @@ void ozaki_free(imsrg_basis *b);
 
 // Magnus flow step as a CUDA graph (graph.cu)
 int flow_tmp_ops(imsrg_basis *b, imsrg_op **H0, imsrg_op **DG, imsrg_op **X0, imsrg_op **X1);  // api.cpp
+// work operator k of the basis (created on first use; 15 and 16 belong to the ODE flow)
+int work_op(imsrg_basis *b, int k, imsrg_op **out);
+// dHds (IMSRG_ODE.f90:416-463): DH = [eta(HS), HS] with generator IMSRG_GEN_*
+int dhds_dev(imsrg_basis *b, const double *HS, int hH, double *DH, int generator, int precision);
 int flow_graph_begin(imsrg_op *HS, imsrg_op *G, int precision, double ds, double *e0, double *emp2);
 int flow_graph_launch(imsrg_basis *b);
 int flow_graph_finish(imsrg_basis *b, double *s, double *e0, double *emp2, int *nc, int *status);

@@ -37,7 +37,7 @@ SYMBOLS = (
     "imsrg_gpu_magnus_decouple_graph", "imsrg_gpu_magnus_decouple_batch", "imsrg_gpu_magnus_decouple_tangent",
     "imsrg_gpu_split_schedule", "imsrg_gpu_split_schedule_set", "imsrg_gpu_build_gs_atan", "imsrg_gpu_build_gs_w2", "imsrg_gpu_magnus_decouple_gen",
     "imsrg_gpu_op_save", "imsrg_gpu_op_load", "imsrg_gpu_checkpoint_name", "imsrg_gpu_normal_order",
-    "imsrg_gpu_dhds", "imsrg_gpu_transform_bch",
+    "imsrg_gpu_dhds", "imsrg_gpu_transform_bch", "imsrg_gpu_ode_decouple",
 )
 
 KERNELS = ("cc_forward", "gemm_fp64", "assemble_2body", "assemble_1body", "ozaki_slice", "ozaki_mma",
@@ -117,6 +117,7 @@ def lib():
             "imsrg_gpu_checkpoint_name": [C.c_char_p, C.c_char_p, d, C.c_char_p, i],
             "imsrg_gpu_normal_order": [vp],
             "imsrg_gpu_dhds": [vp, vp, i, i],
+            "imsrg_gpu_ode_decouple": [vp, i, i, d, d, i, d, d, dp, ip, C.POINTER(C.c_long)],
             "imsrg_gpu_transform_bch": [vp, vp, i, ip],
         }
         for name, args in sig.items():
@@ -478,6 +479,20 @@ def normal_order(H: Operator):
 
 def dhds(HS: Operator, DH: Operator, generator: str = "white", precision: str = "fp64"):
     _check(lib().imsrg_gpu_dhds(HS.handle, DH.handle, GENERATORS[generator], PREC[precision]), "dhds")
+
+
+def ode_decouple(HS: Operator, generator: str = "white", precision: str = "fp64", ds: float = 0.1,
+                 s_max: float = 0.0, max_steps: int = 10000, relerr: float = 1e-6, abserr: float = 1e-6):
+    """decouple_hamiltonian (IMSRG_ODE.f90:9-178): the Shampine-Gordon flow of
+    HS (advanced in place) in output steps of ds until |E_mbpt2| < 1e-6 (or
+    s >= s_max > 0, or max_steps).  Returns steps, the trace rows (step, s, E0,
+    E0 + E_mbpt2, |E_mbpt2|) and the number of derivative evaluations."""
+    trace = np.zeros(5 * (max_steps + 1))
+    st, nf = C.c_int(0), C.c_long(0)
+    _check(lib().imsrg_gpu_ode_decouple(HS.handle, GENERATORS[generator], PREC[precision], float(ds), float(s_max),
+                                        int(max_steps), float(relerr), float(abserr), _dp(trace), C.byref(st),
+                                        C.byref(nf)), "ode_decouple")
+    return dict(steps=st.value, trace=trace[:5 * (st.value + 1)].reshape(-1, 5), nfev=nf.value)
 
 
 def transform_bch(Op: Operator, G: Operator, precision: str = "fp64") -> int:

@@ -174,6 +174,20 @@ int imsrg_gpu_build_gs_w2(const imsrg_op_t *H, imsrg_op_t *ETA, int precision);
  * imsrg_gpu_op_download_packed is its yp vector). */
 int imsrg_gpu_dhds(const imsrg_op_t *HS, imsrg_op_t *DH, int generator, int precision);
 
+/* decouple_hamiltonian (IMSRG_ODE.f90:9-178), one operator: integrates
+ * dHS/ds = [eta(HS), HS] with the Shampine-Gordon Adams solver of
+ * adams_ode.f90 (ODE/DE/STEP/INTRP, :33-1357; the reference passes relerr =
+ * abserr = 1e-6 and ds = 0.1) in output steps of ds, continuing the
+ * integration across steps, until |E_mbpt2| < 1e-6, or s >= s_max when
+ * s_max > 0 (not in the reference), or max_steps steps (the reference's
+ * 10000).  HS (herm +1) is advanced in place.  trace receives
+ * (step, s, E0, E0 + E_mbpt2, |E_mbpt2|) per step, (max_steps + 1) x 5
+ * doubles, like the reference's _0bflow.dat; *steps_out the steps taken,
+ * *nfev the derivative evaluations.  relerr/abserr may be raised by the
+ * solver as the reference's are (its IFLAG 3). */
+int imsrg_gpu_ode_decouple(imsrg_op_t *HS, int generator, int precision, double ds, double s_max, int max_steps,
+                           double relerr, double abserr, double *trace, int *steps_out, long *nfev);
+
 /* --- Magnus flow ------------------------------------------------------- */
 /* MAGNUS_EXPAND (IMSRG_MAGNUS.f90:622-693): DG in = eta, out = dOmega/ds.
  * *ncomm = commutators evaluated. */
