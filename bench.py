@@ -370,6 +370,7 @@ def run_gpu(args, world, rank, local):
         line.update(extra)
         if not args.no_flows:
             line["flow"] = flow_emax6(api, orb, lay)
+            line["ode"] = ode_emax6(api, orb, lay)
             line["batch"] = batch_flows(api, args.batch)
         if world == 1 and not args.no_cpu_baseline:
             line["cpu_baseline"] = cpu_baseline(orb, lay, seconds=args.cpu_seconds)
@@ -398,6 +399,28 @@ def flow_emax6(api, orb, lay):
         dt = time.perf_counter() - t0
         out[prec] = {"steps": r["steps"], "commutators": r["ncomm"], "e0_MeV": float(r["trace"][-1, 2]),
                      "seconds": dt, "commutators_per_s": r["ncomm"] / dt}
+    out["abs_dE0_MeV"] = abs(out["ozaki"]["e0_MeV"] - out["fp64"]["e0_MeV"])
+    return out
+
+
+def ode_emax6(api, orb, lay):
+    """The emax = 6 ODE flow (decouple_hamiltonian with the Shampine-Gordon
+    solver, ds = 0.1, tolerances 1e-6) to |E_mbpt2| < 1e-6 in split precision
+    and in FP64: E0 difference, output steps, derivative evaluations (one
+    generator + one commutator each), wall time."""
+    from imsrg_gpu.synth import synth_hamiltonian
+    B = api.Basis.from_dict(orb)
+    Hh = synth_hamiltonian(lay, 13)
+    out = {"emax": EMAX, "ds": 0.1, "relerr": 1e-6, "abserr": 1e-6}
+    for prec in ("ozaki", "fp64"):
+        HS = api.Operator(B, 1, Hh)
+        api.ode_decouple(api.Operator(B, 1, Hh), precision=prec, s_max=0.1)  # warm-up (plans, graphs)
+        B.synchronize()
+        t0 = time.perf_counter()
+        r = api.ode_decouple(HS, precision=prec, max_steps=2000)
+        dt = time.perf_counter() - t0
+        out[prec] = {"steps": r["steps"], "s": float(r["trace"][-1, 1]), "derivatives": r["nfev"],
+                     "e0_MeV": float(r["trace"][-1, 2]), "seconds": dt, "derivatives_per_s": r["nfev"] / dt}
     out["abs_dE0_MeV"] = abs(out["ozaki"]["e0_MeV"] - out["fp64"]["e0_MeV"])
     return out
 
