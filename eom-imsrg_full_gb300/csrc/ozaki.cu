@@ -19,7 +19,10 @@
 //   3. k_oz_mma: persistent kernel, one 128 x 64 output tile at a time.  A
 //      producer thread streams the six A digit planes and fifteen B planes
 //      (d_1..d_6, 2^7 d_1..d_5, 2^14 d_1..d_4) of each K = 16 step into
-//      shared memory with cp.async.bulk; one thread issues the 21
+//      shared memory with two TMA tensor loads (3-D boxes: 256-byte core
+//      matrix rows x row groups x planes, one per operand; one request per
+//      plane measured 4.8 us slower per commutator at 12 instead of 21
+//      requests, whatever the bytes); one thread issues the 21
 //      tcgen05.mma products d_s x d_t with s + t <= 7 (negating A for terms
 //      with coefficient -1) into four FP32 accumulators in TMEM: one per
 //      level l = s + t = 2, 3, 4 and one "tail" that sums levels 5, 6, 7 in
@@ -41,6 +44,8 @@
 //
 // Every mbarrier wait is bounded (about 2 s of %globaltimer); a timeout sets
 // an error flag that the host reports as IMSRG_ERR_TIMEOUT.
+#include <cuda.h>
+#include <cudaTypedefs.h>
 #include <cuda_bf16.h>
 
 #include <algorithm>
@@ -91,6 +96,7 @@ struct OzTerm {
   const uint8_t *a_img, *b_img;
   long a_plane, b_plane;
   int a_rg, b_rg;
+  int a_map, b_map;  // tensor maps of the A and B images (index into the plan's maps)
   int neg, use_hl, use_hr;
 };
 
@@ -141,6 +147,8 @@ struct OzPlan {
   bool tuned = false;
   std::vector<int> tile_ksteps, tile_live;  // per tile: K steps x terms, live outputs / 64
   std::vector<int2> tile_slot;
+  std::vector<CUtensorMap> maps;     // TMA maps of the digit images, by role (see map_of)
+  CUtensorMap *d_maps = nullptr;
   bool ok = false;
 };
 
@@ -192,11 +200,14 @@ __device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity, volati
   }
 }
 
-__device__ __forceinline__ void bulk_g2s(void *sdst, const void *gsrc, uint32_t bytes, uint64_t *bar) {
+// One 3-D TMA tile of a digit image into shared memory (x = 0: the 16-byte
+// rule on the innermost coordinate always holds; rows past the image arrive
+// as zeros).
+__device__ __forceinline__ void tma_load_3d(void *sdst, const CUtensorMap *map, int y, int z, uint64_t *bar) {
   asm volatile(
-      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
-          smem_u32(sdst)),
-      "l"(gsrc), "r"(bytes), "r"(smem_u32(bar))
+      "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], "
+      "[%5];" ::"r"(smem_u32(sdst)),
+      "l"(reinterpret_cast<uint64_t>(map)), "r"(0), "r"(y), "r"(z), "r"(smem_u32(bar))
       : "memory");
 }
 
@@ -394,7 +405,8 @@ __global__ void __launch_bounds__(256) k_oz_slice(const OzMatrix *__restrict__ m
 __global__ void __launch_bounds__(OZ_THREADS, 1) k_oz_mma(const OzProb *__restrict__ probs, int nprobs,
                                                           const int2 *__restrict__ sched,
                                                           const int *__restrict__ sched_off,
-                                                          const int *__restrict__ exps, int hL, int hR, int *err) {
+                                                          const int *__restrict__ exps, int hL, int hR, int *err,
+                                                          const CUtensorMap *__restrict__ maps) {
   extern __shared__ __align__(1024) uint8_t smem_raw[];
   uint8_t *smem = (uint8_t *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
   uint64_t *full = (uint64_t *)(smem + STAGES * STAGE_BYTES);
@@ -419,12 +431,7 @@ __global__ void __launch_bounds__(OZ_THREADS, 1) k_oz_mma(const OzProb *__restri
     *abort_flag = 0;
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
-  // Tiles copy only the row groups that exist; the rows of a stage past M (or
-  // N) keep digits of an earlier tile, which only reach accumulator rows (or
-  // columns) that are never stored.  Zeroing the stages once keeps those rows
-  // finite from the start.
-  for (int i = threadIdx.x; i < STAGES * STAGE_BYTES / 16; i += blockDim.x)
-    reinterpret_cast<uint4 *>(smem)[i] = make_uint4(0u, 0u, 0u, 0u);
+  // (every stage is written whole by its two TMA boxes before the MMAs read it)
   asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
   if (warp == 1) {
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_slot)),
@@ -450,27 +457,21 @@ __global__ void __launch_bounds__(OZ_THREADS, 1) k_oz_mma(const OzProb *__restri
         int tm = lt % P.tiles_m, tn = lt / P.tiles_m;
         for (int it = 0; it < P.nterms; it++) {
           const OzTerm &T = P.t[it];
-          // row groups of this tile present in the images (the rest of the stage is not read back)
-          const uint32_t a_bytes = (uint32_t)min(TM / 8, T.a_rg - tm * (TM / 8)) * 256u;
-          const uint32_t b_bytes = (uint32_t)min(TN / 8, T.b_rg - tn * (TN / 8)) * 256u;
+          const CUtensorMap *amap = maps + T.a_map, *bmap = maps + T.b_map;
           for (int kk = 0; kk < P.ksteps; kk++) {
             if (!mbar_wait(&empty[stage], phase ^ 1, abort_flag)) {
               atomicExch(err, 1);
               *abort_flag = 1;
               break;
             }
-            mbar_expect_tx(&full[stage], OZ_S * a_bytes + OZ_BPLANES * b_bytes);
+            // two whole boxes: the row groups past the tile's operand rows
+            // (next K step's rows, or zeros past the image) only reach
+            // accumulator rows and columns that are never stored
+            mbar_expect_tx(&full[stage], STAGE_BYTES);
             uint8_t *sa = smem + stage * STAGE_BYTES;
             uint8_t *sb = sa + OZ_S * A_SLICE_BYTES;
-            const uint8_t *ga = T.a_img + ((long)kk * T.a_rg + tm * (TM / 8)) * 256;
-            const uint8_t *gb = T.b_img + ((long)kk * T.b_rg + tn * (TN / 8)) * 256;
-#pragma unroll
-            for (int s = 0; s < OZ_S; s++) {
-              bulk_g2s(sa + s * A_SLICE_BYTES, ga + s * T.a_plane, a_bytes, &full[stage]);
-            }
-#pragma unroll
-            for (int k = 0; k < OZ_BPLANES; k++)
-              bulk_g2s(sb + k * B_SLICE_BYTES, gb + k * T.b_plane, b_bytes, &full[stage]);
+            tma_load_3d(sa, amap, kk * T.a_rg + tm * (TM / 8), 0, &full[stage]);
+            tma_load_3d(sb, bmap, kk * T.b_rg + tn * (TN / 8), 0, &full[stage]);
             if (++stage == STAGES) {
               stage = 0;
               phase ^= 1;
@@ -695,7 +696,7 @@ int autotune(imsrg_basis *b, OzPlan *pl, int hL, int hR) {
   auto launch_timed = [&](float *ms) -> int {
     IMSRG_CUDA_TRY(cudaEventRecord(e0, b->stream));
     k_oz_mma<<<pl->grid, OZ_THREADS, smem, b->stream>>>(pl->d_probs, pl->nprobs, pl->d_sched, pl->d_sched_off,
-                                                       pl->d_exps, hL, hR, pl->d_err);
+                                                       pl->d_exps, hL, hR, pl->d_err, pl->d_maps);
     b->launches++;
     IMSRG_CUDA_TRY(cudaEventRecord(e1, b->stream));
     IMSRG_CUDA_TRY(cudaEventSynchronize(e1));
@@ -871,6 +872,44 @@ int ozaki_prepare(imsrg_basis *b) {
     pl->img[s] = (uint8_t *)p;
   }
 
+  // TMA maps of the images, one per (image, role): a digit image is planes x
+  // (K steps x row groups) x 256-byte core-matrix rows; an A tile is the box
+  // 16 row groups x 6 planes, a B tile 8 row groups x 15 planes.  The encoder
+  // is the driver's cuTensorMapEncodeTiled, reached through the runtime.
+  static PFN_cuTensorMapEncodeTiled_v12000 encode = nullptr;
+  if (!encode) {
+    void *fn = nullptr;
+    cudaDriverEntryPointQueryResult q = cudaDriverEntryPointSymbolNotFound;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &q) !=
+            cudaSuccess ||
+        q != cudaDriverEntryPointSuccess || !fn)
+      return IMSRG_ERR_CUDA;
+    encode = (PFN_cuTensorMapEncodeTiled_v12000)fn;
+  }
+  std::map<std::pair<const uint8_t *, int>, int> map_index;
+  auto map_of = [&](const uint8_t *img, long plane, int np, int brole, int *idx) -> int {
+    auto it = map_index.find({img, brole});
+    if (it != map_index.end()) {
+      *idx = it->second;
+      return IMSRG_OK;
+    }
+    const cuuint32_t box_planes = brole ? OZ_BPLANES : OZ_S;
+    if (plane <= 0 || plane % 256 || (long)np < (long)box_planes) return IMSRG_ERR_INVALID;
+    CUtensorMap m;
+    const cuuint64_t gdim[3] = {32, (cuuint64_t)(plane / 256), (cuuint64_t)np};
+    const cuuint64_t gstride[2] = {256, (cuuint64_t)plane};
+    const cuuint32_t box[3] = {32, (cuuint32_t)(brole ? TN / 8 : TM / 8), box_planes};
+    const cuuint32_t estride[3] = {1, 1, 1};
+    if (encode(&m, CU_TENSOR_MAP_DATA_TYPE_UINT64, 3, (void *)img, gdim, gstride, box, estride,
+               CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+               CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
+      return IMSRG_ERR_INVALID;
+    *idx = (int)pl->maps.size();
+    pl->maps.push_back(m);
+    map_index[{img, brole}] = *idx;
+    return IMSRG_OK;
+  };
+
   // problems: the FP64 grouped-GEMM list mapped onto images
   int tiles = 0;
   std::vector<int> &tile_ksteps = pl->tile_ksteps, &tile_live = pl->tile_live;
@@ -898,6 +937,8 @@ int ozaki_prepare(imsrg_basis *b) {
         o.b_img = pl->img[B.src] + (t.tb ? B.img_r : B.img_c);
         o.b_plane = t.tb ? B.plane_r : B.plane_c;
         o.b_rg = t.tb ? B.rg_r : B.rg_c;
+        IMSRG_TRY(map_of(o.a_img, o.a_plane, t.ta ? A.np_c : A.np_r, 0, &o.a_map));
+        IMSRG_TRY(map_of(o.b_img, o.b_plane, t.tb ? B.np_r : B.np_c, 1, &o.b_map));
         if (it == 0) {
           p.gA = A.group;
           p.gB = B.group;
@@ -942,6 +983,8 @@ int ozaki_prepare(imsrg_basis *b) {
   IMSRG_TRY(up(sched.data(), sched.size() * sizeof(int2), (void **)&pl->d_sched));
   IMSRG_TRY(up(sched_off.data(), sched_off.size() * sizeof(int), (void **)&pl->d_sched_off));
   IMSRG_TRY(up(blk_mat.data(), blk_mat.size() * sizeof(int), (void **)&pl->d_blk_mat));
+  // (cudaMalloc memory is 256-byte aligned: the 64-byte alignment of a tensor map holds)
+  IMSRG_TRY(up(pl->maps.data(), pl->maps.size() * sizeof(CUtensorMap), (void **)&pl->d_maps));
   std::vector<int2> ccg(b->ccblocks);
   for (int q1 = 0; q1 < b->ccblocks; q1++)
     ccg[q1] = make_int2(pl->group_lo[2] + q1, pl->group_lo[2] + b->ccblocks + q1);
@@ -1005,7 +1048,7 @@ int ozaki_mma(imsrg_basis *b, int hL, int hR) {
   ProfScope ps(b, IMSRG_KERNEL_OZAKI_MMA);
   const int smem = STAGES * STAGE_BYTES + 1024 + 256;
   k_oz_mma<<<pl->grid, OZ_THREADS, smem, b->stream>>>(pl->d_probs, pl->nprobs, pl->d_sched, pl->d_sched_off,
-                                                     pl->d_exps, hL, hR, pl->d_err);
+                                                     pl->d_exps, hL, hR, pl->d_err, pl->d_maps);
   b->launches++;
   return cuda_status(cudaGetLastError());
 }
@@ -1073,6 +1116,7 @@ void ozaki_free(imsrg_basis *b) {
   cudaFree(pl->d_blk_mat);
   cudaFree(pl->d_ccgroups);
   cudaFree(pl->d_exps);
+  cudaFree(pl->d_maps);
   cudaFree(pl->d_err);
   delete pl;
   b->ozaki = nullptr;
