@@ -506,6 +506,7 @@ __global__ void __launch_bounds__(OZ_THREADS, 1) k_oz_mma(const OzProb *__restri
           const OzTerm &T = P.t[it];
           int neg = T.neg ^ (T.use_hl & (hL < 0)) ^ (T.use_hr & (hR < 0));
           const uint32_t idesc = idesc_bf16(TM, TN, neg);
+          const uint32_t idesc2 = idesc_bf16(TM, 2 * TN, neg), idesc3 = idesc_bf16(TM, 3 * TN, neg);
           for (int kk = 0; kk < P.ksteps; kk++) {
             if (!mbar_wait(&full[stage], phase, abort_flag)) {
               atomicExch(err, 3);
@@ -518,17 +519,22 @@ __global__ void __launch_bounds__(OZ_THREADS, 1) k_oz_mma(const OzProb *__restri
             const uint64_t db = da + (uint64_t)((OZ_S * A_SLICE_BYTES) >> 4);
 #pragma unroll
             for (int s = 0; s < OZ_S; s++) {
+              // level l = s + u + 2 (digits are 1-based).  Levels 2..4 have
+              // their own accumulators, side by side in TMEM, and B planes
+              // u = 0, 1, 2 lie side by side in the stage: the exact products
+              // of A plane s are one MMA of width (3 - s) x 64 into
+              // accumulators s..2 (s <= 2).  Levels 5..7 share the tail
+              // accumulator, with B pre-scaled by 2^(7 (7 - l)).  The first
+              // product into every accumulator of a tile overwrites it.
+              if (s <= 2)
+                mma_bf16(dbase + (uint32_t)(s * TN), da + (uint64_t)(s * (A_SLICE_BYTES >> 4)), db,
+                         s == 0 ? idesc3 : s == 1 ? idesc2 : idesc, (first && s == 0) ? 0 : 1);
 #pragma unroll
-              for (int u = 0; u < OZ_S - s; u++) {
-                // level l = s + u + 2 (digits are 1-based): levels 2..4 have
-                // their own accumulator; 5..7 share the tail accumulator, with
-                // B pre-scaled by 2^(7 (7 - l)); the first product of every
-                // accumulator in a tile (s = 0, u <= 3) overwrites it
+              for (int u = s <= 2 ? 3 - s : 0; u < OZ_S - s; u++) {
                 const int lvl = s + u + 2;
-                const int acc_i = lvl <= 4 ? lvl - 2 : 3;
-                const int bp = lvl <= 4 || lvl == 7 ? u : lvl == 6 ? 6 + u : 11 + u;
-                mma_bf16(dbase + (uint32_t)(acc_i * TN), da + (uint64_t)(s * (A_SLICE_BYTES >> 4)),
-                         db + (uint64_t)(bp * (B_SLICE_BYTES >> 4)), idesc, (first && s == 0 && u <= 3) ? 0 : 1);
+                const int bp = lvl == 7 ? u : lvl == 6 ? 6 + u : 11 + u;
+                mma_bf16(dbase + (uint32_t)(3 * TN), da + (uint64_t)(s * (A_SLICE_BYTES >> 4)),
+                         db + (uint64_t)(bp * (B_SLICE_BYTES >> 4)), idesc, (first && s == 0 && u == 3) ? 0 : 1);
               }
             }
             first = false;
