@@ -337,16 +337,14 @@ def run_gpu(args, world, rank, local):
     pin_r = torch.empty(lay.nfull, dtype=torch.float64, pin_memory=True).numpy()
     pin_o[:], pin_h[:] = Oh, Hh
     n_e2e = max(min(args.steps // 2, 500), 3)
+    # imsrg_gpu_commutator_host: copy Omega and H in, commutator, copy RES out,
+    # returning when RES is in host memory (one call per step)
     for _ in range(2):
-        O.upload(pin_o); H.upload(pin_h); api.commutator(O, H, RES, precision=precision)
-        RES.download(out=pin_r)
+        api.commutator_host(B, pin_o, -1, pin_h, 1, pin_r, precision=precision)
     B.synchronize()
     t0 = time.perf_counter()
     for _ in range(n_e2e):
-        O.upload(pin_o)
-        H.upload(pin_h)
-        api.commutator(O, H, RES, precision=precision)
-        RES.download(out=pin_r)
+        api.commutator_host(B, pin_o, -1, pin_h, 1, pin_r, precision=precision)
     e2e_dt = time.perf_counter() - t0
     e2e = {"value": world * n_e2e / e2e_dt, "unit": UNIT, "h2d_bytes_per_step": 2 * lay.nfull * 8,
            "d2h_bytes_per_step": lay.nfull * 8}

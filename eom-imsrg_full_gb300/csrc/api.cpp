@@ -99,15 +99,21 @@ int dhds_dev(imsrg_basis *b, const double *HS, int hH, double *DH, int generator
 // side stream, forked from and joined back into the basis stream with events,
 // so the call stays one ordered unit on that stream.
 int commutator_launches(imsrg_basis *b, const double *L, int hL, const double *R, int hR, double *RES, int hRES,
-                        int precision, int with_e0) {
+                        int precision, int with_e0, const HostIO *io = nullptr) {
   // While kernel timing is on, every launch goes to the basis stream in the
   // same order, so each kernel class's event pair times that kernel alone.
   const bool serial = b->prof.on;
   cudaStream_t side = serial ? b->stream : b->side, side2 = serial ? b->stream : b->side2;
+  const size_t bytes = (size_t)b->nfull * sizeof(double);
+  if (io) {  // host operands: L first, so the digit images of L start while R is in flight
+    IMSRG_CUDA_TRY(cudaMemcpyAsync(const_cast<double *>(L), io->L, bytes, cudaMemcpyHostToDevice, b->stream));
+    IMSRG_CUDA_TRY(cudaEventRecord(b->ev_hostL, b->stream));
+    IMSRG_CUDA_TRY(cudaMemcpyAsync(const_cast<double *>(R), io->R, bytes, cudaMemcpyHostToDevice, b->stream));
+  }
   auto fork = [&](int k) -> int {
     if (serial) return IMSRG_OK;
     IMSRG_CUDA_TRY(cudaEventRecord(b->ev_fork[k], b->stream));
-    IMSRG_CUDA_TRY(cudaStreamWaitEvent(b->side, b->ev_fork[k], 0));
+    IMSRG_CUDA_TRY(cudaStreamWaitEvent(b->side, (io && k == 0) ? b->ev_hostL : b->ev_fork[k], 0));
     return IMSRG_OK;
   };
   auto join = [&](int k) -> int {
@@ -144,6 +150,7 @@ int commutator_launches(imsrg_basis *b, const double *L, int hL, const double *R
   if (with_e0) IMSRG_TRY(launch_e0(b, L, hL, R, hR, RES, side));
   IMSRG_TRY(launch_assemble_2body(b, L, hL, R, hR, RES, hRES, precision));
   IMSRG_TRY(join(1));
+  if (io) IMSRG_CUDA_TRY(cudaMemcpyAsync(io->RES, RES, bytes, cudaMemcpyDeviceToHost, b->stream));
   return IMSRG_OK;
 }
 
@@ -156,18 +163,30 @@ constexpr size_t kCommGraphs = 8;
 // and replayed (one launch instead of ~12, and no host work per kernel); the
 // graph runs the same kernels on the same data, so results are unchanged.
 int commutator_dev(imsrg_basis *b, const double *L, int hL, const double *R, int hR, double *RES, int hRES,
-                   int precision, int with_e0) {
+                   int precision, int with_e0, const HostIO *io) {
   if (precision != IMSRG_PREC_FP64 && precision != IMSRG_PREC_OZAKI) return IMSRG_ERR_INVALID;
   if (precision == IMSRG_PREC_OZAKI) IMSRG_TRY(ozaki_prepare(b));
   cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
   IMSRG_CUDA_TRY(cudaStreamIsCapturing(b->stream, &cs));
-  const bool graphable = !b->prof.on && cs == cudaStreamCaptureStatusNone &&
+  bool pinned = true;  // host copies enter a graph only from page-locked memory
+  if (io)
+    for (const void *p : {(const void *)io->L, (const void *)io->R, (const void *)io->RES}) {
+      cudaPointerAttributes a{};
+      if (cudaPointerGetAttributes(&a, p) != cudaSuccess || a.type != cudaMemoryTypeHost) {
+        cudaGetLastError();
+        pinned = false;
+      }
+    }
+  const bool graphable = !b->prof.on && cs == cudaStreamCaptureStatusNone && pinned &&
                          (precision != IMSRG_PREC_OZAKI || ozaki_tuned(b));
-  if (!graphable) return commutator_launches(b, L, hL, R, hR, RES, hRES, precision, with_e0);
+  if (!graphable) return commutator_launches(b, L, hL, R, hR, RES, hRES, precision, with_e0, io);
+  const HostIO none{nullptr, nullptr, nullptr};
+  const HostIO &key = io ? *io : none;
   b->comm_calls++;
   for (imsrg_basis::CommGraph &g : b->comm_graphs)
     if (g.L == L && g.R == R && g.RES == RES && g.hL == hL && g.hR == hR && g.hRES == hRES &&
-        g.precision == precision && g.with_e0 == with_e0) {
+        g.precision == precision && g.with_e0 == with_e0 && g.io.L == key.L && g.io.R == key.R &&
+        g.io.RES == key.RES) {
       g.last_use = b->comm_calls;
       b->launches += g.nlaunch;
       return cuda_status(cudaGraphLaunch(g.exec, b->stream));
@@ -175,7 +194,7 @@ int commutator_dev(imsrg_basis *b, const double *L, int hL, const double *R, int
   // capture the sequence of this argument set
   IMSRG_CUDA_TRY(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
   const long launches0 = b->launches;
-  int s = commutator_launches(b, L, hL, R, hR, RES, hRES, precision, with_e0);
+  int s = commutator_launches(b, L, hL, R, hR, RES, hRES, precision, with_e0, io);
   cudaGraph_t graph = nullptr;
   cudaError_t e = cudaStreamEndCapture(b->stream, &graph);
   IMSRG_TRY(s);
@@ -191,7 +210,7 @@ int commutator_dev(imsrg_basis *b, const double *L, int hL, const double *R, int
     cudaGraphExecDestroy(b->comm_graphs[lru].exec);
     b->comm_graphs.erase(b->comm_graphs.begin() + lru);
   }
-  b->comm_graphs.push_back({L, R, RES, hL, hR, hRES, precision, with_e0, exec, b->comm_calls,
+  b->comm_graphs.push_back({L, R, RES, hL, hR, hRES, precision, with_e0, key, exec, b->comm_calls,
                             b->launches - launches0});
   return cuda_status(cudaGraphLaunch(exec, b->stream));
 }
@@ -486,6 +505,30 @@ int imsrg_gpu_commutator(const imsrg_op_t *L, const imsrg_op_t *R, imsrg_op_t *R
   int hRES = -L->herm * R->herm;
   RES->herm = hRES;
   return imsrg::commutator_dev(L->b, L->d, L->herm, R->d, R->herm, RES->d, hRES, precision, with_e0 ? 1 : 0);
+}
+
+int imsrg_gpu_commutator_host(imsrg_basis_t *b, const double *L, int herm_L, const double *R, int herm_R,
+                              double *RES, int precision, int with_e0) {
+  if (!b || !L || !R || !RES) return IMSRG_ERR_INVALID;
+  if ((herm_L != 1 && herm_L != -1) || (herm_R != 1 && herm_R != -1)) return IMSRG_ERR_INVALID;
+  const size_t bytes = (size_t)b->nfull * sizeof(double);
+  auto overlap = [&](const void *x, const void *y) {
+    const char *p = (const char *)x, *q = (const char *)y;
+    return p < q + bytes && q < p + bytes;
+  };
+  if (overlap(RES, L) || overlap(RES, R)) return IMSRG_ERR_INVALID;
+  imsrg_op *dL, *dR, *dRES;  // device copies of the operands (work operators 17-19)
+  IMSRG_TRY(tmp_op(b, 17, &dL));
+  IMSRG_TRY(tmp_op(b, 18, &dR));
+  IMSRG_TRY(tmp_op(b, 19, &dRES));
+  dL->herm = herm_L;
+  dR->herm = herm_R;
+  dRES->herm = -herm_L * herm_R;
+  const imsrg::HostIO io{L, R, RES};
+  IMSRG_TRY(imsrg::commutator_dev(b, dL->d, herm_L, dR->d, herm_R, dRES->d, dRES->herm, precision, with_e0 ? 1 : 0,
+                                  &io));
+  IMSRG_CUDA_TRY(cudaStreamSynchronize(b->stream));
+  return imsrg::ozaki_check_error(b);
 }
 
 int imsrg_gpu_build_gs_white(const imsrg_op_t *H, imsrg_op_t *ETA) {

@@ -356,6 +356,7 @@ int build_basis(imsrg_basis *b) {
   IMSRG_CUDA_TRY(cudaStreamCreateWithFlags(&b->side, cudaStreamNonBlocking));
   IMSRG_CUDA_TRY(cudaStreamCreateWithFlags(&b->side2, cudaStreamNonBlocking));
   IMSRG_CUDA_TRY(cudaEventCreateWithFlags(&b->ev_join2, cudaEventDisableTiming));
+  IMSRG_CUDA_TRY(cudaEventCreateWithFlags(&b->ev_hostL, cudaEventDisableTiming));
   for (int k = 0; k < 2; k++) {
     IMSRG_CUDA_TRY(cudaEventCreateWithFlags(&b->ev_fork[k], cudaEventDisableTiming));
     IMSRG_CUDA_TRY(cudaEventCreateWithFlags(&b->ev_join[k], cudaEventDisableTiming));
@@ -844,7 +845,8 @@ void free_basis_device(imsrg_basis *b) {
   if (b->side2) cudaStreamDestroy(b->side2);
   b->side = b->side2 = nullptr;
   if (b->ev_join2) cudaEventDestroy(b->ev_join2);
-  b->ev_join2 = nullptr;
+  if (b->ev_hostL) cudaEventDestroy(b->ev_hostL);
+  b->ev_join2 = b->ev_hostL = nullptr;
   for (int k = 0; k < 2; k++) {
     if (b->ev_fork[k]) cudaEventDestroy(b->ev_fork[k]);
     if (b->ev_join[k]) cudaEventDestroy(b->ev_join[k]);

@@ -169,6 +169,14 @@ struct NormChunk {
 struct imsrg_op;
 
 namespace imsrg {
+// Host operands of one commutator (flat layout, nfull doubles each).
+struct HostIO {
+  const double *L, *R;
+  double *RES;
+};
+}  // namespace imsrg
+
+namespace imsrg {
 // Live kernel timing with CUDA events on the basis stream.
 struct Profiler {
   bool on = false;
@@ -206,6 +214,7 @@ struct imsrg_basis {
   // from and joined back into `stream` with events.
   cudaStream_t side = nullptr, side2 = nullptr;
   cudaEvent_t ev_fork[2] = {nullptr, nullptr}, ev_join[2] = {nullptr, nullptr}, ev_join2 = nullptr;
+  cudaEvent_t ev_hostL = nullptr;  // a host operand L has arrived (commutator_host)
   int device = 0;
   imsrg::Profiler prof;
   // commutator workspace
@@ -240,6 +249,7 @@ struct imsrg_basis {
     const double *L, *R;
     double *RES;
     int hL, hR, hRES, precision, with_e0;
+    imsrg::HostIO io;  // host operands copied in and out by the graph (all null if none)
     cudaGraphExec_t exec;
     long last_use;
     long nlaunch;  // library kernel launches in the sequence
@@ -344,9 +354,11 @@ struct ProfScope {
 int profile_collect(imsrg_basis *b);
 void profile_free(imsrg_basis *b);
 
-// one full commutator (api.cpp)
+// one full commutator (api.cpp); io != nullptr: L and R are first copied
+// from io->L, io->R (host) and RES is copied to io->RES afterwards, all on the
+// basis stream
 int commutator_dev(imsrg_basis *b, const double *L, int hL, const double *R, int hR, double *RES, int hRES,
-                   int precision, int with_e0);
+                   int precision, int with_e0, const HostIO *io = nullptr);
 
 }  // namespace imsrg
 

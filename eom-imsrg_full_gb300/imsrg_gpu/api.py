@@ -37,7 +37,7 @@ SYMBOLS = (
     "imsrg_gpu_magnus_decouple_graph", "imsrg_gpu_magnus_decouple_batch", "imsrg_gpu_magnus_decouple_tangent",
     "imsrg_gpu_split_schedule", "imsrg_gpu_split_schedule_set", "imsrg_gpu_build_gs_atan", "imsrg_gpu_build_gs_w2", "imsrg_gpu_magnus_decouple_gen",
     "imsrg_gpu_op_save", "imsrg_gpu_op_load", "imsrg_gpu_checkpoint_name", "imsrg_gpu_normal_order",
-    "imsrg_gpu_dhds", "imsrg_gpu_transform_bch", "imsrg_gpu_ode_decouple",
+    "imsrg_gpu_dhds", "imsrg_gpu_transform_bch", "imsrg_gpu_ode_decouple", "imsrg_gpu_commutator_host",
 )
 
 KERNELS = ("cc_forward", "gemm_fp64", "assemble_2body", "assemble_1body", "ozaki_slice", "ozaki_mma",
@@ -91,6 +91,7 @@ def lib():
             "imsrg_gpu_op_mbpt2": [vp, dp],
             "imsrg_gpu_op_get_e0": [vp, dp],
             "imsrg_gpu_commutator": [vp, vp, vp, i, i],
+            "imsrg_gpu_commutator_host": [vp, dp, i, dp, i, dp, i, i],
             "imsrg_gpu_build_gs_white": [vp, vp],
             "imsrg_gpu_magnus_expand": [vp, vp, i, ip],
             "imsrg_gpu_bch_expand": [vp, vp, vp, i, ip],
@@ -351,6 +352,17 @@ def mbpt2(H: Operator) -> float:
 def commutator(L: Operator, R: Operator, RES: Operator, precision: str = "fp64", with_e0: bool = True):
     """[L, R] -> RES (RES herm = -herm(L) herm(R)); asynchronous on the basis stream."""
     _check(lib().imsrg_gpu_commutator(L.handle, R.handle, RES.handle, PREC[precision], int(with_e0)), "commutator")
+
+
+def commutator_host(basis: Basis, L: np.ndarray, herm_L: int, R: np.ndarray, herm_R: int, RES: np.ndarray,
+                    precision: str = "fp64", with_e0: bool = True):
+    """[L, R] on host operands in the flat layout (RES written in place, herm
+    -herm_L herm_R): copies in, commutator, copy out, one call.  Pinned
+    (page-locked) buffers let the sequence replay as one CUDA graph."""
+    for a in (L, R, RES):
+        assert a.dtype == np.float64 and a.flags["C_CONTIGUOUS"] and a.size == basis.nfull
+    _check(lib().imsrg_gpu_commutator_host(basis.handle, _dp(L), int(herm_L), _dp(R), int(herm_R), _dp(RES),
+                                           PREC[precision], int(with_e0)), "commutator_host")
 
 
 def commutator_noalloc(basis: Basis, d_L: int, herm_L: int, d_R: int, herm_R: int, d_RES: int,

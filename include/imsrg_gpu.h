@@ -156,6 +156,15 @@ int imsrg_gpu_op_get_e0(const imsrg_op_t *op, double *e0);
  * RES E0 unchanged, as MAGNUS_EXPAND does (IMSRG_MAGNUS.f90:676-685).
  * RES must not alias L or R. */
 int imsrg_gpu_commutator(const imsrg_op_t *L, const imsrg_op_t *R, imsrg_op_t *RES, int precision, int with_e0);
+/* The same commutator on host operands in the flat layout (nfull doubles
+ * each; RES herm = -herm_L herm_R), for callers whose operators live in host
+ * memory as the reference's sq_op arrays do: L and R are copied in, the
+ * result copied back, and the call returns when RES is written.  The copies
+ * overlap the commutator where its order allows (the digit images of L start
+ * while R is in flight); from page-locked (pinned) buffers the whole sequence
+ * replays as one CUDA graph.  RES must not overlap L or R. */
+int imsrg_gpu_commutator_host(imsrg_basis_t *b, const double *L, int herm_L, const double *R, int herm_R,
+                              double *RES, int precision, int with_e0);
 
 /* build_gs_white (generators.f90:4-106): ETA (herm -1) from H.  ETA E0 is
  * left unchanged, as in the reference. */
