@@ -96,8 +96,8 @@ int dhds_dev(imsrg_basis *b, const double *HS, int hH, double *DH, int generator
 }
 
 // The launch sequence of one commutator.  Independent launches run on the
-// side stream, forked from and joined back into the basis stream with events,
-// so the call stays one ordered unit on that stream.
+// two side streams, forked from and joined back into the basis stream with
+// events, so the call stays one ordered unit on that stream.
 int commutator_launches(imsrg_basis *b, const double *L, int hL, const double *R, int hR, double *RES, int hRES,
                         int precision, int with_e0, const HostIO *io = nullptr) {
   // While kernel timing is on, every launch goes to the basis stream in the
@@ -105,7 +105,23 @@ int commutator_launches(imsrg_basis *b, const double *L, int hL, const double *R
   const bool serial = b->prof.on;
   cudaStream_t side = serial ? b->stream : b->side, side2 = serial ? b->stream : b->side2;
   const size_t bytes = (size_t)b->nfull * sizeof(double);
-  if (io) {  // host operands: L first, so the digit images of L start while R is in flight
+  const bool oz = precision == IMSRG_PREC_OZAKI;
+  // Page-locked host operands (outside profiling): R is copied first, so its
+  // digit images and its half of the Pandya transform run on side2 while L is
+  // in flight, and RES comes back by output range beside the two-body assembly.
+  const bool overlap = io && io->pinned && !serial;
+  // the transform also reduces the LCC/RCC block exponents (split precision)
+  int *cc_exps = nullptr, gL = 0, gR = 0;
+  if (overlap) {
+    if (oz) IMSRG_TRY(ozaki_cc_exponents(b, b->stream, &cc_exps, &gL, &gR));
+    IMSRG_CUDA_TRY(cudaMemcpyAsync(const_cast<double *>(R), io->R, bytes, cudaMemcpyHostToDevice, b->stream));
+    IMSRG_CUDA_TRY(cudaEventRecord(b->ev_hostR, b->stream));
+    IMSRG_CUDA_TRY(cudaMemcpyAsync(const_cast<double *>(L), io->L, bytes, cudaMemcpyHostToDevice, b->stream));
+    IMSRG_CUDA_TRY(cudaStreamWaitEvent(b->side2, b->ev_hostR, 0));
+    if (oz) IMSRG_TRY(ozaki_slice(b, L, R, 1, b->side2));
+    IMSRG_TRY(launch_cc_forward(b, L, hL, R, hR, cc_exps, gL, gR, 2, b->side2));
+    IMSRG_CUDA_TRY(cudaEventRecord(b->ev_join2, b->side2));
+  } else if (io) {  // pageable host operands: L first, so the digit images of L start while R is in flight
     IMSRG_CUDA_TRY(cudaMemcpyAsync(const_cast<double *>(L), io->L, bytes, cudaMemcpyHostToDevice, b->stream));
     IMSRG_CUDA_TRY(cudaEventRecord(b->ev_hostL, b->stream));
     IMSRG_CUDA_TRY(cudaMemcpyAsync(const_cast<double *>(R), io->R, bytes, cudaMemcpyHostToDevice, b->stream));
@@ -113,7 +129,7 @@ int commutator_launches(imsrg_basis *b, const double *L, int hL, const double *R
   auto fork = [&](int k) -> int {
     if (serial) return IMSRG_OK;
     IMSRG_CUDA_TRY(cudaEventRecord(b->ev_fork[k], b->stream));
-    IMSRG_CUDA_TRY(cudaStreamWaitEvent(b->side, (io && k == 0) ? b->ev_hostL : b->ev_fork[k], 0));
+    IMSRG_CUDA_TRY(cudaStreamWaitEvent(b->side, (io && !overlap && k == 0) ? b->ev_hostL : b->ev_fork[k], 0));
     return IMSRG_OK;
   };
   auto join = [&](int k) -> int {
@@ -122,15 +138,26 @@ int commutator_launches(imsrg_basis *b, const double *L, int hL, const double *R
     IMSRG_CUDA_TRY(cudaStreamWaitEvent(b->stream, b->ev_join[k], 0));
     return IMSRG_OK;
   };
-  if (precision == IMSRG_PREC_OZAKI) {
+  if (overlap) {  // R's half is under way on side2; L's half once L is in
+    IMSRG_TRY(fork(0));
+    if (oz) IMSRG_TRY(ozaki_slice(b, L, R, 0, side));
+    IMSRG_TRY(launch_cc_forward(b, L, hL, R, hR, cc_exps, gL, gR, 1));
+    IMSRG_CUDA_TRY(cudaStreamWaitEvent(b->stream, b->ev_join2, 0));
+    if (oz) {
+      IMSRG_TRY(ozaki_slice(b, L, R, 2, b->stream, cc_exps != nullptr));
+      IMSRG_TRY(join(0));
+      IMSRG_TRY(ozaki_mma(b, hL, hR));
+    } else {
+      IMSRG_TRY(join(0));
+      IMSRG_TRY(launch_gemm_fp64(b, L, hL, R, hR));
+    }
+  } else if (oz) {
     // digit images of L and of R on the two side streams, beside the Pandya
     // transform and the images of LCC and RCC
     IMSRG_TRY(fork(0));
     if (!serial) IMSRG_CUDA_TRY(cudaStreamWaitEvent(b->side2, b->ev_fork[0], 0));
     IMSRG_TRY(ozaki_slice(b, L, R, 0, side));
     IMSRG_TRY(ozaki_slice(b, L, R, 1, side2));
-    // the transform also reduces the LCC/RCC block exponents
-    int *cc_exps = nullptr, gL = 0, gR = 0;
     IMSRG_TRY(ozaki_cc_exponents(b, b->stream, &cc_exps, &gL, &gR));
     IMSRG_TRY(launch_cc_forward(b, L, hL, R, hR, cc_exps, gL, gR));
     IMSRG_TRY(ozaki_slice(b, L, R, 2, b->stream, cc_exps != nullptr));
@@ -148,6 +175,27 @@ int commutator_launches(imsrg_basis *b, const double *L, int hL, const double *R
   IMSRG_TRY(fork(1));
   IMSRG_TRY(launch_assemble_1body(b, L, hL, R, hR, RES, hRES, side));
   if (with_e0) IMSRG_TRY(launch_e0(b, L, hL, R, hR, RES, side));
+  if (overlap) {
+    // two-body elements by output range; each range's copy to the host runs on
+    // side2 beside the assembly of the next (see imsrg_basis::asm2_el)
+    IMSRG_TRY(launch_ph_inputs(b, hL, hR, precision));
+    for (int c = 0; c < kOutChunks; c++) {
+      IMSRG_TRY(launch_asm2_range(b, L, hL, R, hR, RES, hRES, b->asm2_el[c], b->asm2_el[c + 1], true));
+      IMSRG_CUDA_TRY(cudaEventRecord(b->ev_out[c], b->stream));
+      IMSRG_CUDA_TRY(cudaStreamWaitEvent(b->side2, b->ev_out[c], 0));
+      const long a0 = b->asm2_addr[c], a1 = b->asm2_addr[c + 1];
+      if (a1 > a0)
+        IMSRG_CUDA_TRY(cudaMemcpyAsync(io->RES + a0, RES + a0, (size_t)(a1 - a0) * sizeof(double),
+                                       cudaMemcpyDeviceToHost, b->side2));
+    }
+    IMSRG_TRY(join(1));
+    // E0 and the one-body part
+    IMSRG_CUDA_TRY(cudaMemcpyAsync(io->RES, RES, (size_t)b->asm2_addr[0] * sizeof(double), cudaMemcpyDeviceToHost,
+                                   b->stream));
+    IMSRG_CUDA_TRY(cudaEventRecord(b->ev_outj, b->side2));
+    IMSRG_CUDA_TRY(cudaStreamWaitEvent(b->stream, b->ev_outj, 0));
+    return IMSRG_OK;
+  }
   IMSRG_TRY(launch_assemble_2body(b, L, hL, R, hR, RES, hRES, precision));
   IMSRG_TRY(join(1));
   if (io) IMSRG_CUDA_TRY(cudaMemcpyAsync(io->RES, RES, bytes, cudaMemcpyDeviceToHost, b->stream));
@@ -177,6 +225,12 @@ int commutator_dev(imsrg_basis *b, const double *L, int hL, const double *R, int
         pinned = false;
       }
     }
+  HostIO hio{};
+  if (io) {
+    hio = *io;
+    hio.pinned = pinned;
+    io = &hio;
+  }
   const bool graphable = !b->prof.on && cs == cudaStreamCaptureStatusNone && pinned &&
                          (precision != IMSRG_PREC_OZAKI || ozaki_tuned(b));
   if (!graphable) return commutator_launches(b, L, hL, R, hR, RES, hRES, precision, with_e0, io);

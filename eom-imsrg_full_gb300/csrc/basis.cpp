@@ -361,6 +361,9 @@ int build_basis(imsrg_basis *b) {
     IMSRG_CUDA_TRY(cudaEventCreateWithFlags(&b->ev_fork[k], cudaEventDisableTiming));
     IMSRG_CUDA_TRY(cudaEventCreateWithFlags(&b->ev_join[k], cudaEventDisableTiming));
   }
+  IMSRG_CUDA_TRY(cudaEventCreateWithFlags(&b->ev_hostR, cudaEventDisableTiming));
+  IMSRG_CUDA_TRY(cudaEventCreateWithFlags(&b->ev_outj, cudaEventDisableTiming));
+  for (cudaEvent_t &ev : b->ev_out) IMSRG_CUDA_TRY(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
   DevTables &T = b->T;
   T.norb = N;
   T.A = A;
@@ -508,7 +511,9 @@ int build_basis(imsrg_basis *b) {
     std::vector<Asm2Head> heads;
     std::vector<PhTerm> zt;
     std::vector<unsigned long long> terms;
-    std::vector<std::pair<long, int>> items;  // (signature, head)
+    std::vector<std::pair<long, int>> items;      // (signature, head)
+    std::vector<std::pair<long, int>> items_out;  // (output range << 40 | signature, head)
+    const long two0 = b->off_fpp + (long)P * P;  // first two-body index of the flat layout
     auto row16 = [](int r) -> unsigned long long { return r < 0 ? 0xFFFFull : (unsigned long long)r; };
     for (unsigned long long key : qorder) {
       const std::vector<El> &els = qmap[key];
@@ -585,22 +590,42 @@ int build_basis(imsrg_basis *b) {
         h.meta = (unsigned)n122 | ((unsigned)n_in << 5) | ((unsigned)n_out << 10) | ((unsigned)valid << 15) |
                  ((unsigned)n2par << 16) | ((unsigned)nd << 18) | ((unsigned)(sq[g] && el.IX == el.JX) << 20) |
                  ((unsigned)sq[g] << 21) | ((unsigned)(g == 2) << 22);
-        // warps run elements of one loop-trip signature
+        // warps run elements of one loop-trip signature; in the order by
+        // output range, within the range of the element's lower write
+        const long lo = el.em >= 0 ? std::min(el.e, el.em) : el.e;
+        const long span = b->nfull - two0;
+        const long chunk = span > 0 ? std::min<long>((lo - two0) * kOutChunks / span, kOutChunks - 1) : 0;
         const long sig = (((long)n_in * 32 + n_out) * 32 + n122) * 2 + (valid ? 1 : 0);
         items.push_back({sig, (int)heads.size()});
+        items_out.push_back({chunk << 40 | sig, (int)heads.size()});
         heads.push_back(h);
       }
     }
     if (b->nfull >= (1L << 28) || b->off_fpp + (long)P * P >= (1L << 20)) return IMSRG_ERR_TOO_LARGE;
     for (int q1 = 0; q1 < b->ccblocks; q1++)
       if (b->cc_rlen[q1] >= 0xFFFF) return IMSRG_ERR_TOO_LARGE;
-    std::stable_sort(items.begin(), items.end(),
-                     [](const std::pair<long, int> &x, const std::pair<long, int> &y) { return x.first < y.first; });
-    std::vector<Asm2Head> ordered(heads.size());
-    for (size_t t = 0; t < items.size(); t++) ordered[t] = heads[items[t].second];
+    auto by_key = [](const std::pair<long, int> &x, const std::pair<long, int> &y) { return x.first < y.first; };
+    std::stable_sort(items.begin(), items.end(), by_key);
+    std::stable_sort(items_out.begin(), items_out.end(), by_key);
+    std::vector<Asm2Head> ordered(heads.size()), ordered_out(heads.size());
+    for (size_t t = 0; t < items.size(); t++) {
+      ordered[t] = heads[items[t].second];
+      ordered_out[t] = heads[items_out[t].second];
+    }
+    {
+      const long span = b->nfull - two0;
+      for (int c = 0; c <= kOutChunks; c++) {
+        b->asm2_addr[c] = two0 + ((long)c * span + kOutChunks - 1) / kOutChunks;
+        b->asm2_el[c] = std::lower_bound(items_out.begin(), items_out.end(), (long)c << 40,
+                                         [](const std::pair<long, int> &x, long key) { return x.first < key; }) -
+                        items_out.begin();
+      }
+      b->asm2_addr[kOutChunks] = b->nfull;
+    }
     T.n_asm2 = (int)ordered.size();
     T.n_ph = (int)zt.size();
     IMSRG_TRY(dev_upload(b, ordered, &T.asm2_head));
+    IMSRG_TRY(dev_upload(b, ordered_out, &T.asm2_head_out));
     IMSRG_TRY(dev_upload(b, terms, &T.asm2_terms));
     IMSRG_TRY(dev_upload(b, zt, &T.ph_terms));
 
@@ -846,7 +871,13 @@ void free_basis_device(imsrg_basis *b) {
   b->side = b->side2 = nullptr;
   if (b->ev_join2) cudaEventDestroy(b->ev_join2);
   if (b->ev_hostL) cudaEventDestroy(b->ev_hostL);
-  b->ev_join2 = b->ev_hostL = nullptr;
+  if (b->ev_hostR) cudaEventDestroy(b->ev_hostR);
+  if (b->ev_outj) cudaEventDestroy(b->ev_outj);
+  b->ev_join2 = b->ev_hostL = b->ev_hostR = b->ev_outj = nullptr;
+  for (cudaEvent_t &ev : b->ev_out) {
+    if (ev) cudaEventDestroy(ev);
+    ev = nullptr;
+  }
   for (int k = 0; k < 2; k++) {
     if (b->ev_fork[k]) cudaEventDestroy(b->ev_fork[k]);
     if (b->ev_join[k]) cudaEventDestroy(b->ev_join[k]);

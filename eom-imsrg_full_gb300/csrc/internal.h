@@ -53,8 +53,10 @@ struct DevTables {
   // element of the work order, its commutator_122 terms asm2_terms[head.start
   // ..]; the 222_ph recoupling inputs Z (one per orbit quadruple, channel and
   // J', shared by the quadruple's elements of every J) come from the ph_terms
-  // list (see Asm2Head, PhTerm).
-  const struct Asm2Head *asm2_head;
+  // list (see Asm2Head, PhTerm).  asm2_head_out holds the same heads grouped
+  // by output range first (imsrg_basis::asm2_el), for copies of RES to the
+  // host that run beside the assembly.
+  const struct Asm2Head *asm2_head, *asm2_head_out;
   const unsigned long long *asm2_terms;
   int n_asm2;
   const struct PhTerm *ph_terms;
@@ -169,11 +171,20 @@ struct NormChunk {
 struct imsrg_op;
 
 namespace imsrg {
-// Host operands of one commutator (flat layout, nfull doubles each).
+// Host operands of one commutator (flat layout, nfull doubles each).  pinned:
+// all three are page-locked, so copies may run asynchronously beside kernels.
 struct HostIO {
   const double *L, *R;
   double *RES;
+  bool pinned = false;
 };
+// The two-body part of RES is assembled, and copied back to a page-locked host
+// result, in this many address ranges, so that each range's copy runs beside
+// the assembly of the next.  Two: the assembly is latency-bound and needs
+// most of the GPU's warp slots, which a smaller range no longer fills (emax=6:
+// 284 us per host-operand commutator with two ranges, 287 with four, 322
+// with eight, 291 with one).
+constexpr int kOutChunks = 2;
 }  // namespace imsrg
 
 namespace imsrg {
@@ -215,6 +226,14 @@ struct imsrg_basis {
   cudaStream_t side = nullptr, side2 = nullptr;
   cudaEvent_t ev_fork[2] = {nullptr, nullptr}, ev_join[2] = {nullptr, nullptr}, ev_join2 = nullptr;
   cudaEvent_t ev_hostL = nullptr;  // a host operand L has arrived (commutator_host)
+  cudaEvent_t ev_hostR = nullptr;  // a host operand R has arrived
+  cudaEvent_t ev_out[imsrg::kOutChunks] = {}, ev_outj = nullptr;  // chunked copy of RES to the host
+  // Two-body work order by output range: elements asm2_el[c] .. asm2_el[c+1]
+  // write only RES[asm2_addr[c] ..) (the mirror of a square-array element
+  // lies at a lower address, so an element belongs to the range of its lower
+  // write); RES[asm2_addr[c] .. asm2_addr[c+1]) is final once every range up
+  // to c is assembled.
+  long asm2_el[imsrg::kOutChunks + 1] = {}, asm2_addr[imsrg::kOutChunks + 1] = {};
   int device = 0;
   imsrg::Profiler prof;
   // commutator workspace
@@ -277,12 +296,18 @@ inline int asm2_ctas(const imsrg_basis *b) { return (b->T.n_asm2 + ASM2_THREADS 
 
 // launchers (kernels_*.cu); all enqueue on b->stream and bump b->launches
 // Pandya transform into b->lcc, b->rcc; exps != nullptr: also the largest
-// exponent of each LCC block q1 into exps[gL + q1] and RCC block into exps[gR + q1]
+// exponent of each LCC block q1 into exps[gL + q1] and RCC block into exps[gR + q1];
+// sides 1 / 2 / 3: LCC only, RCC only, both; st = nullptr: the basis stream
 int launch_cc_forward(imsrg_basis *b, const double *L, int hL, const double *R, int hR, int *exps = nullptr,
-                      int gL = 0, int gR = 0);
+                      int gL = 0, int gR = 0, int sides = 3, cudaStream_t st = nullptr);
 int launch_gemm_fp64(imsrg_basis *b, const double *L, int hL, const double *R, int hR);
+// recoupling inputs of 222_ph, then the two-body elements of the work order
+// (all of them; or those in [w0, w1) of the order by output range)
 int launch_assemble_2body(imsrg_basis *b, const double *L, int hL, const double *R, int hR, double *RES, int hRES,
                           int precision);
+int launch_ph_inputs(imsrg_basis *b, int hL, int hR, int precision);
+int launch_asm2_range(imsrg_basis *b, const double *L, int hL, const double *R, int hR, double *RES, int hRES,
+                      long w0, long w1, bool by_range);
 int launch_assemble_1body(imsrg_basis *b, const double *L, int hL, const double *R, int hR, double *RES, int hRES,
                           cudaStream_t st);
 // E0 of [L, R] into RES[0] on stream st (independent of the assembly kernels)

@@ -33,6 +33,9 @@ namespace {
 // exponent of every LCC block (into exps[gL + block]) and RCC block (exps[gR +
 // block]) for the digit slicing: lanes of a warp that share a block combine
 // theirs, one integer atomicMax per block and warp (order-independent).
+// SIDES: 1 = LCC only, 2 = RCC only, 3 = both from one pass over the gather
+// list (the separate passes let the RCC half run while L is still arriving).
+template <int SIDES>
 __global__ void __launch_bounds__(256) k_cc_forward(DevTables T, const double *__restrict__ L, int hL,
                                                     const double *__restrict__ R, int hR, double *LCC, double *RCC,
                                                     int *exps, int gL, int gR) {
@@ -49,20 +52,24 @@ __global__ void __launch_bounds__(256) k_cc_forward(DevTables T, const double *_
       const int ix = T.cct_idx[k];
       const int tr = (int)((unsigned)ix >> 31), idx = ix & 0x7fffffff;
       const double c = T.cct_coef[k];
-      sl = fma(c, dflip(L[idx], tr & nL), sl);
-      sr = fma(c, dflip(R[idx], tr & nR), sr);
+      if (SIDES & 1) sl = fma(c, dflip(L[idx], tr & nL), sl);
+      if (SIDES & 2) sr = fma(c, dflip(R[idx], tr & nR), sr);
     }
-    LCC[e] = sl;
-    RCC[e] = sr;
-    xL = (int)((__double_as_longlong(sl) >> 52) & 0x7FF);
-    xR = (int)((__double_as_longlong(sr) >> 52) & 0x7FF);
+    if (SIDES & 1) {
+      LCC[e] = sl;
+      xL = (int)((__double_as_longlong(sl) >> 52) & 0x7FF);
+    }
+    if (SIDES & 2) {
+      RCC[e] = sr;
+      xR = (int)((__double_as_longlong(sr) >> 52) & 0x7FF);
+    }
   }
   if (exps) {  // every lane of the warp takes part (no early exit above)
     const unsigned peers = __match_any_sync(0xffffffffu, q1);
     const int mL = __reduce_max_sync(peers, xL), mR = __reduce_max_sync(peers, xR);
     if (q1 >= 0 && (int)(threadIdx.x & 31) == __ffs(peers) - 1) {
-      atomicMax(exps + gL + q1, mL);
-      atomicMax(exps + gR + q1, mR);
+      if (SIDES & 1) atomicMax(exps + gL + q1, mL);
+      if (SIDES & 2) atomicMax(exps + gR + q1, mR);
     }
   }
 }
@@ -284,19 +291,21 @@ __device__ __forceinline__ double sum122(const unsigned long long *tm, int n122,
 // Every two-body element of RES once (upper triangles of square arrays, the
 // mirror written alongside): the one-body insertions of commutator_122, the
 // antisymmetrised ladder epilogue of 222_pp_hh (:658-764) and the 222_ph
-// recoupling sum over J' of {6j} Z(J').  has220 (the allocation-free path):
-// each CTA leaves its commutator_220 partial in e0p for k_energy.
+// recoupling sum over J' of {6j} Z(J').  Thread t takes element w0 + t of the
+// work order `heads` while below w1.  has220 (the allocation-free path, w0 =
+// 0): each CTA leaves its commutator_220 partial in e0p for k_energy.
 __global__ void __launch_bounds__(ASM2_THREADS) k_assemble_2body(DevTables T, const double *__restrict__ L, int hL,
                                                                  const double *__restrict__ R, int hR,
                                                                  const double *__restrict__ W1,
                                                                  const double *__restrict__ W2,
                                                                  const double *__restrict__ Z, double *RES, int hRES,
+                                                                 const Asm2Head *__restrict__ heads, long w0, long w1,
                                                                  int has220, double *e0p) {
   __shared__ double sh220[ASM2_THREADS / 32];
-  const long w = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  const long w = w0 + (long)blockIdx.x * blockDim.x + threadIdx.x;
   double e220 = 0.0;  // this element's commutator_220 term (pphh arrays only)
-  if (w < T.n_asm2) {
-    const Asm2Head h = T.asm2_head[w];
+  if (w < w1) {
+    const Asm2Head h = heads[w];
     const unsigned long long *tm = T.asm2_terms + h.start;
     const unsigned meta = h.meta;
     const int nL = hL < 0, nR = hR < 0, nres = hRES < 0, npm = (hL * hR) < 0;
@@ -531,12 +540,19 @@ __global__ void __launch_bounds__(128) k_assemble_1body(DevTables T, const doubl
 
 }  // namespace
 
-int launch_cc_forward(imsrg_basis *b, const double *L, int hL, const double *R, int hR, int *exps, int gL, int gR) {
+int launch_cc_forward(imsrg_basis *b, const double *L, int hL, const double *R, int hR, int *exps, int gL, int gR,
+                      int sides, cudaStream_t st) {
   long n = b->cc_total;
   if (n == 0) return IMSRG_OK;
-  ProfScope ps(b, IMSRG_KERNEL_CC_FORWARD);
-  k_cc_forward<<<(unsigned)((n + 255) / 256), 256, 0, b->stream>>>(b->T, L, hL, R, hR, b->lcc, b->rcc, exps, gL,
-                                                                   gR);
+  if (!st) st = b->stream;
+  ProfScope ps(b, IMSRG_KERNEL_CC_FORWARD, st);
+  const unsigned grid = (unsigned)((n + 255) / 256);
+  if (sides == 1)
+    k_cc_forward<1><<<grid, 256, 0, st>>>(b->T, L, hL, R, hR, b->lcc, b->rcc, exps, gL, gR);
+  else if (sides == 2)
+    k_cc_forward<2><<<grid, 256, 0, st>>>(b->T, L, hL, R, hR, b->lcc, b->rcc, exps, gL, gR);
+  else
+    k_cc_forward<3><<<grid, 256, 0, st>>>(b->T, L, hL, R, hR, b->lcc, b->rcc, exps, gL, gR);
   b->launches++;
   return cuda_status(cudaGetLastError());
 }
@@ -560,9 +576,7 @@ int launch_gemm_fp64(imsrg_basis *b, const double *L, int hL, const double *R, i
   return cuda_status(cudaGetLastError());
 }
 
-int launch_assemble_2body(imsrg_basis *b, const double *L, int hL, const double *R, int hR, double *RES, int hRES,
-                          int precision) {
-  ProfScope ps(b, IMSRG_KERNEL_ASSEMBLE_2BODY);
+int launch_ph_inputs(imsrg_basis *b, int hL, int hR, int precision) {
   const int *exps = nullptr;
   const int2 *ccg = nullptr;
   if (precision == IMSRG_PREC_OZAKI) IMSRG_TRY(ozaki_wcc_scale(b, &exps, &ccg));
@@ -571,13 +585,26 @@ int launch_assemble_2body(imsrg_basis *b, const double *L, int hL, const double 
                                                                             b->zph);
     b->launches++;
   }
-  const long n = b->T.n_asm2;
+  return cuda_status(cudaGetLastError());
+}
+
+int launch_asm2_range(imsrg_basis *b, const double *L, int hL, const double *R, int hR, double *RES, int hRES,
+                      long w0, long w1, bool by_range) {
+  const long n = w1 - w0;
   if (n > 0) {
     k_assemble_2body<<<(unsigned)((n + ASM2_THREADS - 1) / ASM2_THREADS), ASM2_THREADS, 0, b->stream>>>(
-        b->T, L, hL, R, hR, b->w1, b->w2, b->zph, RES, hRES, 0, nullptr);
+        b->T, L, hL, R, hR, b->w1, b->w2, b->zph, RES, hRES, by_range ? b->T.asm2_head_out : b->T.asm2_head, w0,
+        w1, 0, nullptr);
     b->launches++;
   }
   return cuda_status(cudaGetLastError());
+}
+
+int launch_assemble_2body(imsrg_basis *b, const double *L, int hL, const double *R, int hR, double *RES, int hRES,
+                          int precision) {
+  ProfScope ps(b, IMSRG_KERNEL_ASSEMBLE_2BODY);
+  IMSRG_TRY(launch_ph_inputs(b, hL, hR, precision));
+  return launch_asm2_range(b, L, hL, R, hR, RES, hRES, 0, b->T.n_asm2, false);
 }
 
 int launch_e0(imsrg_basis *b, const double *L, int hL, const double *R, int hR, double *RES, cudaStream_t st) {
@@ -605,8 +632,8 @@ int launch_commutator_fp64_ws(imsrg_basis *b, const Workspace &ws, const double 
                               double *RES, int hRES, int with_e0, cudaStream_t st) {
   long ncc = b->cc_total;
   if (ncc > 0) {
-    k_cc_forward<<<(unsigned)((ncc + 255) / 256), 256, 0, st>>>(b->T, L, hL, R, hR, ws.lcc, ws.rcc, nullptr, 0,
-                                                                 0);
+    k_cc_forward<3><<<(unsigned)((ncc + 255) / 256), 256, 0, st>>>(b->T, L, hL, R, hR, ws.lcc, ws.rcc, nullptr, 0,
+                                                                    0);
     b->launches++;
   }
   if (b->ntiles > 0) {
@@ -633,7 +660,7 @@ int launch_commutator_fp64_ws(imsrg_basis *b, const Workspace &ws, const double 
   if (n2 > 0) {
     const int has220 = with_e0 && hL * hR == -1;
     k_assemble_2body<<<(unsigned)((n2 + ASM2_THREADS - 1) / ASM2_THREADS), ASM2_THREADS, 0, st>>>(
-        b->T, L, hL, R, hR, ws.w1, ws.w2, ws.zph, RES, hRES, has220, ws.e0p);
+        b->T, L, hL, R, hR, ws.w1, ws.w2, ws.zph, RES, hRES, b->T.asm2_head, 0, n2, has220, ws.e0p);
     b->launches++;
   }
   const int grid1 = b->T.n_asm1_heavy + (b->T.n_asm1_light + 3) / 4;

@@ -91,7 +91,7 @@ def lib():
             "imsrg_gpu_op_mbpt2": [vp, dp],
             "imsrg_gpu_op_get_e0": [vp, dp],
             "imsrg_gpu_commutator": [vp, vp, vp, i, i],
-            "imsrg_gpu_commutator_host": [vp, dp, i, dp, i, dp, i, i],
+            "imsrg_gpu_commutator_host": [vp, vp, i, vp, i, vp, i, i],
             "imsrg_gpu_build_gs_white": [vp, vp],
             "imsrg_gpu_magnus_expand": [vp, vp, i, ip],
             "imsrg_gpu_bch_expand": [vp, vp, vp, i, ip],
@@ -143,6 +143,15 @@ def _check(status: int, where: str):
 def _dp(a: np.ndarray):
     assert a.dtype == np.float64 and a.flags["C_CONTIGUOUS"]
     return a.ctypes.data_as(C.POINTER(C.c_double))
+
+
+_F64 = np.dtype(np.float64)
+
+
+def _addr(a: np.ndarray) -> int:
+    """Address of an array's data for a void* argument (the cheapest route
+    for writable arrays, whose buffer ctypes can wrap directly)."""
+    return C.addressof(C.c_char.from_buffer(a)) if a.flags.writeable else a.ctypes.data
 
 
 class Basis:
@@ -359,9 +368,11 @@ def commutator_host(basis: Basis, L: np.ndarray, herm_L: int, R: np.ndarray, her
     """[L, R] on host operands in the flat layout (RES written in place, herm
     -herm_L herm_R): copies in, commutator, copy out, one call.  Pinned
     (page-locked) buffers let the sequence replay as one CUDA graph."""
+    n = basis.nfull
     for a in (L, R, RES):
-        assert a.dtype == np.float64 and a.flags["C_CONTIGUOUS"] and a.size == basis.nfull
-    _check(lib().imsrg_gpu_commutator_host(basis.handle, _dp(L), int(herm_L), _dp(R), int(herm_R), _dp(RES),
+        if a.dtype != _F64 or not a.flags.c_contiguous or a.size != n:
+            raise ValueError(f"commutator_host: operands must be C-contiguous float64 arrays of {n} elements")
+    _check(lib().imsrg_gpu_commutator_host(basis.handle, _addr(L), int(herm_L), _addr(R), int(herm_R), _addr(RES),
                                            PREC[precision], int(with_e0)), "commutator_host")
 
 

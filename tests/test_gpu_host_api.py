@@ -40,9 +40,34 @@ def test_host_commutator_equals_device_commutator(gpu_lib, precision, pinned):
             assert np.array_equal(hr, ref)
 
 
+@pytest.mark.parametrize("precision", ["fp64", "ozaki"])
+def test_host_commutator_emax6_every_element_returned(gpu_lib, precision):
+    """At emax=6 the result comes back in several address ranges beside the
+    assembly; every element (the host buffer starts as NaN) must equal the
+    device-operand commutator, with the operands' Hermiticity either way."""
+    from imsrg_gpu.synth import synth_hamiltonian, synth_omega
+    bas, lay = make_case(6)
+    B = gpu_lib.Basis.from_dict(bas)
+    Hh, Oh = synth_hamiltonian(lay, 3), synth_omega(lay, 3)
+    (ho, to), (hh, th), (hr, tr) = _pinned(Oh), _pinned(Hh), _pinned(np.zeros(lay.nfull))
+    omega, ham = (-1, Oh, ho), (1, Hh, hh)
+    for (hL, XL, pL), (hR, XR, pR) in ((omega, ham), (ham, omega)):
+        L, R, RES = gpu_lib.Operator(B, hL, XL), gpu_lib.Operator(B, hR, XR), gpu_lib.Operator(B, 1)
+        gpu_lib.commutator(L, R, RES, precision=precision)
+        ref = RES.download()
+        for _ in range(2):
+            hr[:] = np.nan
+            gpu_lib.commutator_host(B, pL, hL, pR, hR, hr, precision=precision)
+            assert np.array_equal(hr, ref)
+
+
 def test_host_commutator_rejects_aliased_result(gpu_lib):
     bas, lay = make_case(2)
     B = gpu_lib.Basis.from_dict(bas)
     a, r = np.zeros(lay.nfull), np.zeros(lay.nfull)
     with pytest.raises(gpu_lib.ImsrgError):
         gpu_lib.commutator_host(B, a, -1, r, 1, r)
+    # wrong length, dtype or a strided view are refused before the call
+    for bad in (a[:-1], a.astype(np.float32), np.zeros(2 * lay.nfull)[::2]):
+        with pytest.raises(ValueError):
+            gpu_lib.commutator_host(B, bad, -1, a, 1, np.zeros(lay.nfull))
