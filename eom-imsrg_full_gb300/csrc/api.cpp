@@ -138,6 +138,24 @@ int commutator_launches(imsrg_basis *b, const double *L, int hL, const double *R
     IMSRG_CUDA_TRY(cudaStreamWaitEvent(b->stream, b->ev_join[k], 0));
     return IMSRG_OK;
   };
+  // E0 needs only L and R: its single CTA runs on side3 from here, beside the
+  // Pandya transform and the slicing, and is joined at the end (after the
+  // one-body assembly, where it ran before, it finished last: the one-body
+  // kernel runs slowly beside the 3,769 CTAs of the two-body assembly)
+  if (with_e0) {
+    if (serial) {
+      IMSRG_TRY(launch_e0(b, L, hL, R, hR, RES, b->stream));
+    } else {
+      IMSRG_CUDA_TRY(cudaEventRecord(b->ev_fork[0], b->stream));
+      IMSRG_CUDA_TRY(cudaStreamWaitEvent(b->side3, b->ev_fork[0], 0));
+      IMSRG_TRY(launch_e0(b, L, hL, R, hR, RES, b->side3));
+      IMSRG_CUDA_TRY(cudaEventRecord(b->ev_join3, b->side3));
+    }
+  }
+  auto join_e0 = [&]() -> int {
+    if (with_e0 && !serial) IMSRG_CUDA_TRY(cudaStreamWaitEvent(b->stream, b->ev_join3, 0));
+    return IMSRG_OK;
+  };
   if (overlap) {  // R's half is under way on side2; L's half once L is in
     IMSRG_TRY(fork(0));
     if (oz) IMSRG_TRY(ozaki_slice(b, L, R, 0, side));
@@ -171,14 +189,18 @@ int commutator_launches(imsrg_basis *b, const double *L, int hL, const double *R
     IMSRG_TRY(launch_cc_forward(b, L, hL, R, hR));
     IMSRG_TRY(launch_gemm_fp64(b, L, hL, R, hR));
   }
-  // one-body assembly and E0 beside the two-body assembly
+  // one-body assembly beside the two-body assembly, after the packed (L, R)
+  // pairs of the 122 gathers, which are built beside the recoupling inputs
+  // (earlier, beside the Pandya transform, they slowed it)
   IMSRG_TRY(fork(1));
+  IMSRG_TRY(launch_lr_pack(b, L, R, side));
+  if (!serial) IMSRG_CUDA_TRY(cudaEventRecord(b->ev_lr, side));
   IMSRG_TRY(launch_assemble_1body(b, L, hL, R, hR, RES, hRES, side));
-  if (with_e0) IMSRG_TRY(launch_e0(b, L, hL, R, hR, RES, side));
   if (overlap) {
     // two-body elements by output range; each range's copy to the host runs on
     // side2 beside the assembly of the next (see imsrg_basis::asm2_el)
     IMSRG_TRY(launch_ph_inputs(b, hL, hR, precision));
+    IMSRG_CUDA_TRY(cudaStreamWaitEvent(b->stream, b->ev_lr, 0));
     for (int c = 0; c < kOutChunks; c++) {
       IMSRG_TRY(launch_asm2_range(b, L, hL, R, hR, RES, hRES, b->asm2_el[c], b->asm2_el[c + 1], true));
       IMSRG_CUDA_TRY(cudaEventRecord(b->ev_out[c], b->stream));
@@ -189,6 +211,7 @@ int commutator_launches(imsrg_basis *b, const double *L, int hL, const double *R
                                        cudaMemcpyDeviceToHost, b->side2));
     }
     IMSRG_TRY(join(1));
+    IMSRG_TRY(join_e0());
     // E0 and the one-body part
     IMSRG_CUDA_TRY(cudaMemcpyAsync(io->RES, RES, (size_t)b->asm2_addr[0] * sizeof(double), cudaMemcpyDeviceToHost,
                                    b->stream));
@@ -196,8 +219,14 @@ int commutator_launches(imsrg_basis *b, const double *L, int hL, const double *R
     IMSRG_CUDA_TRY(cudaStreamWaitEvent(b->stream, b->ev_outj, 0));
     return IMSRG_OK;
   }
-  IMSRG_TRY(launch_assemble_2body(b, L, hL, R, hR, RES, hRES, precision));
+  {
+    ProfScope ps(b, IMSRG_KERNEL_ASSEMBLE_2BODY);
+    IMSRG_TRY(launch_ph_inputs(b, hL, hR, precision));
+    if (!serial) IMSRG_CUDA_TRY(cudaStreamWaitEvent(b->stream, b->ev_lr, 0));
+    IMSRG_TRY(launch_asm2_range(b, L, hL, R, hR, RES, hRES, 0, b->T.n_asm2, false));
+  }
   IMSRG_TRY(join(1));
+  IMSRG_TRY(join_e0());
   if (io) IMSRG_CUDA_TRY(cudaMemcpyAsync(io->RES, RES, bytes, cudaMemcpyDeviceToHost, b->stream));
   return IMSRG_OK;
 }

@@ -355,6 +355,8 @@ int build_basis(imsrg_basis *b) {
   b->stream = b->own_stream;
   IMSRG_CUDA_TRY(cudaStreamCreateWithFlags(&b->side, cudaStreamNonBlocking));
   IMSRG_CUDA_TRY(cudaStreamCreateWithFlags(&b->side2, cudaStreamNonBlocking));
+  IMSRG_CUDA_TRY(cudaStreamCreateWithFlags(&b->side3, cudaStreamNonBlocking));
+  IMSRG_CUDA_TRY(cudaEventCreateWithFlags(&b->ev_join3, cudaEventDisableTiming));
   IMSRG_CUDA_TRY(cudaEventCreateWithFlags(&b->ev_join2, cudaEventDisableTiming));
   IMSRG_CUDA_TRY(cudaEventCreateWithFlags(&b->ev_hostL, cudaEventDisableTiming));
   for (int k = 0; k < 2; k++) {
@@ -362,6 +364,7 @@ int build_basis(imsrg_basis *b) {
     IMSRG_CUDA_TRY(cudaEventCreateWithFlags(&b->ev_join[k], cudaEventDisableTiming));
   }
   IMSRG_CUDA_TRY(cudaEventCreateWithFlags(&b->ev_hostR, cudaEventDisableTiming));
+  IMSRG_CUDA_TRY(cudaEventCreateWithFlags(&b->ev_lr, cudaEventDisableTiming));
   IMSRG_CUDA_TRY(cudaEventCreateWithFlags(&b->ev_outj, cudaEventDisableTiming));
   for (cudaEvent_t &ev : b->ev_out) IMSRG_CUDA_TRY(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
   DevTables &T = b->T;
@@ -489,6 +492,19 @@ int build_basis(imsrg_basis *b) {
     };
     std::map<unsigned long long, std::vector<El>> qmap;
     std::vector<unsigned long long> qorder;  // quadruples in first-seen order
+    // sqrt(2) factors of every stored element (all of each array: a term may
+    // read the lower triangle of a square one)
+    std::vector<unsigned char> vsq(b->nfull, 0);
+    for (int qb = 0; qb < b->nblocks; qb++)
+      for (int g = 0; g < 6; g++) {
+        const int n1 = b->gam_n1[qb * 6 + g], n2 = b->gam_n2[qb * 6 + g];
+        const std::vector<int> &qr = b->qn[qb * 3 + c1tab[g]], &qc = b->qn[qb * 3 + c2tab[g]];
+        for (int JX = 0; JX < n2; JX++)
+          for (int IX = 0; IX < n1; IX++)
+            vsq[b->gam_off[qb * 6 + g] + IX + (long)JX * n1] =
+                (unsigned char)((qr[2 * IX] == qr[2 * IX + 1]) + (qc[2 * JX] == qc[2 * JX + 1]));
+      }
+    bool vsq_ok = true;  // every commutator_122 term's factor is its element's
     for (int qb = 0; qb < b->nblocks; qb++)
       for (int g = 0; g < 6; g++) {
         const int n1 = b->gam_n1[qb * 6 + g], n2 = b->gam_n2[qb * 6 + g];
@@ -562,6 +578,7 @@ int build_basis(imsrg_basis *b) {
         // commutator_122: one-body insertions on the four legs
         auto add122 = [&](int leg_sign, int fa, int fb, const HLoc &v) {
           if (v.idx < 0) return;
+          if (v.nsq != vsq[v.idx]) vsq_ok = false;
           int ftr;
           long fi = floc(fa, fb, &ftr);
           terms.push_back((unsigned long long)v.idx | ((unsigned long long)fi << 28) |
@@ -601,6 +618,8 @@ int build_basis(imsrg_basis *b) {
         heads.push_back(h);
       }
     }
+    if (!vsq_ok) return IMSRG_ERR_INVALID;
+    b->off_2b = two0;
     if (b->nfull >= (1L << 28) || b->off_fpp + (long)P * P >= (1L << 20)) return IMSRG_ERR_TOO_LARGE;
     for (int q1 = 0; q1 < b->ccblocks; q1++)
       if (b->cc_rlen[q1] >= 0xFFFF) return IMSRG_ERR_TOO_LARGE;
@@ -628,6 +647,7 @@ int build_basis(imsrg_basis *b) {
     IMSRG_TRY(dev_upload(b, ordered_out, &T.asm2_head_out));
     IMSRG_TRY(dev_upload(b, terms, &T.asm2_terms));
     IMSRG_TRY(dev_upload(b, zt, &T.ph_terms));
+    IMSRG_TRY(dev_upload(b, vsq, &T.vsq));
 
     std::vector<std::pair<long, int>> cit;
     T.ccf_packed = b->cc_total < (1L << 24) && b->ccblocks <= 128;
@@ -837,6 +857,8 @@ int build_basis(imsrg_basis *b) {
   b->wcc = (double *)p;
   IMSRG_TRY(dev_alloc(b, (size_t)T.n_ph * sizeof(double), &p));
   b->zph = (double *)p;
+  IMSRG_TRY(dev_alloc(b, b->nfull * sizeof(double2), &p));
+  b->lr = (double2 *)p;
   IMSRG_TRY(dev_alloc(b, (size_t)2 * N * N * sizeof(double), &p));  // monopoles of H and of a tangent dH
   b->mono = (double *)p;
   IMSRG_TRY(dev_alloc(b, 64 * sizeof(double), &p));
@@ -868,12 +890,16 @@ void free_basis_device(imsrg_basis *b) {
   b->stream = b->own_stream = nullptr;
   if (b->side) cudaStreamDestroy(b->side);
   if (b->side2) cudaStreamDestroy(b->side2);
-  b->side = b->side2 = nullptr;
+  if (b->side3) cudaStreamDestroy(b->side3);
+  b->side = b->side2 = b->side3 = nullptr;
+  if (b->ev_join3) cudaEventDestroy(b->ev_join3);
+  b->ev_join3 = nullptr;
   if (b->ev_join2) cudaEventDestroy(b->ev_join2);
   if (b->ev_hostL) cudaEventDestroy(b->ev_hostL);
   if (b->ev_hostR) cudaEventDestroy(b->ev_hostR);
+  if (b->ev_lr) cudaEventDestroy(b->ev_lr);
   if (b->ev_outj) cudaEventDestroy(b->ev_outj);
-  b->ev_join2 = b->ev_hostL = b->ev_hostR = b->ev_outj = nullptr;
+  b->ev_join2 = b->ev_hostL = b->ev_hostR = b->ev_lr = b->ev_outj = nullptr;
   for (cudaEvent_t &ev : b->ev_out) {
     if (ev) cudaEventDestroy(ev);
     ev = nullptr;

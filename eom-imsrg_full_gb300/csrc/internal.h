@@ -57,6 +57,10 @@ struct DevTables {
   // by output range first (imsrg_basis::asm2_el), for copies of RES to the
   // host that run beside the assembly.
   const struct Asm2Head *asm2_head, *asm2_head_out;
+  // [flat index] number of sqrt(2) normalisation factors v_elem applies to a
+  // stored two-body element (identical-orbit row pair + identical-orbit
+  // column pair: 0, 1 or 2)
+  const unsigned char *vsq;
   const unsigned long long *asm2_terms;
   int n_asm2;
   const struct PhTerm *ph_terms;
@@ -223,10 +227,13 @@ struct imsrg_basis {
   cudaStream_t own_stream = nullptr;  // the library's own stream
   // Library streams for independent launches inside one commutator, forked
   // from and joined back into `stream` with events.
-  cudaStream_t side = nullptr, side2 = nullptr;
+  // side3 runs E0 (one CTA) from the first fork to the end.
+  cudaStream_t side = nullptr, side2 = nullptr, side3 = nullptr;
   cudaEvent_t ev_fork[2] = {nullptr, nullptr}, ev_join[2] = {nullptr, nullptr}, ev_join2 = nullptr;
+  cudaEvent_t ev_join3 = nullptr;
   cudaEvent_t ev_hostL = nullptr;  // a host operand L has arrived (commutator_host)
   cudaEvent_t ev_hostR = nullptr;  // a host operand R has arrived
+  cudaEvent_t ev_lr = nullptr;     // the packed (L, R) pairs are built
   cudaEvent_t ev_out[imsrg::kOutChunks] = {}, ev_outj = nullptr;  // chunked copy of RES to the host
   // Two-body work order by output range: elements asm2_el[c] .. asm2_el[c+1]
   // write only RES[asm2_addr[c] ..) (the mirror of a square-array element
@@ -239,6 +246,11 @@ struct imsrg_basis {
   // commutator workspace
   double *w1 = nullptr, *w2 = nullptr, *lcc = nullptr, *rcc = nullptr, *wcc = nullptr;
   double *zph = nullptr;        // 222_ph recoupling inputs (T.n_ph)
+  // [flat index] (c L, c R) of the commutator's operands with c the element's
+  // sqrt(2)^vsq factor as v_elem applies it: one 16-byte gather per
+  // commutator_122 term instead of two (two-body indices only)
+  double2 *lr = nullptr;
+  long off_2b = 0;              // first two-body index of the flat layout
   double *mono = nullptr;       // 2 x norb x norb monopole tables of the White generator (H, tangent dH)
   double *scal = nullptr;       // small device scratch for reductions (E0, norms)
   double *partials = nullptr;   // norm/mbpt2 partial sums
@@ -301,11 +313,12 @@ inline int asm2_ctas(const imsrg_basis *b) { return (b->T.n_asm2 + ASM2_THREADS 
 int launch_cc_forward(imsrg_basis *b, const double *L, int hL, const double *R, int hR, int *exps = nullptr,
                       int gL = 0, int gR = 0, int sides = 3, cudaStream_t st = nullptr);
 int launch_gemm_fp64(imsrg_basis *b, const double *L, int hL, const double *R, int hR);
-// recoupling inputs of 222_ph, then the two-body elements of the work order
-// (all of them; or those in [w0, w1) of the order by output range)
-int launch_assemble_2body(imsrg_basis *b, const double *L, int hL, const double *R, int hR, double *RES, int hRES,
-                          int precision);
+// the two-body assembly: the recoupling inputs of 222_ph, then the elements
+// [w0, w1) of the signature work order or of the order by output range
+// (which read b->lr, see launch_lr_pack)
 int launch_ph_inputs(imsrg_basis *b, int hL, int hR, int precision);
+// b->lr from L and R on stream st (before the two-body assembly)
+int launch_lr_pack(imsrg_basis *b, const double *L, const double *R, cudaStream_t st);
 int launch_asm2_range(imsrg_basis *b, const double *L, int hL, const double *R, int hR, double *RES, int hRES,
                       long w0, long w1, bool by_range);
 int launch_assemble_1body(imsrg_basis *b, const double *L, int hL, const double *R, int hR, double *RES, int hRES,
