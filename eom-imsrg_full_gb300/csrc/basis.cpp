@@ -117,6 +117,48 @@ GemmTerm term(int a, long aoff, int lda, int ta, int bsrc, long boff, int ldb, i
 
 }  // namespace
 
+double sixj(int a, int b, int c, int d, int e, int f) {
+  static const SixJ sj;
+  return sj(a, b, c, d, e, f);
+}
+
+// Host restatement of the element location of v_elem (basic_IMSRG.f90:
+// 1270-1385): the stored element that <a bb|V|c d>_J reads, with the
+// pair-reordering phase, the sqrt(2) factors of identical-orbit pairs and
+// whether it is read transposed (times herm).
+HLoc v_location(const imsrg_basis *b, int a, int bb, int c, int d, int J2) {
+  const int N = b->norb, nJ = b->jtm + 1;
+  HLoc r{-1, 0, 0, 0};
+  if (!(tri(b->jj[a], b->jj[bb], J2) && tri(b->jj[c], b->jj[d], J2))) return r;
+  int Pp = (b->ll[a] + b->ll[bb]) & 1;
+  if (((b->ll[c] + b->ll[d]) & 1) != Pp) return r;
+  int tz2 = b->itzp[a] + b->itzp[bb];
+  if (b->itzp[c] + b->itzp[d] != tz2) return r;
+  int qq = 3 * J2 + 2 * (tz2 / 2 + 1) + Pp;
+  int C1 = b->con[a] + b->con[bb] + 1, C2 = b->con[c] + b->con[d] + 1;
+  int qx = C1 * C2;
+  if (qx == 9) qx = 5;
+  int i1, i2;
+  if (a > bb) {
+    i1 = b->pairrow[((size_t)bb * N + a) * nJ + J2 / 2];
+    r.neg = (1 + (b->jj[a] + b->jj[bb] - J2) / 2) & 1;
+  } else {
+    r.nsq += (a == bb);
+    i1 = b->pairrow[((size_t)a * N + bb) * nJ + J2 / 2];
+  }
+  if (c > d) {
+    i2 = b->pairrow[((size_t)d * N + c) * nJ + J2 / 2];
+    r.neg ^= (1 + (b->jj[c] + b->jj[d] - J2) / 2) & 1;
+  } else {
+    r.nsq += (c == d);
+    i2 = b->pairrow[((size_t)c * N + d) * nJ + J2 / 2];
+  }
+  int sg = qq * 6 + qx - 1;
+  r.trans = C1 > C2;
+  r.idx = r.trans ? b->gam_off[sg] + i2 + (long)i1 * b->gam_n1[sg] : b->gam_off[sg] + i1 + (long)i2 * b->gam_n1[sg];
+  return r;
+}
+
 int build_basis(imsrg_basis *b) {
   const int N = b->norb;
   // holes / particles (find_holes, basic_IMSRG.f90:380-398)
@@ -147,7 +189,8 @@ int build_basis(imsrg_basis *b) {
   b->gam_off.assign(b->nblocks * 6, 0);
   b->gam_n1.assign(b->nblocks * 6, 0);
   b->gam_n2.assign(b->nblocks * 6, 0);
-  std::vector<int> pairrow((size_t)N * N * nJ, -1);
+  b->pairrow.assign((size_t)N * N * nJ, -1);
+  std::vector<int> &pairrow = b->pairrow;
   std::vector<int> blk_J2(b->nblocks);
   b->off_fhh = 1;
   b->off_fph = 1 + (long)A * A;
@@ -421,46 +464,9 @@ int build_basis(imsrg_basis *b) {
   IMSRG_TRY(dev_upload(b, cc_colstart, &T.cc_colstart));
   IMSRG_TRY(dev_upload(b, ph_pairs, &T.ph_pairs));
 
-  // --- host restatement of the element locations of v_elem
-  // (basic_IMSRG.f90:1270-1385) and f_elem (:1147-1177), shared by every
-  // gather list below
-  struct HLoc {
-    long idx;   // flat index, -1 if structurally zero
-    int neg;    // pair-reordering phase
-    int nsq;    // sqrt(2) normalisation factors
-    int trans;  // read transposed (times herm)
-  };
-  auto vloc = [&](int a, int bb, int c, int d, int J2) {
-    HLoc r{-1, 0, 0, 0};
-    if (!(tri(b->jj[a], b->jj[bb], J2) && tri(b->jj[c], b->jj[d], J2))) return r;
-    int Pp = (b->ll[a] + b->ll[bb]) & 1;
-    if (((b->ll[c] + b->ll[d]) & 1) != Pp) return r;
-    int tz2 = b->itzp[a] + b->itzp[bb];
-    if (b->itzp[c] + b->itzp[d] != tz2) return r;
-    int qq = 3 * J2 + 2 * (tz2 / 2 + 1) + Pp;
-    int C1 = b->con[a] + b->con[bb] + 1, C2 = b->con[c] + b->con[d] + 1;
-    int qx = C1 * C2;
-    if (qx == 9) qx = 5;
-    int i1, i2;
-    if (a > bb) {
-      i1 = pairrow[((size_t)bb * N + a) * nJ + J2 / 2];
-      r.neg = (1 + (b->jj[a] + b->jj[bb] - J2) / 2) & 1;
-    } else {
-      r.nsq += (a == bb);
-      i1 = pairrow[((size_t)a * N + bb) * nJ + J2 / 2];
-    }
-    if (c > d) {
-      i2 = pairrow[((size_t)d * N + c) * nJ + J2 / 2];
-      r.neg ^= (1 + (b->jj[c] + b->jj[d] - J2) / 2) & 1;
-    } else {
-      r.nsq += (c == d);
-      i2 = pairrow[((size_t)c * N + d) * nJ + J2 / 2];
-    }
-    int sg = qq * 6 + qx - 1;
-    r.trans = C1 > C2;
-    r.idx = r.trans ? b->gam_off[sg] + i2 + (long)i1 * b->gam_n1[sg] : b->gam_off[sg] + i1 + (long)i2 * b->gam_n1[sg];
-    return r;
-  };
+  // --- element locations of v_elem (v_location) and f_elem (:1147-1177),
+  // shared by every gather list below
+  auto vloc = [&](int a, int bb, int c, int d, int J2) { return v_location(b, a, bb, c, d, J2); };
   // f_elem: flat index and whether the element is read transposed (a ph
   // element asked as hp takes the operator's herm)
   auto floc = [&](int a, int bb, int *trans) -> long {

@@ -216,6 +216,7 @@ struct imsrg_basis {
   std::vector<int> gam_n1, gam_n2;
   std::vector<std::vector<int>> qn;  // [q*3+c] pair list (0-based, 2 ints per pair)
   std::vector<int> cc_rlen, cc_nph, cc_J2;
+  std::vector<int> pairrow;          // [(a * norb + b) * (jtm + 1) + J2 / 2] row of pair a <= b in its block
   std::vector<long> cc_off, wcc_off;
   long nfull = 0, neq = 0, cc_total = 0, wcc_total = 0;
   long off_fhh = 1, off_fph = 0, off_fpp = 0;
@@ -298,6 +299,17 @@ struct imsrg_op {
 namespace imsrg {
 
 int build_basis(imsrg_basis *b);            // host tables + device upload (basis.cpp)
+// Where v_elem (basic_IMSRG.f90:1270-1385) finds <a b|V|c d>_J in the flat
+// layout (idx -1: structurally zero) and how it modifies the stored value.
+struct HLoc {
+  long idx;   // flat index, -1 if structurally zero
+  int neg;    // pair-reordering phase
+  int nsq;    // sqrt(2) normalisation factors
+  int trans;  // read transposed (times herm)
+};
+HLoc v_location(const imsrg_basis *b, int a, int bb, int c, int d, int J2);
+// {a b c; d e f} with doubled arguments (host, exact Racah sum)
+double sixj(int a, int b, int c, int d, int e, int f);
 void free_basis_device(imsrg_basis *b);
 int cuda_status(cudaError_t e);
 

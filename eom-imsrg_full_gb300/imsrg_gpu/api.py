@@ -38,6 +38,7 @@ SYMBOLS = (
     "imsrg_gpu_split_schedule", "imsrg_gpu_split_schedule_set", "imsrg_gpu_build_gs_atan", "imsrg_gpu_build_gs_w2", "imsrg_gpu_magnus_decouple_gen",
     "imsrg_gpu_op_save", "imsrg_gpu_op_load", "imsrg_gpu_checkpoint_name", "imsrg_gpu_normal_order",
     "imsrg_gpu_dhds", "imsrg_gpu_transform_bch", "imsrg_gpu_ode_decouple", "imsrg_gpu_commutator_host",
+    "imsrg_gpu_read_interaction", "imsrg_gpu_h0_harm_osc", "imsrg_gpu_hartree_fock",
 )
 
 KERNELS = ("cc_forward", "gemm_fp64", "assemble_2body", "assemble_1body", "ozaki_slice", "ozaki_mma",
@@ -120,6 +121,9 @@ def lib():
             "imsrg_gpu_dhds": [vp, vp, i, i],
             "imsrg_gpu_ode_decouple": [vp, i, i, d, d, i, d, d, dp, ip, C.POINTER(C.c_long)],
             "imsrg_gpu_transform_bch": [vp, vp, i, ip],
+            "imsrg_gpu_read_interaction": [vp, C.c_char_p, i, d, d, d, i],
+            "imsrg_gpu_h0_harm_osc": [vp, i, d, d, d, i],
+            "imsrg_gpu_hartree_fock": [vp, d, i, dp, ip, dp],
         }
         for name, args in sig.items():
             f = getattr(L, name)
@@ -167,6 +171,8 @@ class Basis:
         self.info = info
         self.nfull = info.nfull
         self.neq = info.neq
+        self.norb = len(arrs[2])
+        self.jj, self.con = arrs[2].copy(), arrs[4].copy()
 
     @classmethod
     def from_dict(cls, d):
@@ -498,6 +504,46 @@ def checkpoint_name(directory: str, prefix: str, s: float) -> str:
 
 def normal_order(H: Operator):
     _check(lib().imsrg_gpu_normal_order(H.handle), "normal_order")
+
+
+def _nucleons(basis: Basis) -> int:
+    # A = sum over hole orbits of (2j + 1)
+    return int(sum(j + 1 for j, c in zip(basis.jj, basis.con) if c == 1))
+
+
+def read_interaction(H: Operator, path: str, htype: int = 1, hw: float = 20.0, com_hw: float | None = None,
+                     lawson_beta: float = 0.0, mass: int | None = None):
+    """read_interaction (interaction_IO.f90:8-107): H (herm +1) is cleared and
+    filled with the two-body elements of the ASCII file at `path`, plus the
+    centre-of-mass / Lawson terms of `htype`, `lawson_beta`, `com_hw` (default
+    hw).  `mass` defaults to the reference's nucleon count."""
+    m = _nucleons(H.basis) if mass is None else int(mass)
+    _check(lib().imsrg_gpu_read_interaction(H.handle, os.fsencode(path), int(htype), float(hw),
+                                            float(hw if com_hw is None else com_hw), float(lawson_beta), m),
+           "read_interaction")
+
+
+def h0_harm_osc(H: Operator, htype: int = 1, hw: float = 20.0, com_hw: float | None = None,
+                lawson_beta: float = 0.0, mass: int | None = None):
+    """calculate_h0_harm_osc (basic_IMSRG.f90:2049-2147): the HO one-body part
+    of H for `htype` 1-5."""
+    m = _nucleons(H.basis) if mass is None else int(mass)
+    _check(lib().imsrg_gpu_h0_harm_osc(H.handle, int(htype), float(hw), float(hw if com_hw is None else com_hw),
+                                       float(lawson_beta), m), "h0_harm_osc")
+
+
+def hartree_fock(H: Operator, tol: float = 1e-6, max_iter: int = 1000) -> dict:
+    """calc_HF (HF_mod.f90:14-106) without a three-body force: H (T + V, not
+    normal ordered) becomes the normal-ordered Hamiltonian in the HF basis.
+    Returns e_hf, the iteration count and the coefficients D (norb x norb,
+    D[a, i] = weight of HO orbit a in HF orbit i)."""
+    n = H.basis.norb
+    e = C.c_double()
+    it = C.c_int()
+    D = np.zeros(n * n)
+    _check(lib().imsrg_gpu_hartree_fock(H.handle, float(tol), int(max_iter), C.byref(e), C.byref(it), _dp(D)),
+           "hartree_fock")
+    return {"e_hf": e.value, "iterations": it.value, "coefs": D.reshape(n, n, order="F")}
 
 
 def dhds(HS: Operator, DH: Operator, generator: str = "white", precision: str = "fp64"):

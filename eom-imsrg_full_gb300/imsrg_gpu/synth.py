@@ -123,3 +123,53 @@ def synth_omega(lay: Layout, seed: int, sigma: float = 0.05, stream: int = 2):
     M[...] = rng.normal(0.0, sigma, M.shape) * _ljt_mask(lay, lay.parts, lay.holes)
     _fill_two_body(lay, op, -1, lambda shape: rng.normal(0.0, sigma, shape))
     return op
+
+
+def write_vrenorm(lay: Layout, op, path: str, seed: int | None = None) -> int:
+    """Write the two-body part of a Hermitian operator as the ASCII file that
+    read_interaction reads (n-parzuchowski/EOM-IMSRG_FULL,
+    im-SRG/interaction_IO.f90:8-107): eight header lines, then one line
+    "Tz Par 2J a b c d V" per stored element (orbits 1-based; square arrays
+    upper triangles only, the reader stores both orders).  With a seed, pair
+    orders and bra/ket are swapped at random with the value carrying the pair
+    phases the reader undoes, so every branch of the reader is exercised.
+    Returns the number of element lines."""
+    rng = _rng(seed, 7) if seed is not None else None
+
+    def ph(a, b, J2):  # the reader's phase of a reversed pair
+        return -1.0 if (1 + (lay.jj[a - 1] + lay.jj[b - 1] - J2) // 2) % 2 else 1.0
+
+    n = 0
+    with open(path, "w") as f:
+        f.write("# two-body matrix elements, J-coupled, normalised kets\n")
+        for k in range(6):
+            f.write(f"# header line {k + 2}\n")
+        f.write("# Tz Par 2J a b c d V\n")
+        for b in lay.blocks:
+            for g in range(6):
+                n1, n2 = b.shape[g]
+                if n1 * n2 == 0:
+                    continue
+                X = op[b.off[g]:b.off[g] + n1 * n2].reshape(n2, n1).T
+                rows, cols = b.qn[GAM_ROWCAT[g]], b.qn[GAM_COLCAT[g]]
+                for JX in range(n2):
+                    for IX in range(n1):
+                        if SQUARE[g] and IX > JX:
+                            continue
+                        v = float(X[IX, JX])
+                        if v == 0.0:
+                            continue
+                        a, bb = (int(x) for x in rows[IX])
+                        c, d = (int(x) for x in cols[JX])
+                        if rng is not None:
+                            if rng.random() < 0.5 and a != bb:
+                                a, bb = bb, a
+                                v *= ph(a, bb, b.J2)
+                            if rng.random() < 0.5 and c != d:
+                                c, d = d, c
+                                v *= ph(c, d, b.J2)
+                            if rng.random() < 0.5:
+                                a, bb, c, d = c, d, a, bb
+                        f.write(f"{b.tz} {b.par} {b.J2} {a} {bb} {c} {d} {v!r}\n")
+                        n += 1
+    return n

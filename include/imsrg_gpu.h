@@ -291,6 +291,36 @@ int imsrg_gpu_profile_enable(imsrg_basis_t *b, int on);
 int imsrg_gpu_profile_read(imsrg_basis_t *b, int kernel, double *ms, long *launches);
 int imsrg_gpu_profile_reset(imsrg_basis_t *b);
 
+/* --- setup: interaction file, one-body HO part, Hartree-Fock ---------------
+ * imsrg_gpu_read_interaction replaces read_interaction (interaction_IO.f90:
+ * 8-107): the ASCII two-body file of VRenormalize (eight header lines, then
+ * "Tz Par 2J a b c d V" per line, orbits 1-based in the basis order).  H is
+ * cleared, then every element read is stored with the reference's pair
+ * phases (normalised kets, hermitian input assumed) after the centre-of-mass
+ * correction V += (beta (p1.p2 + (com_hw/hw)^2 r1.r2) - [htype == 1] p1.p2)
+ * hw / mass (the r1.r2 and p1.p2 HO matrix elements of basic_IMSRG.f90:
+ * 4310-4530).  H must have herm +1.  IMSRG_ERR_IO if the file cannot be read
+ * or a line is malformed, IMSRG_ERR_INVALID for an orbit outside the basis. */
+int imsrg_gpu_read_interaction(imsrg_op_t *H, const char *path, int htype, double hw, double com_hw,
+                               double lawson_beta, int mass);
+/* calculate_h0_harm_osc (basic_IMSRG.f90:2049-2147): sets fhh, fph and fpp of
+ * H to the HO kinetic matrix of htype 1 (T - Tcm, Lawson-modified when
+ * |lawson_beta| >= 1e-5), 2 (T + U_HO), 3 (T), 4 (T / mass) or 5 (the Hcm
+ * one-body part); E0 and the two-body part are left as they are. */
+int imsrg_gpu_h0_harm_osc(imsrg_op_t *H, int htype, double hw, double com_hw, double lawson_beta, int mass);
+/* calc_HF (HF_mod.f90:14-106) without a three-body force: iterates the
+ * Hartree-Fock equations of the (l, j, tz) blocks from the HO reference
+ * until the summed eigenvalue change is below tol (the reference uses 1e-6),
+ * at most max_iter times (IMSRG_ERR_NOT_CONVERGED beyond), then leaves H in
+ * the normal-ordered HF basis: the one-body part is the Fock matrix in the HF
+ * basis, the two-body part transformed, E0 = E_HF.  H holds T (one-body) and
+ * V (two-body) on entry, not normal ordered (the reference's state after
+ * read_interaction and calculate_h0_harm_osc).  coefs (may be NULL) receives
+ * the HF coefficients D: norb x norb, column-major, D(a, i) the weight of HO
+ * orbit a in HF orbit i (zero across blocks).  Density, Fock matrix,
+ * diagonalisation and both transformations run on the GPU. */
+int imsrg_gpu_hartree_fock(imsrg_op_t *H, double tol, int max_iter, double *e_hf, int *iterations, double *coefs);
+
 /* --- allocation-free commutator (no counterpart in the reference) --------
  * For callers that may not allocate device memory while they run: a host
  * program whose device memory is owned by another allocator or capped, code
