@@ -54,9 +54,10 @@ double reduced_rp(const imsrg_basis *b, int a, int c, bool p) {
 // the spin-orbit recoupled single-particle factor of r1_r2 / p1_p2
 double jfac(const imsrg_basis *b, int x, int y, bool p) {
   if (b->itzp[x] != b->itzp[y]) return 0.0;
+  const double red = reduced_rp(b, x, y, p);
+  if (red == 0.0) return 0.0;
   const int jx = b->jj[x], jy = b->jj[y], lx = b->ll[x], ly = b->ll[y];
-  return std::sqrt((jx + 1.0) * (jy + 1.0)) * phase((3 + 2 * lx + jy) / 2) * sixj(jx, 2, jy, 2 * ly, 1, 2 * lx) *
-         reduced_rp(b, x, y, p);
+  return std::sqrt((jx + 1.0) * (jy + 1.0)) * phase((3 + 2 * lx + jy) / 2) * sixj(jx, 2, jy, 2 * ly, 1, 2 * lx) * red;
 }
 
 // r1.r2 (times b^2) or p1.p2 (over b^2) between normalised kets |a b; J>,
