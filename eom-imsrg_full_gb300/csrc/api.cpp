@@ -96,10 +96,16 @@ int dhds_dev(imsrg_basis *b, const double *HS, int hH, double *DH, int generator
 }
 
 // The launch sequence of one commutator.  Independent launches run on the
-// two side streams, forked from and joined back into the basis stream with
-// events, so the call stays one ordered unit on that stream.
+// side streams, forked from and joined back into the basis stream with
+// events, so the call stays one ordered unit on that stream.  `phases`
+// selects the part before the products (kPhaseFront: E0, images, Pandya
+// transform), the products (kPhaseProducts) and the part after them
+// (kPhaseBack: assemblies, joins); a batch of commutators runs the products
+// of all its bases in one launch between the two (device operands only).
 int commutator_launches(imsrg_basis *b, const double *L, int hL, const double *R, int hR, double *RES, int hRES,
-                        int precision, int with_e0, const HostIO *io = nullptr) {
+                        int precision, int with_e0, const HostIO *io, int phases) {
+  const bool front = phases & kPhaseFront, prods = phases & kPhaseProducts, back = phases & kPhaseBack;
+  if (io && phases != kPhaseAll) return IMSRG_ERR_INVALID;
   // While kernel timing is on, every launch goes to the basis stream in the
   // same order, so each kernel class's event pair times that kernel alone.
   const bool serial = b->prof.on;
@@ -142,7 +148,7 @@ int commutator_launches(imsrg_basis *b, const double *L, int hL, const double *R
   // Pandya transform and the slicing, and is joined at the end (after the
   // one-body assembly, where it ran before, it finished last: the one-body
   // kernel runs slowly beside the 3,769 CTAs of the two-body assembly)
-  if (with_e0) {
+  if (with_e0 && front) {
     if (serial) {
       IMSRG_TRY(launch_e0(b, L, hL, R, hR, RES, b->stream));
     } else {
@@ -172,23 +178,26 @@ int commutator_launches(imsrg_basis *b, const double *L, int hL, const double *R
   } else if (oz) {
     // digit images of L and of R on the two side streams, beside the Pandya
     // transform and the images of LCC and RCC
-    IMSRG_TRY(fork(0));
-    if (!serial) IMSRG_CUDA_TRY(cudaStreamWaitEvent(b->side2, b->ev_fork[0], 0));
-    IMSRG_TRY(ozaki_slice(b, L, R, 0, side));
-    IMSRG_TRY(ozaki_slice(b, L, R, 1, side2));
-    IMSRG_TRY(ozaki_cc_exponents(b, b->stream, &cc_exps, &gL, &gR));
-    IMSRG_TRY(launch_cc_forward(b, L, hL, R, hR, cc_exps, gL, gR));
-    IMSRG_TRY(ozaki_slice(b, L, R, 2, b->stream, cc_exps != nullptr));
-    IMSRG_TRY(join(0));
-    if (!serial) {
-      IMSRG_CUDA_TRY(cudaEventRecord(b->ev_join2, b->side2));
-      IMSRG_CUDA_TRY(cudaStreamWaitEvent(b->stream, b->ev_join2, 0));
+    if (front) {
+      IMSRG_TRY(fork(0));
+      if (!serial) IMSRG_CUDA_TRY(cudaStreamWaitEvent(b->side2, b->ev_fork[0], 0));
+      IMSRG_TRY(ozaki_slice(b, L, R, 0, side));
+      IMSRG_TRY(ozaki_slice(b, L, R, 1, side2));
+      IMSRG_TRY(ozaki_cc_exponents(b, b->stream, &cc_exps, &gL, &gR));
+      IMSRG_TRY(launch_cc_forward(b, L, hL, R, hR, cc_exps, gL, gR));
+      IMSRG_TRY(ozaki_slice(b, L, R, 2, b->stream, cc_exps != nullptr));
+      IMSRG_TRY(join(0));
+      if (!serial) {
+        IMSRG_CUDA_TRY(cudaEventRecord(b->ev_join2, b->side2));
+        IMSRG_CUDA_TRY(cudaStreamWaitEvent(b->stream, b->ev_join2, 0));
+      }
     }
-    IMSRG_TRY(ozaki_mma(b, hL, hR));
+    if (prods) IMSRG_TRY(ozaki_mma(b, hL, hR));
   } else {
-    IMSRG_TRY(launch_cc_forward(b, L, hL, R, hR));
-    IMSRG_TRY(launch_gemm_fp64(b, L, hL, R, hR));
+    if (front) IMSRG_TRY(launch_cc_forward(b, L, hL, R, hR));
+    if (prods) IMSRG_TRY(launch_gemm_fp64(b, L, hL, R, hR));
   }
+  if (!back) return IMSRG_OK;
   // one-body assembly beside the two-body assembly, after the packed (L, R)
   // pairs of the 122 gathers, which are built beside the recoupling inputs
   // (earlier, beside the Pandya transform, they slowed it)
@@ -262,7 +271,7 @@ int commutator_dev(imsrg_basis *b, const double *L, int hL, const double *R, int
   }
   const bool graphable = !b->prof.on && cs == cudaStreamCaptureStatusNone && pinned &&
                          (precision != IMSRG_PREC_OZAKI || ozaki_tuned(b));
-  if (!graphable) return commutator_launches(b, L, hL, R, hR, RES, hRES, precision, with_e0, io);
+  if (!graphable) return commutator_launches(b, L, hL, R, hR, RES, hRES, precision, with_e0, io, kPhaseAll);
   const HostIO none{nullptr, nullptr, nullptr};
   const HostIO &key = io ? *io : none;
   b->comm_calls++;
@@ -277,7 +286,7 @@ int commutator_dev(imsrg_basis *b, const double *L, int hL, const double *R, int
   // capture the sequence of this argument set
   IMSRG_CUDA_TRY(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
   const long launches0 = b->launches;
-  int s = commutator_launches(b, L, hL, R, hR, RES, hRES, precision, with_e0, io);
+  int s = commutator_launches(b, L, hL, R, hR, RES, hRES, precision, with_e0, io, kPhaseAll);
   cudaGraph_t graph = nullptr;
   cudaError_t e = cudaStreamEndCapture(b->stream, &graph);
   IMSRG_TRY(s);
@@ -612,6 +621,166 @@ int imsrg_gpu_commutator_host(imsrg_basis_t *b, const double *L, int herm_L, con
                                   &io));
   IMSRG_CUDA_TRY(cudaStreamSynchronize(b->stream));
   return imsrg::ozaki_check_error(b);
+}
+
+}  // extern "C"
+
+// A batch of independent commutators, one per basis (imsrg_gpu_batch_*).
+struct imsrg_batch {
+  std::vector<imsrg_basis *> bases;
+  void *oz = nullptr;  // the merged split-precision plan
+  cudaStream_t st = nullptr;
+  cudaEvent_t ev_start = nullptr, ev_mma = nullptr;
+  std::vector<cudaEvent_t> ev_front, ev_back;
+  struct Graph {
+    std::vector<const void *> key;
+    cudaGraphExec_t exec;
+  };
+  std::vector<Graph> graphs;  // one per argument set, least recently built dropped first
+};
+
+namespace {
+
+void batch_release(imsrg_batch *bt) {
+  for (imsrg_batch::Graph &g : bt->graphs) cudaGraphExecDestroy(g.exec);
+  bt->graphs.clear();
+  for (cudaEvent_t e : bt->ev_front) cudaEventDestroy(e);
+  for (cudaEvent_t e : bt->ev_back) cudaEventDestroy(e);
+  if (bt->ev_start) cudaEventDestroy(bt->ev_start);
+  if (bt->ev_mma) cudaEventDestroy(bt->ev_mma);
+  if (bt->st) cudaStreamDestroy(bt->st);
+  imsrg::ozaki_batch_free(bt->oz);
+  delete bt;
+}
+
+// One step of the batch on the batch stream: every basis's part before the
+// products on its own streams, the products of all bases in one launch (split
+// precision; FP64 runs each basis's own sequence), every basis's part after
+// them, joined back into the batch stream.
+int batch_sequence(imsrg_batch *bt, imsrg_op_t *const *L, imsrg_op_t *const *R, imsrg_op_t *const *RES,
+                   int precision, int with_e0) {
+  const int n = (int)bt->bases.size();
+  const bool oz = precision == IMSRG_PREC_OZAKI;
+  IMSRG_CUDA_TRY(cudaEventRecord(bt->ev_start, bt->st));
+  for (int i = 0; i < n; i++) {
+    imsrg_basis *b = bt->bases[i];
+    IMSRG_CUDA_TRY(cudaStreamWaitEvent(b->stream, bt->ev_start, 0));
+    IMSRG_TRY(imsrg::commutator_launches(b, L[i]->d, L[i]->herm, R[i]->d, R[i]->herm, RES[i]->d, RES[i]->herm,
+                                         precision, with_e0, nullptr,
+                                         oz ? imsrg::kPhaseFront : imsrg::kPhaseAll));
+    IMSRG_CUDA_TRY(cudaEventRecord(bt->ev_front[i], b->stream));
+    IMSRG_CUDA_TRY(cudaStreamWaitEvent(bt->st, bt->ev_front[i], 0));
+  }
+  if (!oz) return IMSRG_OK;
+  IMSRG_TRY(imsrg::ozaki_batch_mma(bt->oz, bt->st, L[0]->herm, R[0]->herm));
+  for (imsrg_basis *b : bt->bases) b->launches++;
+  IMSRG_CUDA_TRY(cudaEventRecord(bt->ev_mma, bt->st));
+  for (int i = 0; i < n; i++) {
+    imsrg_basis *b = bt->bases[i];
+    IMSRG_CUDA_TRY(cudaStreamWaitEvent(b->stream, bt->ev_mma, 0));
+    IMSRG_TRY(imsrg::commutator_launches(b, L[i]->d, L[i]->herm, R[i]->d, R[i]->herm, RES[i]->d, RES[i]->herm,
+                                         precision, with_e0, nullptr, imsrg::kPhaseBack));
+    IMSRG_CUDA_TRY(cudaEventRecord(bt->ev_back[i], b->stream));
+    IMSRG_CUDA_TRY(cudaStreamWaitEvent(bt->st, bt->ev_back[i], 0));
+  }
+  return IMSRG_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int imsrg_gpu_batch_create(int n, imsrg_basis_t *const *bases, imsrg_batch_t **out) {
+  if (!out || n <= 0 || !bases) return IMSRG_ERR_INVALID;
+  *out = nullptr;
+  for (int i = 0; i < n; i++) {
+    if (!bases[i]) return IMSRG_ERR_INVALID;
+    for (int k = 0; k < i; k++)
+      if (bases[k] == bases[i]) return IMSRG_ERR_INVALID;  // each basis once: its streams and workspace
+  }
+  imsrg_batch *bt = new imsrg_batch();
+  bt->bases.assign(bases, bases + n);
+  int s = IMSRG_OK;
+  auto ev = [&](cudaEvent_t *e) {
+    if (s == IMSRG_OK) s = imsrg::cuda_status(cudaEventCreateWithFlags(e, cudaEventDisableTiming));
+  };
+  IMSRG_CUDA_TRY(cudaSetDevice(bases[0]->device));
+  s = imsrg::cuda_status(cudaStreamCreateWithFlags(&bt->st, cudaStreamNonBlocking));
+  ev(&bt->ev_start);
+  ev(&bt->ev_mma);
+  bt->ev_front.assign(n, nullptr);
+  bt->ev_back.assign(n, nullptr);
+  for (int i = 0; i < n; i++) {
+    ev(&bt->ev_front[i]);
+    ev(&bt->ev_back[i]);
+  }
+  if (s == IMSRG_OK) s = imsrg::ozaki_batch_create(bt->bases.data(), n, &bt->oz);
+  if (s != IMSRG_OK) {
+    batch_release(bt);
+    return s;
+  }
+  *out = bt;
+  return IMSRG_OK;
+}
+
+int imsrg_gpu_batch_destroy(imsrg_batch_t *batch) {
+  if (!batch) return IMSRG_ERR_INVALID;
+  cudaStreamSynchronize(batch->st);
+  batch_release(batch);
+  return IMSRG_OK;
+}
+
+int imsrg_gpu_batch_commutator(imsrg_batch_t *batch, imsrg_op_t *const *L, imsrg_op_t *const *R,
+                               imsrg_op_t *const *RES, int precision, int with_e0) {
+  if (!batch || !L || !R || !RES) return IMSRG_ERR_INVALID;
+  if (precision != IMSRG_PREC_FP64 && precision != IMSRG_PREC_OZAKI) return IMSRG_ERR_INVALID;
+  const int n = (int)batch->bases.size();
+  bool graphable = true;
+  std::vector<const void *> key{(const void *)(long)precision, (const void *)(long)(with_e0 ? 1 : 0)};
+  for (int i = 0; i < n; i++) {
+    imsrg_basis *b = batch->bases[i];
+    for (imsrg_op_t *op : {L[i], R[i], RES[i]}) {
+      IMSRG_TRY(check_op(op));
+      if (op->b != b) return IMSRG_ERR_MISMATCH;
+    }
+    if (RES[i] == L[i] || RES[i] == R[i]) return IMSRG_ERR_INVALID;
+    // one launch takes one pair of Hermiticities
+    if (L[i]->herm != L[0]->herm || R[i]->herm != R[0]->herm) return IMSRG_ERR_INVALID;
+    RES[i]->herm = -L[i]->herm * R[i]->herm;
+    graphable = graphable && !b->prof.on;
+    key.push_back(L[i]->d);
+    key.push_back(R[i]->d);
+    key.push_back(RES[i]->d);
+  }
+  key.push_back((const void *)(long)L[0]->herm);
+  key.push_back((const void *)(long)R[0]->herm);
+  if (!graphable) {
+    IMSRG_TRY(batch_sequence(batch, L, R, RES, precision, with_e0 ? 1 : 0));
+  } else {
+    cudaGraphExec_t exec = nullptr;
+    for (const imsrg_batch::Graph &g : batch->graphs)
+      if (g.key == key) exec = g.exec;
+    if (!exec) {
+      IMSRG_CUDA_TRY(cudaStreamBeginCapture(batch->st, cudaStreamCaptureModeThreadLocal));
+      const int s = batch_sequence(batch, L, R, RES, precision, with_e0 ? 1 : 0);
+      cudaGraph_t graph = nullptr;
+      const cudaError_t e = cudaStreamEndCapture(batch->st, &graph);
+      IMSRG_TRY(s);
+      IMSRG_CUDA_TRY(e);
+      const cudaError_t ei = cudaGraphInstantiate(&exec, graph, 0);
+      cudaGraphDestroy(graph);
+      IMSRG_CUDA_TRY(ei);
+      if (batch->graphs.size() >= 4) {
+        cudaGraphExecDestroy(batch->graphs.front().exec);
+        batch->graphs.erase(batch->graphs.begin());
+      }
+      batch->graphs.push_back({key, exec});
+    }
+    IMSRG_CUDA_TRY(cudaGraphLaunch(exec, batch->st));
+  }
+  IMSRG_CUDA_TRY(cudaStreamSynchronize(batch->st));
+  if (precision == IMSRG_PREC_OZAKI) IMSRG_TRY(imsrg::ozaki_batch_error(batch->oz, batch->st));
+  return IMSRG_OK;
 }
 
 int imsrg_gpu_build_gs_white(const imsrg_op_t *H, imsrg_op_t *ETA) {

@@ -379,6 +379,14 @@ int ozaki_wcc_scale(imsrg_basis *b, const int **exps, const int2 **ccgroups);
 int ozaki_schedule_info(imsrg_basis *b, int *choice, int *ncand, double *us, int max);
 int ozaki_set_schedule(imsrg_basis *b, int model);  // pin one cost model, no timing
 void ozaki_free(imsrg_basis *b);
+// The products of several bases as one persistent launch (a batch of
+// independent commutators): ozaki_batch_create merges the bases' plans,
+// ozaki_batch_mma gathers their block exponents and launches on st,
+// ozaki_batch_error reads (and clears) the bounded-wait flag.
+int ozaki_batch_create(imsrg_basis *const *bases, int n, void **out);
+int ozaki_batch_mma(void *batch, cudaStream_t st, int hL, int hR);
+int ozaki_batch_error(void *batch, cudaStream_t st);
+void ozaki_batch_free(void *batch);
 
 // Magnus flow step as a CUDA graph (graph.cu)
 int flow_tmp_ops(imsrg_basis *b, imsrg_op **H0, imsrg_op **DG, imsrg_op **X0, imsrg_op **X1);  // api.cpp
@@ -409,6 +417,11 @@ void profile_free(imsrg_basis *b);
 // basis stream
 int commutator_dev(imsrg_basis *b, const double *L, int hL, const double *R, int hR, double *RES, int hRES,
                    int precision, int with_e0, const HostIO *io = nullptr);
+// parts of the launch sequence of one commutator (device operands for any
+// part short of kPhaseAll)
+constexpr int kPhaseFront = 1, kPhaseProducts = 2, kPhaseBack = 4, kPhaseAll = 7;
+int commutator_launches(imsrg_basis *b, const double *L, int hL, const double *R, int hR, double *RES, int hRES,
+                        int precision, int with_e0, const HostIO *io, int phases);
 
 }  // namespace imsrg
 

@@ -1115,6 +1115,130 @@ int ozaki_schedule_info(imsrg_basis *b, int *choice, int *ncand, double *us, int
   return IMSRG_OK;
 }
 
+// ---------------------------------------------------------------------------
+// One persistent launch for the products of several bases.  Every problem
+// keeps its own output pointer; its exponent groups and tensor maps are
+// renumbered into merged arrays, and the tiles of all bases are assigned
+// longest first over one grid.  Each basis's slicing still writes its own
+// exponents; ozaki_batch_mma gathers them (one small copy per basis) before
+// the launch.  Tiles compute exactly as in a basis's own launch, so results
+// are bit-identical.
+namespace {
+struct OzBatch {
+  std::vector<OzPlan *> plans;
+  std::vector<int> exps_base;
+  OzProb *d_probs = nullptr;
+  int nprobs = 0, grid = 0, ngroups = 0;
+  int2 *d_sched = nullptr;
+  int *d_sched_off = nullptr, *d_exps = nullptr, *d_err = nullptr;
+  CUtensorMap *d_maps = nullptr;
+  ~OzBatch() {
+    cudaFree(d_probs);
+    cudaFree(d_sched);
+    cudaFree(d_sched_off);
+    cudaFree(d_exps);
+    cudaFree(d_err);
+    cudaFree(d_maps);
+  }
+};
+}  // namespace
+
+int ozaki_batch_create(imsrg_basis *const *bases, int n, void **out) {
+  *out = nullptr;
+  if (n <= 0) return IMSRG_ERR_INVALID;
+  OzBatch *bt = new OzBatch();
+  auto fail = [&](int s) {
+    delete bt;
+    return s;
+  };
+  OzPlan all;  // the merged tile list, for build_sched
+  std::vector<OzProb> probs;
+  std::vector<CUtensorMap> maps;
+  int model = -1;
+  for (int i = 0; i < n; i++) {
+    const int s = ozaki_prepare(bases[i]);
+    if (s != IMSRG_OK) return fail(s);
+    OzPlan *pl = plan_of(bases[i]);
+    if (!pl || !pl->ok || bases[i]->device != bases[0]->device) return fail(IMSRG_ERR_INVALID);
+    bt->plans.push_back(pl);
+    bt->exps_base.push_back(bt->ngroups);
+    const int p0 = (int)probs.size(), m0 = (int)maps.size();
+    for (const OzProb &p : pl->probs) {
+      OzProb q = p;
+      q.gA += bt->ngroups;
+      q.gB += bt->ngroups;
+      for (int t = 0; t < q.nterms; t++) {
+        q.t[t].a_map += m0;
+        q.t[t].b_map += m0;
+      }
+      probs.push_back(q);
+    }
+    for (size_t k = 0; k < pl->tile_slot.size(); k++) {
+      all.tile_ksteps.push_back(pl->tile_ksteps[k]);
+      all.tile_live.push_back(pl->tile_live[k]);
+      all.tile_slot.push_back(make_int2(pl->tile_slot[k].x + p0, pl->tile_slot[k].y));
+    }
+    maps.insert(maps.end(), pl->maps.begin(), pl->maps.end());
+    bt->ngroups += pl->ngroups;
+    // the bases' own tuned cost model when they agree, else the one usually chosen
+    const int m = pl->tuned ? pl->tune_choice : 1;
+    model = (model < 0 || model == m) ? m : 1;
+  }
+  int nsm = 0;
+  IMSRG_CUDA_TRY(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, bases[0]->device));
+  all.grid = std::min(nsm, std::max((int)all.tile_slot.size(), 1));
+  std::vector<int2> sched;
+  std::vector<int> sched_off;
+  build_sched(&all, kSchedModels[model < 0 ? 1 : model], sched, sched_off);
+  bt->grid = all.grid;
+  bt->nprobs = (int)probs.size();
+  auto up = [&](const void *h, size_t bytes, void **d) -> int {
+    IMSRG_CUDA_TRY(cudaMalloc(d, std::max<size_t>(bytes, 16)));
+    if (bytes) IMSRG_CUDA_TRY(cudaMemcpy(*d, h, bytes, cudaMemcpyHostToDevice));
+    return IMSRG_OK;
+  };
+  int s = IMSRG_OK;
+  if (s == IMSRG_OK) s = up(probs.data(), probs.size() * sizeof(OzProb), (void **)&bt->d_probs);
+  if (s == IMSRG_OK) s = up(sched.data(), sched.size() * sizeof(int2), (void **)&bt->d_sched);
+  if (s == IMSRG_OK) s = up(sched_off.data(), sched_off.size() * sizeof(int), (void **)&bt->d_sched_off);
+  // (cudaMalloc memory is 256-byte aligned: the 64-byte alignment of a tensor map holds)
+  if (s == IMSRG_OK) s = up(maps.data(), maps.size() * sizeof(CUtensorMap), (void **)&bt->d_maps);
+  if (s == IMSRG_OK) s = cuda_status(cudaMalloc((void **)&bt->d_exps, std::max(bt->ngroups, 1) * sizeof(int)));
+  const int zero = 0;
+  if (s == IMSRG_OK) s = up(&zero, sizeof(int), (void **)&bt->d_err);
+  if (s != IMSRG_OK) return fail(s);
+  *out = bt;
+  return IMSRG_OK;
+}
+
+int ozaki_batch_mma(void *batch, cudaStream_t st, int hL, int hR) {
+  OzBatch *bt = (OzBatch *)batch;
+  if (!bt) return IMSRG_ERR_INVALID;
+  for (size_t i = 0; i < bt->plans.size(); i++)
+    if (bt->plans[i]->ngroups > 0)
+      IMSRG_CUDA_TRY(cudaMemcpyAsync(bt->d_exps + bt->exps_base[i], bt->plans[i]->d_exps,
+                                     bt->plans[i]->ngroups * sizeof(int), cudaMemcpyDeviceToDevice, st));
+  const int smem = STAGES * STAGE_BYTES + 1024 + 256;
+  k_oz_mma<<<bt->grid, OZ_THREADS, smem, st>>>(bt->d_probs, bt->nprobs, bt->d_sched, bt->d_sched_off, bt->d_exps,
+                                               hL, hR, bt->d_err, bt->d_maps);
+  return cuda_status(cudaGetLastError());
+}
+
+int ozaki_batch_error(void *batch, cudaStream_t st) {
+  OzBatch *bt = (OzBatch *)batch;
+  if (!bt) return IMSRG_ERR_INVALID;
+  int h = 0;
+  IMSRG_CUDA_TRY(cudaMemcpyAsync(&h, bt->d_err, sizeof(int), cudaMemcpyDeviceToHost, st));
+  IMSRG_CUDA_TRY(cudaStreamSynchronize(st));
+  if (h) {
+    cudaMemsetAsync(bt->d_err, 0, sizeof(int), st);
+    return IMSRG_ERR_TIMEOUT;
+  }
+  return IMSRG_OK;
+}
+
+void ozaki_batch_free(void *batch) { delete (OzBatch *)batch; }
+
 void ozaki_free(imsrg_basis *b) {
   OzPlan *pl = plan_of(b);
   if (!pl) return;

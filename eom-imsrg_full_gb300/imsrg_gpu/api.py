@@ -39,6 +39,7 @@ SYMBOLS = (
     "imsrg_gpu_op_save", "imsrg_gpu_op_load", "imsrg_gpu_checkpoint_name", "imsrg_gpu_normal_order",
     "imsrg_gpu_dhds", "imsrg_gpu_transform_bch", "imsrg_gpu_ode_decouple", "imsrg_gpu_commutator_host",
     "imsrg_gpu_read_interaction", "imsrg_gpu_h0_harm_osc", "imsrg_gpu_hartree_fock",
+    "imsrg_gpu_batch_create", "imsrg_gpu_batch_commutator", "imsrg_gpu_batch_destroy",
 )
 
 KERNELS = ("cc_forward", "gemm_fp64", "assemble_2body", "assemble_1body", "ozaki_slice", "ozaki_mma",
@@ -124,6 +125,9 @@ def lib():
             "imsrg_gpu_read_interaction": [vp, C.c_char_p, i, d, d, d, i],
             "imsrg_gpu_h0_harm_osc": [vp, i, d, d, d, i],
             "imsrg_gpu_hartree_fock": [vp, d, i, dp, ip, dp],
+            "imsrg_gpu_batch_create": [i, C.POINTER(vp), C.POINTER(vp)],
+            "imsrg_gpu_batch_commutator": [vp, C.POINTER(vp), C.POINTER(vp), C.POINTER(vp), i, i],
+            "imsrg_gpu_batch_destroy": [vp],
         }
         for name, args in sig.items():
             f = getattr(L, name)
@@ -504,6 +508,35 @@ def checkpoint_name(directory: str, prefix: str, s: float) -> str:
 
 def normal_order(H: Operator):
     _check(lib().imsrg_gpu_normal_order(H.handle), "normal_order")
+
+
+class Batch:
+    """Independent commutators, one per basis, whose split-precision products
+    run as one persistent launch (imsrg_gpu_batch_*)."""
+
+    def __init__(self, bases: list):
+        self.bases = list(bases)
+        arr = (C.c_void_p * len(self.bases))(*[b.handle.value for b in self.bases])
+        self._h = C.c_void_p()
+        _check(lib().imsrg_gpu_batch_create(len(self.bases), arr, C.byref(self._h)), "batch_create")
+
+    def commutator(self, L: list, R: list, RES: list, precision: str = "ozaki", with_e0: bool = True):
+        """RES[i] = [L[i], R[i]] for every basis; returns when all are done."""
+        n = len(self.bases)
+        assert len(L) == len(R) == len(RES) == n
+        arrs = [(C.c_void_p * n)(*[o.handle.value for o in ops]) for ops in (L, R, RES)]
+        _check(lib().imsrg_gpu_batch_commutator(self._h, *arrs, PREC[precision], int(with_e0)), "batch_commutator")
+
+    def close(self):
+        if self._h:
+            _check(lib().imsrg_gpu_batch_destroy(self._h), "batch_destroy")
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 def _nucleons(basis: Basis) -> int:

@@ -291,6 +291,27 @@ int imsrg_gpu_profile_enable(imsrg_basis_t *b, int on);
 int imsrg_gpu_profile_read(imsrg_basis_t *b, int kernel, double *ms, long *launches);
 int imsrg_gpu_profile_reset(imsrg_basis_t *b);
 
+/* --- batches of independent commutators ------------------------------------
+ * Many Hamiltonians at once (e.g. a scan over hbar*omega or coupling
+ * constants): one commutator [L_i, R_i] per basis i, the split-precision
+ * products of all bases in ONE persistent tensor-core launch (their tiles
+ * scheduled longest first over the GPU together), the rest of each
+ * commutator on that basis's own streams beside the others.  The reference
+ * runs one commutator_* sequence per Hamiltonian (IMSRG_MAGNUS.f90:207-219).
+ * imsrg_gpu_batch_create takes n distinct bases (each keeps its own
+ * workspace; they must outlive the batch) and prepares the merged plan.
+ * imsrg_gpu_batch_commutator computes RES_i = [L_i, R_i] for every i (each
+ * operator of basis i; one herm_L and one herm_R for the whole batch;
+ * RES_i herm = -herm_L herm_R) in either precision (FP64: each basis's own
+ * sequence, side by side), results identical to imsrg_gpu_commutator, and
+ * returns when all are done.  Each step is one cached CUDA graph per argument
+ * set. */
+typedef struct imsrg_batch imsrg_batch_t;
+int imsrg_gpu_batch_create(int n, imsrg_basis_t *const *bases, imsrg_batch_t **out);
+int imsrg_gpu_batch_commutator(imsrg_batch_t *batch, imsrg_op_t *const *L, imsrg_op_t *const *R,
+                               imsrg_op_t *const *RES, int precision, int with_e0);
+int imsrg_gpu_batch_destroy(imsrg_batch_t *batch);
+
 /* --- setup: interaction file, one-body HO part, Hartree-Fock ---------------
  * imsrg_gpu_read_interaction replaces read_interaction (interaction_IO.f90:
  * 8-107): the ASCII two-body file of VRenormalize (eight header lines, then
