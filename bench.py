@@ -371,6 +371,7 @@ def run_gpu(args, world, rank, local):
             line["ode"] = ode_emax6(api, orb, lay)
             line["hartree_fock"] = hf_emax6(api, orb, lay)
             line["batch"] = batch_flows(api, args.batch)
+            line["batched_commutators"] = batched_commutators(api)
         if world == 1 and not args.no_cpu_baseline:
             line["cpu_baseline"] = cpu_baseline(orb, lay, seconds=args.cpu_seconds)
         print(json.dumps(line), flush=True)
@@ -452,6 +453,57 @@ def hf_emax6(api, orb, lay):
     return {"emax": EMAX, "file_lines": nlines, "read_s": t1 - t0, "hf_s": t3 - t2, "hf_iterations": r["iterations"],
             "e_hf_MeV": r["e_hf"], "flow_steps": f["steps"], "flow_s": t4 - t3,
             "e0_after_flow_MeV": float(f["trace"][-1, 2])}
+
+
+def batched_commutators(api, n=64, reps=20):
+    """n independent Hamiltonians (hbar*omega ~ U[12,28] MeV, two-body scale
+    ~ U[0.5,2] MeV, emax cycling 2, 4, 6): [Omega_i, H_i] for all of them per
+    step, (a) as one batch (the split-precision products of every instance in
+    one persistent launch, one graph per step) and (b) as n single commutators
+    issued back to back on the instances' own streams (each its own graph),
+    then a synchronisation.  Same results (bit for bit); wall time per step."""
+    import numpy as np
+    from imsrg_gpu.layout import Layout, ho_basis
+    from imsrg_gpu.synth import synth_hamiltonian, synth_omega
+    rng = np.random.default_rng(64)
+    bases, L, R, RES, emaxes = [], [], [], [], []
+    t0 = time.perf_counter()
+    for k in range(n):
+        emax = (2, 4, 6)[k % 3]
+        orb = ho_basis(emax)
+        lay = Layout(**orb)
+        B = api.Basis.from_dict(orb)
+        hw, sig = float(rng.uniform(12.0, 28.0)), float(rng.uniform(0.5, 2.0))
+        bases.append(B)
+        L.append(api.Operator(B, -1, synth_omega(lay, 2000 + k)))
+        R.append(api.Operator(B, 1, synth_hamiltonian(lay, 2000 + k, hw=hw, sigma2=sig)))
+        RES.append(api.Operator(B, 1))
+        emaxes.append(emax)
+    setup_s = time.perf_counter() - t0
+    batch = api.Batch(bases)
+    out = {"instances": n, "emax_counts": {e: emaxes.count(e) for e in (2, 4, 6)}, "setup_s": setup_s,
+           "precision": "ozaki", "reps": reps}
+    for _ in range(3):  # graphs, autotuning of each instance's own schedule
+        batch.commutator(L, R, RES)
+        for i in range(n):
+            api.commutator(L[i], R[i], RES[i], precision="ozaki")
+        for B in bases:
+            B.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(reps):
+        batch.commutator(L, R, RES)
+    tb = (time.perf_counter() - t0) / reps
+    t0 = time.perf_counter()
+    for _ in range(reps):
+        for i in range(n):
+            api.commutator(L[i], R[i], RES[i], precision="ozaki")
+        for B in bases:
+            B.synchronize()
+    ts = (time.perf_counter() - t0) / reps
+    batch.close()
+    out.update({"batch_ms_per_step": tb * 1e3, "batch_commutators_per_s": n / tb,
+                "single_calls_ms_per_step": ts * 1e3, "single_calls_commutators_per_s": n / ts})
+    return out
 
 
 def batch_flows(api, n):
