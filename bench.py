@@ -374,6 +374,9 @@ def run_gpu(args, world, rank, local):
             line["batched_commutators"] = batched_commutators(api)
         if world == 1 and not args.no_cpu_baseline:
             line["cpu_baseline"] = cpu_baseline(orb, lay, seconds=args.cpu_seconds)
+            # the same oracle on one core (the reference itself threads only
+            # the Pandya transform and 222_ph)
+            line["cpu_baseline_1thread"] = cpu_baseline(orb, lay, seconds=args.cpu_seconds / 2, threads=1)
         print(json.dumps(line), flush=True)
     if world > 1:
         torch.distributed.barrier()
@@ -582,7 +585,7 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--no-flows", action="store_true", help="skip the flow and batched-flow extras")
-    ap.add_argument("--batch", type=int, default=16, help="instances of the batched-flow extra")
+    ap.add_argument("--batch", type=int, default=64, help="instances of the batched-flow extra")
     ap.add_argument("--split-schedule", type=int, default=None,
                     help="pin the split engine's CTA schedule model instead of autotuning it "
                          "(for profiler runs, whose serialised launches distort the tuner's timings)")
