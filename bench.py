@@ -589,11 +589,17 @@ def main():
     ap.add_argument("--split-schedule", type=int, default=None,
                     help="pin the split engine's CTA schedule model instead of autotuning it "
                          "(for profiler runs, whose serialised launches distort the tuner's timings)")
+    ap.add_argument("--batched-only", type=int, default=0, metavar="N",
+                    help="only the batched-commutator extra with N instances (for profiling the grouped launch)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     world, rank, local = dist_setup()
     if args.impl == "reference":
         return run_reference(args, world, rank)
+    if args.batched_only:
+        from imsrg_gpu import api
+        print(json.dumps({"batched_commutators": batched_commutators(api, n=args.batched_only, reps=args.steps)}))
+        return 0
     return run_gpu(args, world, rank, local)
 
 
