@@ -130,6 +130,25 @@ class ClockSampler:
         return {"sm_mhz": statistics.median(sm), "sm_max_mhz": smax, "reasons": sorted(reasons), "samples": len(sm)}
 
 
+def max_over_ranks(x: float, device: str) -> float:
+    """The largest x over the ranks of the default process group (x itself
+    without one): each replica's timed region, so the whole job is as slow as
+    its slowest replica."""
+    import torch
+    import torch.distributed as dist
+    if not (dist.is_available() and dist.is_initialized()) or dist.get_world_size() == 1:
+        return x
+    t = torch.tensor([x], device=device, dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def whole_job_rate(steps_per_rank: int, world: int, max_ms: float) -> float:
+    """Commutators per second of all replicas together (weak scaling: each
+    rank runs `steps_per_rank` steps of its own Hamiltonian)."""
+    return world * steps_per_rank / (max_ms / 1e3)
+
+
 def dist_setup():
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -260,11 +279,8 @@ def run_gpu(args, world, rank, local):
     if world > 1:
         torch.distributed.barrier()
     total_ms, launches, prof, clocks = timed(precision, args.steps, args.warmup)
-    if world > 1:
-        t = torch.tensor([total_ms], device="cuda", dtype=torch.float64)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        total_ms = float(t.item())
-    value = world * args.steps / (total_ms / 1e3)
+    total_ms = max_over_ranks(total_ms, "cuda")
+    value = whole_job_rate(args.steps, world, total_ms)
 
     # FP64 path beside the split-precision one, and their difference
     extra = {}
