@@ -536,6 +536,15 @@ int build_basis(imsrg_basis *b) {
     std::vector<std::pair<long, int>> items;      // (signature, head)
     std::vector<std::pair<long, int>> items_out;  // (output range << 40 | signature, head)
     const long two0 = b->off_fpp + (long)P * P;  // first two-body index of the flat layout
+    {  // output ranges: the first holds kOutFirst of the two-body part, the rest share the remainder
+      const long span = b->nfull - two0;
+      b->asm2_addr[0] = two0;
+      for (int c = 1; c < kOutChunks; c++) {
+        const double f = kOutFirst + (c - 1) * (1.0 - kOutFirst) / (kOutChunks - 1);
+        b->asm2_addr[c] = two0 + (long)std::ceil(f * (double)span);
+      }
+      b->asm2_addr[kOutChunks] = b->nfull;
+    }
     auto row16 = [](int r) -> unsigned long long { return r < 0 ? 0xFFFFull : (unsigned long long)r; };
     for (unsigned long long key : qorder) {
       const std::vector<El> &els = qmap[key];
@@ -616,8 +625,8 @@ int build_basis(imsrg_basis *b) {
         // warps run elements of one loop-trip signature; in the order by
         // output range, within the range of the element's lower write
         const long lo = el.em >= 0 ? std::min(el.e, el.em) : el.e;
-        const long span = b->nfull - two0;
-        const long chunk = span > 0 ? std::min<long>((lo - two0) * kOutChunks / span, kOutChunks - 1) : 0;
+        long chunk = 0;
+        while (chunk + 1 < kOutChunks && lo >= b->asm2_addr[chunk + 1]) chunk++;
         const long sig = (((long)n_in * 32 + n_out) * 32 + n122) * 2 + (valid ? 1 : 0);
         items.push_back({sig, (int)heads.size()});
         items_out.push_back({chunk << 40 | sig, (int)heads.size()});
@@ -637,16 +646,10 @@ int build_basis(imsrg_basis *b) {
       ordered[t] = heads[items[t].second];
       ordered_out[t] = heads[items_out[t].second];
     }
-    {
-      const long span = b->nfull - two0;
-      for (int c = 0; c <= kOutChunks; c++) {
-        b->asm2_addr[c] = two0 + ((long)c * span + kOutChunks - 1) / kOutChunks;
-        b->asm2_el[c] = std::lower_bound(items_out.begin(), items_out.end(), (long)c << 40,
-                                         [](const std::pair<long, int> &x, long key) { return x.first < key; }) -
-                        items_out.begin();
-      }
-      b->asm2_addr[kOutChunks] = b->nfull;
-    }
+    for (int c = 0; c <= kOutChunks; c++)
+      b->asm2_el[c] = std::lower_bound(items_out.begin(), items_out.end(), (long)c << 40,
+                                       [](const std::pair<long, int> &x, long key) { return x.first < key; }) -
+                      items_out.begin();
     T.n_asm2 = (int)ordered.size();
     T.n_ph = (int)zt.size();
     IMSRG_TRY(dev_upload(b, ordered, &T.asm2_head));

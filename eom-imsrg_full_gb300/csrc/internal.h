@@ -189,6 +189,11 @@ struct HostIO {
 // 284 us per host-operand commutator with two ranges, 287 with four, 322
 // with eight, 291 with one).
 constexpr int kOutChunks = 2;
+// fraction of the two-body part in the first range (its copy is the one that
+// overlaps; the last range's copy is exposed).  Even is best at emax=6: 269
+// us per host-operand call, 274 / 277 / 279 with 0.6 / 0.7 / 0.8 (a smaller
+// last range fills the GPU less while it is assembled).
+constexpr double kOutFirst = 0.5;
 }  // namespace imsrg
 
 namespace imsrg {
