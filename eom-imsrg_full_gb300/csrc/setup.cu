@@ -390,6 +390,106 @@ std::vector<int> orbit_positions(const imsrg_basis *b) {
   return pos;
 }
 
+// (l, j, tz) blocks in the reference's order (allocate_sp_mat,
+// basic_IMSRG.f90:2600-2660): tz, l, j; their states in orbit order
+int sp_blocks(const imsrg_basis *b, std::vector<SpBlock> &blk, std::vector<int> &states) {
+  int lmax = 0, S = 0;
+  for (int i = 0; i < b->norb; i++) lmax = std::max(lmax, b->ll[i]);
+  blk.clear();
+  states.clear();
+  for (int tz = -1; tz <= 1; tz += 2)
+    for (int l = 0; l <= lmax; l++)
+      for (int j2 = 1; j2 <= b->jtm; j2 += 2) {
+        SpBlock B{0, S, j2, (int)states.size()};
+        for (int i = 0; i < b->norb; i++)
+          if (b->ll[i] == l && b->jj[i] == j2 && b->itzp[i] == tz) {
+            states.push_back(i);
+            B.n++;
+          }
+        if (B.n > HF_MAXN) return IMSRG_ERR_TOO_LARGE;
+        blk.push_back(B);
+        S += B.n * B.n;
+      }
+  return IMSRG_OK;
+}
+
+// a block's matrix M (n x n, column-major at M + B.off) into the one-body
+// part of the flat layout as transform_1b_to_HF (HF_mod.f90:460-487) places it
+void place_onebody(const imsrg_basis *b, const std::vector<int> &pos, const std::vector<int> &states,
+                   const SpBlock &B, const double *M, std::vector<double> &h) {
+  for (int a = 0; a < B.n; a++)
+    for (int c = a; c < B.n; c++) {
+      const int i = states[B.st0 + a], j = states[B.st0 + c];
+      bool tr;
+      if (b->con[i] == b->con[j]) {
+        h[f_index(b, pos, i, j, &tr)] = M[B.off + a + c * B.n];
+        h[f_index(b, pos, j, i, &tr)] = M[B.off + a + c * B.n];
+      } else if (b->con[j] > b->con[i]) {
+        h[f_index(b, pos, i, j, &tr)] = M[B.off + a + c * B.n];
+      } else {
+        h[f_index(b, pos, j, i, &tr)] = M[B.off + c + a * B.n];
+      }
+    }
+}
+
+// transform_2b_to_HF (HF_mod.f90:494-619) of the two-body part of Hd in
+// place with the coefficients Dsm (norb x norb, column-major): per block
+// V' = E^T V E, E = C - (-1)^J Crev, two grouped GEMM launches
+int transform_2b(imsrg_basis *b, double *Hd, const std::vector<double> &Dsm, cudaStream_t st) {
+  std::vector<HfBlock2> b2;
+  std::vector<int2> pairs;
+  std::vector<HfGemm> g1, g2;
+  long woff = 0;
+  int tiles = 0;
+  for (int q = 0; q < b->nblocks; q++) {
+    const int nh = b->nhh[q], nb = b->nph[q], np = b->npp[q], nt = nh + nb + np;
+    if (nt == 0) continue;
+    HfBlock2 B{q, nh, nb, np, nt, woff, (int)pairs.size(), ((q / 6) & 1) ? -1 : 1};
+    for (int c : {2, 1, 0}) {
+      const std::vector<int> &qn = b->qn[q * 3 + c];
+      for (size_t k = 0; k + 1 < qn.size(); k += 2) pairs.push_back(make_int2(qn[k], qn[k + 1]));
+    }
+    b2.push_back(B);
+    const int t1 = (nt + 31) / 32;
+    g1.push_back({woff, woff, woff, nt, 0, tiles, t1});  // Tmp = Vf E
+    g2.push_back({woff, woff, woff, nt, 1, tiles, t1});  // Vn = E^T Tmp
+    tiles += t1 * t1;
+    woff += (long)nt * nt;
+  }
+  if (b2.empty()) return IMSRG_OK;
+  HfScratch sc;
+  HfBlock2 *d_b2;
+  int2 *d_pairs;
+  HfGemm *d_g1, *d_g2;
+  double *d_Dsm, *d_V, *d_E, *d_Tmp;
+  int *d_jj;
+  std::vector<int> jjv(b->jj.begin(), b->jj.end());
+  IMSRG_TRY(sc.upload(b2, &d_b2));
+  IMSRG_TRY(sc.upload(pairs, &d_pairs));
+  IMSRG_TRY(sc.upload(g1, &d_g1));
+  IMSRG_TRY(sc.upload(g2, &d_g2));
+  IMSRG_TRY(sc.upload(Dsm, &d_Dsm));
+  IMSRG_TRY(sc.upload(jjv, &d_jj));
+  IMSRG_TRY(sc.zeros(woff, &d_V));
+  IMSRG_TRY(sc.zeros(woff, &d_E));
+  IMSRG_TRY(sc.zeros(woff, &d_Tmp));
+  std::vector<long> goff(b->gam_off.begin(), b->gam_off.end());
+  std::vector<int> gn1(b->gam_n1.begin(), b->gam_n1.end()), gn2(b->gam_n2.begin(), b->gam_n2.end());
+  long *d_goff;
+  int *d_gn1, *d_gn2;
+  IMSRG_TRY(sc.upload(goff, &d_goff));
+  IMSRG_TRY(sc.upload(gn1, &d_gn1));
+  IMSRG_TRY(sc.upload(gn2, &d_gn2));
+  const int n2b = (int)b2.size();
+  k_hf_vfull<<<n2b, 256, 0, st>>>(d_b2, d_goff, d_gn1, Hd, d_pairs, d_Dsm, b->norb, d_jj, d_V, d_E);
+  k_hf_gemm<<<tiles, 256, 0, st>>>(d_g1, n2b, d_V, d_E, d_Tmp);
+  k_hf_gemm<<<tiles, 256, 0, st>>>(d_g2, n2b, d_E, d_Tmp, d_V);
+  k_hf_scatter<<<n2b, 256, 0, st>>>(d_b2, d_goff, d_gn1, d_gn2, d_V, Hd);
+  b->launches += 4;
+  IMSRG_CUDA_TRY(cudaGetLastError());
+  return cuda_status(cudaStreamSynchronize(st));  // before the scratch is freed
+}
+
 }  // namespace
 }  // namespace imsrg
 
@@ -502,27 +602,15 @@ extern "C" int imsrg_gpu_hartree_fock(imsrg_op_t *H, double tol, int max_iter, d
   cudaStream_t st = b->stream;
   IMSRG_CUDA_TRY(cudaStreamSynchronize(st));
   const std::vector<int> pos = orbit_positions(b);
-  // (l, j, tz) blocks in the reference's order (allocate_sp_mat): tz, l, j
-  int lmax = 0;
-  for (int i = 0; i < N; i++) lmax = std::max(lmax, b->ll[i]);
   std::vector<SpBlock> blk;
   std::vector<int> states, eig_off;
+  IMSRG_TRY(sp_blocks(b, blk, states));
   int S = 0, ne = 0;
-  for (int tz = -1; tz <= 1; tz += 2)
-    for (int l = 0; l <= lmax; l++)
-      for (int j2 = 1; j2 <= b->jtm; j2 += 2) {
-        SpBlock B{0, S, j2, (int)states.size()};
-        for (int i = 0; i < N; i++)
-          if (b->ll[i] == l && b->jj[i] == j2 && b->itzp[i] == tz) {
-            states.push_back(i);
-            B.n++;
-          }
-        if (B.n > HF_MAXN) return IMSRG_ERR_TOO_LARGE;
-        blk.push_back(B);
-        eig_off.push_back(ne);
-        S += B.n * B.n;
-        ne += B.n;
-      }
+  for (const SpBlock &B : blk) {
+    eig_off.push_back(ne);
+    S += B.n * B.n;
+    ne += B.n;
+  }
   const int nblk = (int)blk.size();
   // T from the operator's one-body part (write_kin_matrix, :138-166)
   std::vector<double> hop(b->nfull);
@@ -625,79 +713,66 @@ extern "C" int imsrg_gpu_hartree_fock(imsrg_op_t *H, double tol, int max_iter, d
   // the Fock matrix in the HF basis is the new one-body part
   std::vector<double> Dsm((size_t)N * N, 0.0);
   for (long k = b->off_fhh; k < b->off_2b; k++) hop[k] = 0.0;
-  for (const SpBlock &B : blk)
-    for (int a = 0; a < B.n; a++) {
+  for (const SpBlock &B : blk) {
+    for (int a = 0; a < B.n; a++)
       for (int c = 0; c < B.n; c++) Dsm[states[B.st0 + a] + (size_t)states[B.st0 + c] * N] = Dh[B.off + a + c * B.n];
-      for (int c = a; c < B.n; c++) {
-        const int i = states[B.st0 + a], j = states[B.st0 + c];
-        bool tr;
-        if (b->con[i] == b->con[j]) {
-          hop[f_index(b, pos, i, j, &tr)] = Fh[B.off + a + c * B.n];
-          hop[f_index(b, pos, j, i, &tr)] = Fh[B.off + a + c * B.n];
-        } else if (b->con[j] > b->con[i]) {
-          hop[f_index(b, pos, i, j, &tr)] = Fh[B.off + a + c * B.n];
-        } else {
-          hop[f_index(b, pos, j, i, &tr)] = Fh[B.off + c + a * B.n];
-        }
-      }
-    }
+    place_onebody(b, pos, states, B, Fh.data(), hop);
+  }
   hop[0] = ehf;
   IMSRG_CUDA_TRY(cudaMemcpyAsync(H->d, hop.data(), b->off_2b * sizeof(double), cudaMemcpyHostToDevice, st));
   // the two-body transformation, block by block (:494-619)
-  std::vector<HfBlock2> b2;
-  std::vector<int2> pairs;
-  std::vector<HfGemm> g1, g2;
-  long woff = 0;
-  int tiles = 0;
-  for (int q = 0; q < b->nblocks; q++) {
-    const int nh = b->nhh[q], nb = b->nph[q], np = b->npp[q], nt = nh + nb + np;
-    if (nt == 0) continue;
-    HfBlock2 B{q, nh, nb, np, nt, woff, (int)pairs.size(), ((q / 6) & 1) ? -1 : 1};
-    for (int c : {2, 1, 0}) {
-      const std::vector<int> &qn = b->qn[q * 3 + c];
-      for (size_t k = 0; k + 1 < qn.size(); k += 2) pairs.push_back(make_int2(qn[k], qn[k + 1]));
-    }
-    b2.push_back(B);
-    const int t1 = (nt + 31) / 32;
-    g1.push_back({woff, woff, woff, nt, 0, tiles, t1});  // Tmp = Vf E
-    g2.push_back({woff, woff, woff, nt, 1, tiles, t1});  // Vn = E^T Tmp
-    tiles += t1 * t1;
-    woff += (long)nt * nt;
-  }
-  if (!b2.empty()) {
-    HfBlock2 *d_b2;
-    int2 *d_pairs;
-    HfGemm *d_g1, *d_g2;
-    double *d_Dsm, *d_V, *d_E, *d_Tmp;
-    int *d_jj;
-    std::vector<int> jjv(b->jj.begin(), b->jj.end());
-    IMSRG_TRY(sc.upload(b2, &d_b2));
-    IMSRG_TRY(sc.upload(pairs, &d_pairs));
-    IMSRG_TRY(sc.upload(g1, &d_g1));
-    IMSRG_TRY(sc.upload(g2, &d_g2));
-    IMSRG_TRY(sc.upload(Dsm, &d_Dsm));
-    IMSRG_TRY(sc.upload(jjv, &d_jj));
-    IMSRG_TRY(sc.zeros(woff, &d_V));
-    IMSRG_TRY(sc.zeros(woff, &d_E));
-    IMSRG_TRY(sc.zeros(woff, &d_Tmp));
-    std::vector<long> goff(b->gam_off.begin(), b->gam_off.end());
-    std::vector<int> gn1(b->gam_n1.begin(), b->gam_n1.end()), gn2(b->gam_n2.begin(), b->gam_n2.end());
-    long *d_goff;
-    int *d_gn1, *d_gn2;
-    IMSRG_TRY(sc.upload(goff, &d_goff));
-    IMSRG_TRY(sc.upload(gn1, &d_gn1));
-    IMSRG_TRY(sc.upload(gn2, &d_gn2));
-    const int n2b = (int)b2.size();
-    k_hf_vfull<<<n2b, 256, 0, st>>>(d_b2, d_goff, d_gn1, H->d, d_pairs, d_Dsm, N, d_jj, d_V, d_E);
-    k_hf_gemm<<<tiles, 256, 0, st>>>(d_g1, n2b, d_V, d_E, d_Tmp);
-    k_hf_gemm<<<tiles, 256, 0, st>>>(d_g2, n2b, d_E, d_Tmp, d_V);
-    k_hf_scatter<<<n2b, 256, 0, st>>>(d_b2, d_goff, d_gn1, d_gn2, d_V, H->d);
-    b->launches += 4;
-    IMSRG_CUDA_TRY(cudaGetLastError());
-  }
+  IMSRG_TRY(transform_2b(b, H->d, Dsm, st));
   IMSRG_CUDA_TRY(cudaStreamSynchronize(st));
   if (e_hf) *e_hf = ehf;
   if (iterations) *iterations = it;
   if (coefs) std::memcpy(coefs, Dsm.data(), Dsm.size() * sizeof(double));
   return IMSRG_OK;
+}
+
+extern "C" int imsrg_gpu_transform_to_hf(imsrg_op_t *Op, const double *coefs) {
+  IMSRG_TRY(op_ok(Op));
+  if (!coefs || Op->herm != 1) return IMSRG_ERR_INVALID;
+  imsrg_basis *b = Op->b;
+  const int N = b->norb;
+  cudaStream_t st = b->stream;
+  const std::vector<int> pos = orbit_positions(b);
+  std::vector<SpBlock> blk;
+  std::vector<int> states;
+  IMSRG_TRY(sp_blocks(b, blk, states));
+  std::vector<double> Dsm(coefs, coefs + (size_t)N * N);
+  // write_kin_matrix and transform_1b_to_HF (HF_mod.f90:108-136): the
+  // one-body part block by block, X' = D^T X D, on the host (a few matrices
+  // of at most HF_MAXN rows); zero across blocks
+  std::vector<double> h(b->off_2b);
+  IMSRG_CUDA_TRY(cudaMemcpyAsync(h.data(), Op->d, b->off_2b * sizeof(double), cudaMemcpyDeviceToHost, st));
+  IMSRG_CUDA_TRY(cudaStreamSynchronize(st));
+  std::vector<double> M;
+  std::vector<double> out(h);
+  for (long k = b->off_fhh; k < b->off_2b; k++) out[k] = 0.0;
+  for (const SpBlock &B : blk) {
+    const int n = B.n;
+    if (n == 0) continue;
+    std::vector<double> X(n * n), D(n * n), Y(n * n, 0.0);
+    for (int i = 0; i < n; i++)
+      for (int j = 0; j < n; j++) {
+        bool tr;
+        X[i + j * n] = h[f_index(b, pos, states[B.st0 + i], states[B.st0 + j], &tr)];
+        D[i + j * n] = Dsm[states[B.st0 + i] + (size_t)states[B.st0 + j] * N];
+      }
+    M.assign(B.off + n * n, 0.0);
+    for (int i = 0; i < n; i++)  // Y = X D
+      for (int j = 0; j < n; j++)
+        for (int k = 0; k < n; k++) Y[i + j * n] += X[i + k * n] * D[k + j * n];
+    for (int i = 0; i < n; i++)  // D^T Y
+      for (int j = 0; j < n; j++) {
+        double s = 0.0;
+        for (int k = 0; k < n; k++) s += D[k + i * n] * Y[k + j * n];
+        M[B.off + i + j * n] = s;
+      }
+    place_onebody(b, pos, states, B, M.data(), out);
+  }
+  IMSRG_CUDA_TRY(cudaMemcpyAsync(Op->d, out.data(), b->off_2b * sizeof(double), cudaMemcpyHostToDevice, st));
+  IMSRG_TRY(transform_2b(b, Op->d, Dsm, st));
+  // normal ordering with respect to the HF reference
+  return imsrg_gpu_normal_order(Op);
 }

@@ -38,7 +38,7 @@ SYMBOLS = (
     "imsrg_gpu_split_schedule", "imsrg_gpu_split_schedule_set", "imsrg_gpu_build_gs_atan", "imsrg_gpu_build_gs_w2", "imsrg_gpu_magnus_decouple_gen",
     "imsrg_gpu_op_save", "imsrg_gpu_op_load", "imsrg_gpu_checkpoint_name", "imsrg_gpu_normal_order",
     "imsrg_gpu_dhds", "imsrg_gpu_transform_bch", "imsrg_gpu_ode_decouple", "imsrg_gpu_commutator_host",
-    "imsrg_gpu_read_interaction", "imsrg_gpu_h0_harm_osc", "imsrg_gpu_hartree_fock",
+    "imsrg_gpu_read_interaction", "imsrg_gpu_h0_harm_osc", "imsrg_gpu_hartree_fock", "imsrg_gpu_transform_to_hf",
     "imsrg_gpu_batch_create", "imsrg_gpu_batch_commutator", "imsrg_gpu_batch_destroy",
 )
 
@@ -125,6 +125,7 @@ def lib():
             "imsrg_gpu_read_interaction": [vp, C.c_char_p, i, d, d, d, i],
             "imsrg_gpu_h0_harm_osc": [vp, i, d, d, d, i],
             "imsrg_gpu_hartree_fock": [vp, d, i, dp, ip, dp],
+            "imsrg_gpu_transform_to_hf": [vp, dp],
             "imsrg_gpu_batch_create": [i, C.POINTER(vp), C.POINTER(vp)],
             "imsrg_gpu_batch_commutator": [vp, C.POINTER(vp), C.POINTER(vp), C.POINTER(vp), i, i],
             "imsrg_gpu_batch_destroy": [vp],
@@ -577,6 +578,15 @@ def hartree_fock(H: Operator, tol: float = 1e-6, max_iter: int = 1000) -> dict:
     _check(lib().imsrg_gpu_hartree_fock(H.handle, float(tol), int(max_iter), C.byref(e), C.byref(it), _dp(D)),
            "hartree_fock")
     return {"e_hf": e.value, "iterations": it.value, "coefs": D.reshape(n, n, order="F")}
+
+
+def transform_to_hf(Op: Operator, coefs: np.ndarray):
+    """observable_to_HF for a scalar operator (HF_mod.f90:108-136): Op (HO
+    basis, not normal ordered, Hermitian) into the normal-ordered HF basis of
+    the coefficients a hartree_fock call returned, in place."""
+    D = np.ascontiguousarray(np.asarray(coefs, np.float64).reshape(-1, order="F") if np.ndim(coefs) == 2 else coefs,
+                             np.float64)
+    _check(lib().imsrg_gpu_transform_to_hf(Op.handle, _dp(D)), "transform_to_hf")
 
 
 def dhds(HS: Operator, DH: Operator, generator: str = "white", precision: str = "fp64"):

@@ -341,6 +341,12 @@ int imsrg_gpu_h0_harm_osc(imsrg_op_t *H, int htype, double hw, double com_hw, do
  * orbit a in HF orbit i (zero across blocks).  Density, Fock matrix,
  * diagonalisation and both transformations run on the GPU. */
 int imsrg_gpu_hartree_fock(imsrg_op_t *H, double tol, int max_iter, double *e_hf, int *iterations, double *coefs);
+/* observable_to_HF for a scalar operator (sqop_to_HF, HF_mod.f90:108-136):
+ * the Hermitian operator Op (one- and two-body parts in the HO basis, not
+ * normal ordered) is transformed with the HF coefficients coefs (norb x norb,
+ * as imsrg_gpu_hartree_fock returns them) and normal ordered with respect to
+ * the HF reference, in place. */
+int imsrg_gpu_transform_to_hf(imsrg_op_t *Op, const double *coefs);
 
 /* --- allocation-free commutator (no counterpart in the reference) --------
  * For callers that may not allocate device memory while they run: a host

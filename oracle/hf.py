@@ -315,6 +315,35 @@ class Setup:
         self._transform_2b(out, Dsm)
         return out, ehf, Dsm[1:, 1:], it
 
+    def transform_to_hf(self, Op, D):
+        """sqop_to_HF (HF_mod.f90:108-136) of a Hermitian scalar operator with
+        the coefficients D (norb x norb): one-body and two-body parts to the
+        HF basis, then normal ordering (the oracle's normal_order)."""
+        out = Op.copy()
+        out[self.off_fhh:self.off_fpp + self.P * self.P] = 0.0
+        for j, st in self.sp_blocks():
+            if not st:
+                continue
+            idx = np.array(st) - 1
+            X = np.array([[self.orc.f_elem(a, c, Op, 1) for c in st] for a in st])
+            Dq = D[np.ix_(idx, idx)]
+            X1 = Dq.T @ X @ Dq
+            for a in range(len(st)):
+                for c in range(a, len(st)):
+                    i, k = st[a], st[c]
+                    ci, ck = self.con[i - 1], self.con[k - 1]
+                    if ci == ck:
+                        out[self.f_index(i, k)] = X1[a, c]
+                        out[self.f_index(k, i)] = X1[a, c]
+                    elif ck > ci:
+                        out[self.f_index(i, k)] = X1[a, c]
+                    else:
+                        out[self.f_index(k, i)] = X1[c, a]
+        Dsm = np.zeros((self.N + 1, self.N + 1))
+        Dsm[1:, 1:] = D
+        self._transform_2b(out, Dsm)
+        return self.orc.normal_order(out, 1)
+
     def _transform_2b(self, H, Dsm):
         """transform_2b_to_HF (HF_mod.f90:494-619) in place."""
         jj = self.jj

@@ -117,3 +117,32 @@ def test_hartree_fock_not_converged(gpu_lib, oracle_mod, tmp_path):
     with pytest.raises(gpu_lib.ImsrgError) as e:
         gpu_lib.hartree_fock(H, tol=1e-6, max_iter=1)
     assert e.value.status == 4  # IMSRG_ERR_NOT_CONVERGED
+
+
+def test_transform_to_hf_matches_oracle_and_hf(gpu_lib, oracle_mod, tmp_path):
+    """observable_to_HF: a second Hermitian operator in the HF basis equals the
+    oracle's; the bare Hamiltonian transformed with the HF coefficients gives
+    back what hartree_fock left (two-body part bit for bit, E0 and the Fock
+    matrix to the convergence of the iteration)."""
+    from imsrg_gpu.synth import synth_hamiltonian
+    S, orc, lay, B = _both(gpu_lib, oracle_mod, 4)
+    path = str(tmp_path / "v.int")
+    _file(lay, path)
+    H = gpu_lib.Operator(B, 1)
+    gpu_lib.read_interaction(H, path, htype=1, hw=20.0, mass=16)
+    gpu_lib.h0_harm_osc(H, htype=1, hw=20.0, mass=16)
+    bare = H.download()
+    res = gpu_lib.hartree_fock(H, tol=1e-11)
+    hf = H.download()
+    X = gpu_lib.Operator(B, 1, bare)
+    gpu_lib.transform_to_hf(X, res["coefs"])
+    got = X.download()
+    two = lay.off_fpp + lay.P * lay.P
+    assert np.array_equal(got[two:], hf[two:])
+    assert got[0] == pytest.approx(hf[0], abs=1e-8)
+    assert np.max(np.abs(got[1:two] - hf[1:two])) <= 1e-8 * np.max(np.abs(hf))
+    obs = synth_hamiltonian(lay, 77, hw=0.0, sigma1=0.3, sigma2=0.2)  # some other Hermitian scalar operator
+    Y = gpu_lib.Operator(B, 1, obs)
+    gpu_lib.transform_to_hf(Y, res["coefs"])
+    ref = S.transform_to_hf(obs, res["coefs"])
+    assert rel_err(Y.download(), ref) <= 1e-11
