@@ -33,6 +33,7 @@ for _p in (ROOT, PKG):
 METRIC = "emax=6 [Ω,H] commutators/s, split-prec vs FP64 GPU at |ΔE0|<1e-6 MeV"
 UNIT = "commutators/s"
 EMAX = 6
+SPLIT_DIGITS = 5  # digits per operand of the split engine (set from --split-digits)
 
 
 def _workload_flops(lay):
@@ -223,6 +224,7 @@ def run_gpu(args, world, rank, local):
     orb = ho_basis(EMAX)
     lay = Layout(**orb)
     B = api.Basis.from_dict(orb)
+    B.set_split_digits(SPLIT_DIGITS)
     Hh, Oh = synth_hamiltonian(lay, 1 + rank), synth_omega(lay, 1 + rank)
     O, H, RES = api.Operator(B, -1, Oh), api.Operator(B, 1, Hh), api.Operator(B, 1)
     RES64 = api.Operator(B, 1)
@@ -373,7 +375,8 @@ def run_gpu(args, world, rank, local):
             "dtype": "f64" if precision == "fp64" else "bf16-slices/f64",
             "data": "synthetic (seeded HO basis, hw=20 MeV, N(0,1) MeV two-body, N(0,0.05) Omega)",
             "config": {"workload": "emax=6 [Omega,H] commutator, 16O, 56 j-orbits", "emax": EMAX,
-                       "precision": precision, "parallelism": f"replicas x{world}",
+                       "precision": precision, "split_digits": args.split_digits if precision == "ozaki" else None,
+                       "parallelism": f"replicas x{world}",
                        "l2": "flushed between timed steps (256 MiB write)", "nfull": lay.nfull},
             "roofline": roof, "e2e": e2e, "gpu_launches": launches, "clocks": clocks,
         }
@@ -383,7 +386,7 @@ def run_gpu(args, world, rank, local):
                                                "pinned": args.split_schedule is not None}
         line.update(extra)
         if not args.no_flows:
-            line["flow"] = flow_emax6(api, orb, lay)
+            line["flow"] = flow_emax6(api, orb, lay, args.split_digits)
             line["ode"] = ode_emax6(api, orb, lay)
             line["hartree_fock"] = hf_emax6(api, orb, lay)
             line["batch"] = batch_flows(api, args.batch)
@@ -400,14 +403,15 @@ def run_gpu(args, world, rank, local):
     return 0
 
 
-def flow_emax6(api, orb, lay):
+def flow_emax6(api, orb, lay, digits=5):
     """The emax = 6 Magnus flow to s = 50 (graph-captured steps) in split
     precision and in FP64: E0 difference, steps, commutators, wall time.
     The synthetic H is taken as already normal-ordered."""
     from imsrg_gpu.synth import synth_hamiltonian
     B = api.Basis.from_dict(orb)
+    B.set_split_digits(digits)
     Hh = synth_hamiltonian(lay, 13)
-    out = {"emax": EMAX, "s_max": 50.0, "ds": 0.5, "graph_steps": True}
+    out = {"emax": EMAX, "s_max": 50.0, "ds": 0.5, "graph_steps": True, "split_digits": digits}
     for prec in ("ozaki", "fp64"):
         HS, G = api.Operator(B, 1, Hh), api.Operator(B, -1)
         api.magnus_decouple_graph(HS, G, s_max=0.5, ds=0.5, precision=prec)  # builds the step graph
@@ -429,6 +433,7 @@ def ode_emax6(api, orb, lay):
     generator + one commutator each), wall time."""
     from imsrg_gpu.synth import synth_hamiltonian
     B = api.Basis.from_dict(orb)
+    B.set_split_digits(SPLIT_DIGITS)
     Hh = synth_hamiltonian(lay, 13)
     out = {"emax": EMAX, "ds": 0.1, "relerr": 1e-6, "abserr": 1e-6}
     for prec in ("ozaki", "fp64"):
@@ -454,6 +459,7 @@ def hf_emax6(api, orb, lay):
     V = synth_hamiltonian(lay, 13, sigma2=0.5)
     V[:lay.off_fpp + lay.P * lay.P] = 0.0
     B = api.Basis.from_dict(orb)
+    B.set_split_digits(SPLIT_DIGITS)
     with tempfile.TemporaryDirectory() as d:
         path = os.path.join(d, "v.int")
         nlines = write_vrenorm(lay, V, path, seed=13)
@@ -492,6 +498,7 @@ def batched_commutators(api, n=64, reps=20):
         orb = ho_basis(emax)
         lay = Layout(**orb)
         B = api.Basis.from_dict(orb)
+        B.set_split_digits(SPLIT_DIGITS)
         hw, sig = float(rng.uniform(12.0, 28.0)), float(rng.uniform(0.5, 2.0))
         bases.append(B)
         L.append(api.Operator(B, -1, synth_omega(lay, 2000 + k)))
@@ -540,6 +547,7 @@ def batch_flows(api, n):
         orb = ho_basis(emax)
         lay = Layout(**orb)
         B = api.Basis.from_dict(orb)
+        B.set_split_digits(SPLIT_DIGITS)
         hw, sig = float(rng.uniform(12.0, 28.0)), float(rng.uniform(0.5, 2.0))
         HS.append(api.Operator(B, 1, synth_hamiltonian(lay, 1000 + k, hw=hw, sigma2=sig)))
         G.append(api.Operator(B, -1))
@@ -602,6 +610,9 @@ def main():
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--no-flows", action="store_true", help="skip the flow and batched-flow extras")
     ap.add_argument("--batch", type=int, default=64, help="instances of the batched-flow extra")
+    ap.add_argument("--split-digits", type=int, default=5, choices=[4, 5, 6],
+                    help="digits per operand of the split engine (6: 21 BF16 products, 5: 15, 4: 10); "
+                         "five meets |dE0| < 1e-6 MeV by five orders of magnitude")
     ap.add_argument("--split-schedule", type=int, default=None,
                     help="pin the split engine's CTA schedule model instead of autotuning it "
                          "(for profiler runs, whose serialised launches distort the tuner's timings)")
@@ -609,6 +620,8 @@ def main():
                     help="only the batched-commutator extra with N instances (for profiling the grouped launch)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
+    global SPLIT_DIGITS
+    SPLIT_DIGITS = args.split_digits
     world, rank, local = dist_setup()
     if args.impl == "reference":
         return run_reference(args, world, rank)

@@ -1240,6 +1240,13 @@ int imsrg_gpu_split_schedule(imsrg_basis_t *b, int *choice, int *ncand, double *
   return imsrg::ozaki_schedule_info(b, choice, ncand, us, max);
 }
 
+int imsrg_gpu_split_digits_set(imsrg_basis_t *b, int digits) {
+  if (!b || digits < 4 || digits > 6) return IMSRG_ERR_INVALID;
+  if (b->ozaki) return digits == b->split_digits ? IMSRG_OK : IMSRG_ERR_INVALID;  // plan already built
+  b->split_digits = digits;
+  return IMSRG_OK;
+}
+
 int imsrg_gpu_split_schedule_set(imsrg_basis_t *b, int model) {
   if (!b) return IMSRG_ERR_INVALID;
   cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;

@@ -279,6 +279,7 @@ struct imsrg_basis {
   long launches = 0;
   // Ozaki split-precision engine state (allocated on first use)
   void *ozaki = nullptr;
+  int split_digits = 6;  // digits per operand of the split engine (4, 5 or 6), fixed once its plan exists
   // Graph of one Magnus flow step (graph.cu), built on first use
   void *flowgraph = nullptr;
   // Captured commutator launch sequences, one per argument set (api.cpp)
@@ -378,9 +379,10 @@ int ozaki_mma(imsrg_basis *b, int hL, int hR);
 int ozaki_check_error(imsrg_basis *b);  // IMSRG_ERR_TIMEOUT if a bounded device wait gave up
 bool ozaki_tuned(imsrg_basis *b);       // the CTA schedule has been autotuned
 // After a split-precision product WCC holds exact int64 level sums v with
-// WCC = v 2^k, k = (exps[g.x] - 1022) + (exps[g.y] - 1022) - 49 for the
-// groups g = ccgroups[q1] of cross-coupled block q1.
-int ozaki_wcc_scale(imsrg_basis *b, const int **exps, const int2 **ccgroups);
+// WCC = v 2^k, k = (exps[g.x] - 1022) + (exps[g.y] - 1022) - kshift for the
+// groups g = ccgroups[q1] of cross-coupled block q1 (kshift = 7 (S + 1) for S
+// digits: 49 with six, 42 with five).
+int ozaki_wcc_scale(imsrg_basis *b, const int **exps, const int2 **ccgroups, int *kshift);
 int ozaki_schedule_info(imsrg_basis *b, int *choice, int *ncand, double *us, int max);
 int ozaki_set_schedule(imsrg_basis *b, int model);  // pin one cost model, no timing
 void ozaki_free(imsrg_basis *b);

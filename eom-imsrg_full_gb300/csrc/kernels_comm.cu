@@ -185,11 +185,12 @@ __device__ __forceinline__ long long wcc_at_int(const long long *W, int rlen, un
 
 // Recoupling inputs Z of commutator_222_ph, one thread per PhTerm.  With
 // exps == nullptr WCC holds FP64 (the FP64 path); otherwise it holds the
-// split engine's exact int64 level sums, WCC = v 2^k per cross-coupled block,
+// split engine's exact int64 level sums, WCC = v 2^k per cross-coupled block
+// (k = both block exponents - kshift, kshift = 7 x the highest level kept),
 // and the four entries are combined exactly in int64 before one conversion.
 __global__ void __launch_bounds__(256) k_ph_inputs(DevTables T, const double *__restrict__ WCC, int hL, int hR,
                                                    const int *__restrict__ exps, const int2 *__restrict__ ccg,
-                                                   double *__restrict__ Z) {
+                                                   int kshift, double *__restrict__ Z) {
   const long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= T.n_ph) return;
   const PhTerm p = T.ph_terms[t];
@@ -204,7 +205,7 @@ __global__ void __launch_bounds__(256) k_ph_inputs(DevTables T, const double *__
     const long long c = (p.nph ? -w3 : w3) + wcc_at_int(W, rl, y1, x1);
     const long long z = (hL < 0 ? -a : a) - (hR < 0 ? -c : c);
     const int2 g = ccg[p.qx];
-    const int k = (exps[g.x] - 1022) + (exps[g.y] - 1022) - 49;
+    const int k = (exps[g.x] - 1022) + (exps[g.y] - 1022) - kshift;
     // z 2^k: add k to the exponent field on the integer pipe when the result
     // stays normal (exactly ldexp's value), else ldexp
     double d = (double)z;
@@ -620,10 +621,11 @@ int launch_gemm_fp64(imsrg_basis *b, const double *L, int hL, const double *R, i
 int launch_ph_inputs(imsrg_basis *b, int hL, int hR, int precision) {
   const int *exps = nullptr;
   const int2 *ccg = nullptr;
-  if (precision == IMSRG_PREC_OZAKI) IMSRG_TRY(ozaki_wcc_scale(b, &exps, &ccg));
+  int kshift = 0;
+  if (precision == IMSRG_PREC_OZAKI) IMSRG_TRY(ozaki_wcc_scale(b, &exps, &ccg, &kshift));
   if (b->T.n_ph > 0) {
     k_ph_inputs<<<(unsigned)((b->T.n_ph + 255) / 256), 256, 0, b->stream>>>(b->T, b->wcc, hL, hR, exps, ccg,
-                                                                            b->zph);
+                                                                            kshift, b->zph);
     b->launches++;
   }
   return cuda_status(cudaGetLastError());
@@ -697,7 +699,7 @@ int launch_commutator_fp64_ws(imsrg_basis *b, const Workspace &ws, const double 
   }
   if (b->T.n_ph > 0) {
     k_ph_inputs<<<(unsigned)((b->T.n_ph + 255) / 256), 256, 0, st>>>(b->T, ws.wcc, hL, hR, nullptr, nullptr,
-                                                                       ws.zph);
+                                                                       0, ws.zph);
     b->launches++;
   }
   const long n2 = b->T.n_asm2;

@@ -57,10 +57,15 @@ namespace imsrg {
 
 namespace {
 
-constexpr int OZ_S = 6;                      // digits (slices) per operand
-constexpr int OZ_LMAX = OZ_S + 1;            // highest level kept
-constexpr int OZ_NACC = 4;                   // accumulators: levels 2, 3, 4 exact + FP32 tail of 5..7
-constexpr int OZ_BPLANES = 15;               // B planes: d_1..d_6, 2^7 d_1..d_5, 2^14 d_1..d_4
+// S digits (slices) per operand, S = 6 (default), 5 or 4.  Levels l = s + t
+// up to S + 1 are kept; levels 2, 3, 4 have exact accumulators and the levels
+// 5..S+1 share an FP32 tail accumulator in units of level S + 1, with B planes
+// pre-scaled by 2^(7 j), j = S + 1 - l: d_1..d_S (j = 0), 2^7 d_1..d_{S-1}
+// (j = 1, S >= 5) and 2^14 d_1..d_4 (j = 2, S = 6).
+constexpr int OZ_SMAX = 6;
+constexpr int OZ_NACC = 4;                   // accumulators: levels 2, 3, 4 exact + FP32 tail
+__host__ __device__ constexpr int oz_bplanes(int S) { return S == 6 ? 15 : S == 5 ? 9 : 4; }
+__host__ __device__ constexpr int oz_plane_off(int S, int j) { return j == 0 ? 0 : j == 1 ? S : 2 * S - 1; }
 constexpr int TM = 128, TN = 64, TK = 16;
 constexpr int STAGES = 4;
 // Lines (8 elements each) per slicing CTA: small CTAs spread the ~100,000
@@ -70,7 +75,8 @@ constexpr int STAGES = 4;
 constexpr int SLICE_THREADS = 128;
 constexpr int A_SLICE_BYTES = TM * TK * 2;   // 4096
 constexpr int B_SLICE_BYTES = TN * TK * 2;   // 2048
-constexpr int STAGE_BYTES = OZ_S * A_SLICE_BYTES + OZ_BPLANES * B_SLICE_BYTES;
+__host__ __device__ constexpr int oz_stage_bytes(int S) { return S * A_SLICE_BYTES + oz_bplanes(S) * B_SLICE_BYTES; }
+__host__ __device__ constexpr int oz_mma_smem(int S) { return STAGES * oz_stage_bytes(S) + 1024 + 256; }
 constexpr int TMEM_COLS = 512;
 constexpr int EPI_WARPS = 16;                // one per (TMEM lane quadrant, 16-column chunk)
 constexpr int OZ_THREADS = 32 * (2 + EPI_WARPS);  // warp 0 producer, 1 MMA, 2-17 epilogue
@@ -86,7 +92,7 @@ struct OzMatrix {
   long img_c;      // byte offset of the C image (rows n2, K = n1), -1 when no problem reads it
   int rg_r, rg_c;  // row groups (of 8 rows) of each image
   long plane_r, plane_c;  // bytes per digit plane
-  int np_r, np_c;         // digit planes stored: 6 (A role only) or 15 (B role: with the scaled tail planes)
+  int np_r, np_c;         // digit planes stored: S (A role only) or oz_bplanes(S) (B role: with the scaled tail planes)
   int line_r0, line_c0;   // first line of this matrix in the R / C slicing grids
 };
 
@@ -124,6 +130,7 @@ constexpr int kNumSchedModels = 5;
 constexpr SchedModel kSchedModels[kNumSchedModels] = {{4, 20, 4}, {4, 0, 1}, {4, 10, 2}, {4, 40, 4}, {1, 40, 8}};
 
 struct OzPlan {
+  int S = OZ_SMAX;  // digits per operand
   std::vector<OzMatrix> mats;
   std::vector<OzChunk> chunks;
   std::vector<OzProb> probs;
@@ -287,22 +294,23 @@ __global__ void __launch_bounds__(256) k_oz_exponents(const OzChunk *chunks, con
 // ---------------------------------------------------------------------------
 // 2. digit slicing: one thread per 8-element line of a core matrix
 // ---------------------------------------------------------------------------
-// Digits of x with |x| < 2^e: x = 2^(e-42) sum_{s} d_s 128^(5-s), d_0 first.
-// One 64-bit shift rounds |x| to the 42-bit integer V; the balanced base-128
-// digits then come from its two 21-bit halves on the 32-bit integer pipe.
-__device__ __forceinline__ void digits6(double x, int e, int *d) {
+// Digits of x with |x| < 2^e: x = 2^(e-7S) sum_{s} d_s 128^(S-1-s), d_0 first.
+// One 64-bit shift rounds |x| to the 7S-bit integer V; the balanced base-128
+// digits then come from its low 21 bits and the rest on the 32-bit integer pipe.
+template <int S>
+__device__ __forceinline__ void digits(double x, int e, int *d) {
   const unsigned long long bits = (unsigned long long)__double_as_longlong(x);
   const int E = (int)((bits >> 52) & 0x7FF);
   const int neg = (int)(bits >> 63);
   unsigned long long V = 0;
   if (E != 0) {
     const unsigned long long mant = (bits & ((1ull << 52) - 1)) | (1ull << 52);
-    const int rs = e + 1033 - E;  // V = round(|x| 2^(42 - e)), rs >= 11
+    const int rs = e + 1075 - 7 * S - E;  // V = round(|x| 2^(7S - e)), rs >= 11
     if (rs <= 63) V = (mant + (1ull << (rs - 1))) >> rs;
   }
   unsigned lo = (unsigned)(V & 0x1FFFFFu), hi = (unsigned)(V >> 21);
 #pragma unroll
-  for (int s = OZ_S - 1; s >= 3; s--) {
+  for (int s = S - 1; s >= S - 3; s--) {
     int u = (int)(lo & 127u);
     lo >>= 7;
     if (u >= 64) {
@@ -313,7 +321,7 @@ __device__ __forceinline__ void digits6(double x, int e, int *d) {
   }
   hi += lo;  // carry out of the low half
 #pragma unroll
-  for (int s = 2; s >= 1; s--) {
+  for (int s = S - 4; s >= 1; s--) {
     int u = (int)(hi & 127u);
     hi >>= 7;
     if (u >= 64) {
@@ -330,6 +338,7 @@ __device__ __forceinline__ void digits6(double x, int e, int *d) {
 // plane); the other CTAs write R-image lines [r_lo, r_hi) (8 consecutive
 // columns of one row).  blk_mat[b] is the matrix of CTA b's first line.  Padding lines of the images are never
 // written and stay zero.
+template <int S>
 __global__ void __launch_bounds__(SLICE_THREADS) k_oz_slice(const OzMatrix *__restrict__ mats, int nmats,
                                                   const int *__restrict__ blk_mat, int cblocks, int c_lo, int c_hi,
                                                   int r_lo, int r_hi, const double *L, const double *R, const double *LCC,
@@ -377,22 +386,23 @@ __global__ void __launch_bounds__(SLICE_THREADS) k_oz_slice(const OzMatrix *__re
     plane = m.plane_r;
   }
   const int nplanes = cimg ? m.np_c : m.np_r;
-  uint32_t h[8][OZ_S];  // BF16 bits of each digit
+  uint32_t h[8][S];  // BF16 bits of each digit
 #pragma unroll
   for (int i = 0; i < 8; i++) {
-    int d[OZ_S];
-    digits6(x[i], e, d);
+    int d[S];
+    digits<S>(x[i], e, d);
 #pragma unroll
-    for (int s = 0; s < OZ_S; s++) h[i][s] = tab[d[s] + 128];
+    for (int s = 0; s < S; s++) h[i][s] = tab[d[s] + 128];
   }
-  // plane k: digit s = k (k < 6), 2^7 d_{k-6} (6 <= k < 11), 2^14 d_{k-11}
-  // (k >= 11): the scaled planes add 7 or 14 to the BF16 exponent of every
-  // non-zero digit, all exact
+  // plane k: digit s = k (k < S), 2^7 d_{k-S} (S <= k < 2S - 1), 2^14
+  // d_{k-2S+1} (k >= 2S - 1): the scaled planes add 7 or 14 to the BF16
+  // exponent of every non-zero digit, all exact
+  constexpr int P1 = oz_plane_off(S, 1), P2 = oz_plane_off(S, 2);
 #pragma unroll
-  for (int k = 0; k < OZ_BPLANES; k++) {
+  for (int k = 0; k < oz_bplanes(S); k++) {
     if (k >= nplanes) break;
-    const int s = k < 6 ? k : k < 11 ? k - 6 : k - 11;
-    const uint32_t add = k < 6 ? 0u : k < 11 ? (7u << 7) : (14u << 7);
+    const int s = k < P1 ? k : k < P2 ? k - P1 : k - P2;
+    const uint32_t add = k < P1 ? 0u : k < P2 ? (7u << 7) : (14u << 7);
     uint32_t w4[4];
 #pragma unroll
     for (int i = 0; i < 8; i += 2) {
@@ -407,6 +417,7 @@ __global__ void __launch_bounds__(SLICE_THREADS) k_oz_slice(const OzMatrix *__re
 // 3. tensor-core products and exact recombination
 // ---------------------------------------------------------------------------
 
+template <int S>
 __global__ void __launch_bounds__(OZ_THREADS, 1) k_oz_mma(const OzProb *__restrict__ probs, int nprobs,
                                                           const int2 *__restrict__ sched,
                                                           const int *__restrict__ sched_off,
@@ -414,6 +425,7 @@ __global__ void __launch_bounds__(OZ_THREADS, 1) k_oz_mma(const OzProb *__restri
                                                           const CUtensorMap *__restrict__ maps) {
   extern __shared__ __align__(1024) uint8_t smem_raw[];
   uint8_t *smem = (uint8_t *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+  constexpr int STAGE_BYTES = oz_stage_bytes(S), LMAX = S + 1;
   uint64_t *full = (uint64_t *)(smem + STAGES * STAGE_BYTES);
   uint64_t *empty = full + STAGES;
   uint64_t *acc_full = empty + STAGES;   // [2]
@@ -474,7 +486,7 @@ __global__ void __launch_bounds__(OZ_THREADS, 1) k_oz_mma(const OzProb *__restri
             // accumulator rows and columns that are never stored
             mbar_expect_tx(&full[stage], STAGE_BYTES);
             uint8_t *sa = smem + stage * STAGE_BYTES;
-            uint8_t *sb = sa + OZ_S * A_SLICE_BYTES;
+            uint8_t *sb = sa + S * A_SLICE_BYTES;
             tma_load_3d(sa, amap, kk * T.a_rg + tm * (TM / 8), 0, &full[stage]);
             tma_load_3d(sb, bmap, kk * T.b_rg + tn * (TN / 8), 0, &full[stage]);
             if (++stage == STAGES) {
@@ -521,23 +533,23 @@ __global__ void __launch_bounds__(OZ_THREADS, 1) k_oz_mma(const OzProb *__restri
             tc_fence_after();
             // descriptor start-address fields advance in 16-byte units
             const uint64_t da = desc0 + (uint64_t)((stage * STAGE_BYTES) >> 4);
-            const uint64_t db = da + (uint64_t)((OZ_S * A_SLICE_BYTES) >> 4);
+            const uint64_t db = da + (uint64_t)((S * A_SLICE_BYTES) >> 4);
 #pragma unroll
-            for (int s = 0; s < OZ_S; s++) {
+            for (int s = 0; s < S; s++) {
               // level l = s + u + 2 (digits are 1-based).  Levels 2..4 have
               // their own accumulators, side by side in TMEM, and B planes
               // u = 0, 1, 2 lie side by side in the stage: the exact products
               // of A plane s are one MMA of width (3 - s) x 64 into
               // accumulators s..2 (s <= 2).  Levels 5..7 share the tail
-              // accumulator, with B pre-scaled by 2^(7 (7 - l)).  The first
+              // accumulator, with B pre-scaled by 2^(7 (S + 1 - l)).  The first
               // product into every accumulator of a tile overwrites it.
               if (s <= 2)
                 mma_bf16(dbase + (uint32_t)(s * TN), da + (uint64_t)(s * (A_SLICE_BYTES >> 4)), db,
                          s == 0 ? idesc3 : s == 1 ? idesc2 : idesc, (first && s == 0) ? 0 : 1);
 #pragma unroll
-              for (int u = s <= 2 ? 3 - s : 0; u < OZ_S - s; u++) {
+              for (int u = s <= 2 ? 3 - s : 0; u < S - s; u++) {
                 const int lvl = s + u + 2;
-                const int bp = lvl == 7 ? u : lvl == 6 ? 6 + u : 11 + u;
+                const int bp = oz_plane_off(S, LMAX - lvl) + u;
                 mma_bf16(dbase + (uint32_t)(3 * TN), da + (uint64_t)(s * (A_SLICE_BYTES >> 4)),
                          db + (uint64_t)(bp * (B_SLICE_BYTES >> 4)), idesc, (first && s == 0 && u == 3) ? 0 : 1);
               }
@@ -610,24 +622,24 @@ __global__ void __launch_bounds__(OZ_THREADS, 1) k_oz_mma(const OzProb *__restri
         long long *irow = reinterpret_cast<long long *>(crow);
 #pragma unroll
         for (int c = 0; c < 16; c++) {
-          const long long v = ((long long)__float2int_rn(__uint_as_float(acc[0][c])) << 35) +
-                              ((long long)__float2int_rn(__uint_as_float(acc[1][c])) << 28) +
-                              ((long long)__float2int_rn(__uint_as_float(acc[2][c])) << 21) +
+          const long long v = ((long long)__float2int_rn(__uint_as_float(acc[0][c])) << (7 * (LMAX - 2))) +
+                              ((long long)__float2int_rn(__uint_as_float(acc[1][c])) << (7 * (LMAX - 3))) +
+                              ((long long)__float2int_rn(__uint_as_float(acc[2][c])) << (7 * (LMAX - 4))) +
                               __float2ll_rn(__uint_as_float(acc[3][c]));
           const int n = n0 + c;
           if (row_ok && n < Np) irow[(long)n * ldc] = v;
         }
         continue;
       }
-      const int k = (exps[gA] - 1022) + (exps[gB] - 1022) - 7 * OZ_LMAX;  // result = v * 2^k
+      const int k = (exps[gA] - 1022) + (exps[gB] - 1022) - 7 * LMAX;  // result = v * 2^k
 #pragma unroll
       for (int c = 0; c < 16; c++) {
-        // exact integer levels 2..4 and the rounded tail, in units of level 7
+        // exact integer levels 2..4 and the rounded tail, in units of level S + 1
         // (hardware conversions: measured faster here than assembling the
         // double from integer bit operations)
-        long long v = ((long long)__float2int_rn(__uint_as_float(acc[0][c])) << 35) +
-                      ((long long)__float2int_rn(__uint_as_float(acc[1][c])) << 28) +
-                      ((long long)__float2int_rn(__uint_as_float(acc[2][c])) << 21) +
+        long long v = ((long long)__float2int_rn(__uint_as_float(acc[0][c])) << (7 * (LMAX - 2))) +
+                      ((long long)__float2int_rn(__uint_as_float(acc[1][c])) << (7 * (LMAX - 3))) +
+                      ((long long)__float2int_rn(__uint_as_float(acc[2][c])) << (7 * (LMAX - 4))) +
                       __float2ll_rn(__uint_as_float(acc[3][c]));
         double d = (double)v;
         // scale by 2^k: add k to the exponent field on the integer pipe
@@ -653,6 +665,16 @@ __global__ void __launch_bounds__(OZ_THREADS, 1) k_oz_mma(const OzProb *__restri
 }
 
 OzPlan *plan_of(imsrg_basis *b) { return (OzPlan *)b->ozaki; }
+
+void launch_mma(int S, int grid, cudaStream_t st, const OzProb *probs, int nprobs, const int2 *sched,
+                const int *sched_off, const int *exps, int hL, int hR, int *err, const CUtensorMap *maps) {
+  if (S == 4)
+    k_oz_mma<4><<<grid, OZ_THREADS, oz_mma_smem(4), st>>>(probs, nprobs, sched, sched_off, exps, hL, hR, err, maps);
+  else if (S == 5)
+    k_oz_mma<5><<<grid, OZ_THREADS, oz_mma_smem(5), st>>>(probs, nprobs, sched, sched_off, exps, hL, hR, err, maps);
+  else
+    k_oz_mma<6><<<grid, OZ_THREADS, oz_mma_smem(6), st>>>(probs, nprobs, sched, sched_off, exps, hL, hR, err, maps);
+}
 
 // CTA schedule: longest-processing-time-first assignment of tiles to the
 // persistent CTAs under the cost model cost = kw * (K steps x terms) + ew *
@@ -700,14 +722,13 @@ int use_model(imsrg_basis *b, OzPlan *pl, int c) {
 // fastest is kept.  The kernel is deterministic per tile, so the schedule
 // never changes results.
 int autotune(imsrg_basis *b, OzPlan *pl, int hL, int hR) {
-  const int smem = STAGES * STAGE_BYTES + 1024 + 256;
   cudaEvent_t e0 = nullptr, e1 = nullptr;
   IMSRG_CUDA_TRY(cudaEventCreate(&e0));
   IMSRG_CUDA_TRY(cudaEventCreate(&e1));
   auto launch_timed = [&](float *ms) -> int {
     IMSRG_CUDA_TRY(cudaEventRecord(e0, b->stream));
-    k_oz_mma<<<pl->grid, OZ_THREADS, smem, b->stream>>>(pl->d_probs, pl->nprobs, pl->d_sched, pl->d_sched_off,
-                                                       pl->d_exps, hL, hR, pl->d_err, pl->d_maps);
+    launch_mma(pl->S, pl->grid, b->stream, pl->d_probs, pl->nprobs, pl->d_sched, pl->d_sched_off, pl->d_exps, hL, hR,
+               pl->d_err, pl->d_maps);
     b->launches++;
     IMSRG_CUDA_TRY(cudaEventRecord(e1, b->stream));
     IMSRG_CUDA_TRY(cudaEventSynchronize(e1));
@@ -746,6 +767,8 @@ int ozaki_prepare(imsrg_basis *b) {
   if (b->ozaki) return plan_of(b)->ok ? IMSRG_OK : IMSRG_ERR_INVALID;
   OzPlan *pl = new OzPlan();
   b->ozaki = pl;
+  pl->S = b->split_digits;
+  if (pl->S < 4 || pl->S > 6) return IMSRG_ERR_INVALID;
   int dev = b->device, major = 0, nsm = 0;
   IMSRG_CUDA_TRY(cudaDeviceGetAttribute(&major, cudaDevAttrComputeCapabilityMajor, dev));
   IMSRG_CUDA_TRY(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
@@ -826,7 +849,7 @@ int ozaki_prepare(imsrg_basis *b) {
     if (role_r[i]) {
       m.rg_r = (m.n1 + 7) / 8;
       m.plane_r = (long)m.rg_r * ((m.n2 + 15) / 16) * 256;
-      m.np_r = b_role_r[i] ? OZ_BPLANES : OZ_S;
+      m.np_r = b_role_r[i] ? oz_bplanes(pl->S) : pl->S;
       m.img_r = imgb[m.src];
       imgb[m.src] += m.np_r * m.plane_r;
       lines_r += ((m.n2 + 7) / 8) * m.n1;
@@ -834,7 +857,7 @@ int ozaki_prepare(imsrg_basis *b) {
     if (role_c[i]) {
       m.rg_c = (m.n2 + 7) / 8;
       m.plane_c = (long)m.rg_c * ((m.n1 + 15) / 16) * 256;
-      m.np_c = b_role_c[i] ? OZ_BPLANES : OZ_S;
+      m.np_c = b_role_c[i] ? oz_bplanes(pl->S) : pl->S;
       m.img_c = imgb[m.src];
       imgb[m.src] += m.np_c * m.plane_c;
       lines_c += ((m.n1 + 7) / 8) * m.n2;
@@ -904,7 +927,7 @@ int ozaki_prepare(imsrg_basis *b) {
       *idx = it->second;
       return IMSRG_OK;
     }
-    const cuuint32_t box_planes = brole ? OZ_BPLANES : OZ_S;
+    const cuuint32_t box_planes = brole ? oz_bplanes(pl->S) : pl->S;
     if (plane <= 0 || plane % 256 || (long)np < (long)box_planes) return IMSRG_ERR_INVALID;
     CUtensorMap m;
     const cuuint64_t gdim[3] = {32, (cuuint64_t)(plane / 256), (cuuint64_t)np};
@@ -1003,8 +1026,12 @@ int ozaki_prepare(imsrg_basis *b) {
   IMSRG_CUDA_TRY(cudaMalloc((void **)&pl->d_exps, std::max(pl->ngroups, 1) * sizeof(int)));
   IMSRG_CUDA_TRY(cudaMalloc((void **)&pl->d_err, sizeof(int)));
   IMSRG_CUDA_TRY(cudaMemset(pl->d_err, 0, sizeof(int)));
-  int smem = STAGES * STAGE_BYTES + 1024 + 256;
-  IMSRG_CUDA_TRY(cudaFuncSetAttribute(k_oz_mma, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+  IMSRG_CUDA_TRY(pl->S == 4   ? cudaFuncSetAttribute(k_oz_mma<4>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                     oz_mma_smem(4))
+                 : pl->S == 5 ? cudaFuncSetAttribute(k_oz_mma<5>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                     oz_mma_smem(5))
+                              : cudaFuncSetAttribute(k_oz_mma<6>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                     oz_mma_smem(6)));
 
   int herr = 0;
   IMSRG_CUDA_TRY(cudaMemcpy(&herr, pl->d_err, sizeof(int), cudaMemcpyDeviceToHost));
@@ -1039,7 +1066,7 @@ int ozaki_slice(imsrg_basis *b, const double *L, const double *R, int part, cuda
   }
   const int nblk = pl->cblocks[part] + pl->rblocks[part];
   if (nblk) {
-    k_oz_slice<<<nblk, SLICE_THREADS, 0, st>>>(pl->d_mats, pl->nmats, pl->d_blk_mat + pl->blk_off[part], pl->cblocks[part],
+    (pl->S == 4 ? k_oz_slice<4> : pl->S == 5 ? k_oz_slice<5> : k_oz_slice<6>)<<<nblk, SLICE_THREADS, 0, st>>>(pl->d_mats, pl->nmats, pl->d_blk_mat + pl->blk_off[part], pl->cblocks[part],
                                      pl->linec_lo[part], pl->linec_lo[part + 1], pl->liner_lo[part],
                                      pl->liner_lo[part + 1], L, R, b->lcc, b->rcc, pl->d_exps, pl->img[0],
                                      pl->img[1], pl->img[2], pl->img[3]);
@@ -1057,9 +1084,8 @@ int ozaki_mma(imsrg_basis *b, int hL, int hR) {
     if (cs == cudaStreamCaptureStatusNone) IMSRG_TRY(autotune(b, pl, hL, hR));
   }
   ProfScope ps(b, IMSRG_KERNEL_OZAKI_MMA);
-  const int smem = STAGES * STAGE_BYTES + 1024 + 256;
-  k_oz_mma<<<pl->grid, OZ_THREADS, smem, b->stream>>>(pl->d_probs, pl->nprobs, pl->d_sched, pl->d_sched_off,
-                                                     pl->d_exps, hL, hR, pl->d_err, pl->d_maps);
+  launch_mma(pl->S, pl->grid, b->stream, pl->d_probs, pl->nprobs, pl->d_sched, pl->d_sched_off, pl->d_exps, hL, hR,
+             pl->d_err, pl->d_maps);
   b->launches++;
   return cuda_status(cudaGetLastError());
 }
@@ -1077,11 +1103,12 @@ int ozaki_check_error(imsrg_basis *b) {
   return IMSRG_OK;
 }
 
-int ozaki_wcc_scale(imsrg_basis *b, const int **exps, const int2 **ccgroups) {
+int ozaki_wcc_scale(imsrg_basis *b, const int **exps, const int2 **ccgroups, int *kshift) {
   OzPlan *pl = plan_of(b);
   if (!pl || !pl->ok) return IMSRG_ERR_INVALID;
   *exps = pl->d_exps;
   *ccgroups = pl->d_ccgroups;
+  *kshift = 7 * (pl->S + 1);
   return IMSRG_OK;
 }
 
@@ -1161,6 +1188,7 @@ int ozaki_batch_create(imsrg_basis *const *bases, int n, void **out) {
     OzPlan *pl = plan_of(bases[i]);
     if (!pl || !pl->ok || bases[i]->device != bases[0]->device) return fail(IMSRG_ERR_INVALID);
     bt->plans.push_back(pl);
+    if (pl->S != bt->plans[0]->S) return fail(IMSRG_ERR_INVALID);  // one digit count per merged launch
     bt->exps_base.push_back(bt->ngroups);
     const int p0 = (int)probs.size(), m0 = (int)maps.size();
     for (const OzProb &p : pl->probs) {
@@ -1218,9 +1246,8 @@ int ozaki_batch_mma(void *batch, cudaStream_t st, int hL, int hR) {
     if (bt->plans[i]->ngroups > 0)
       IMSRG_CUDA_TRY(cudaMemcpyAsync(bt->d_exps + bt->exps_base[i], bt->plans[i]->d_exps,
                                      bt->plans[i]->ngroups * sizeof(int), cudaMemcpyDeviceToDevice, st));
-  const int smem = STAGES * STAGE_BYTES + 1024 + 256;
-  k_oz_mma<<<bt->grid, OZ_THREADS, smem, st>>>(bt->d_probs, bt->nprobs, bt->d_sched, bt->d_sched_off, bt->d_exps,
-                                               hL, hR, bt->d_err, bt->d_maps);
+  launch_mma(bt->plans[0]->S, bt->grid, st, bt->d_probs, bt->nprobs, bt->d_sched, bt->d_sched_off, bt->d_exps, hL,
+             hR, bt->d_err, bt->d_maps);
   return cuda_status(cudaGetLastError());
 }
 

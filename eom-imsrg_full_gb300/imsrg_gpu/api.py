@@ -35,7 +35,7 @@ SYMBOLS = (
     "imsrg_gpu_basis_get_stream", "imsrg_gpu_basis_set_stream", "imsrg_gpu_profile_enable",
     "imsrg_gpu_profile_read", "imsrg_gpu_profile_reset", "imsrg_gpu_commutator_noalloc",
     "imsrg_gpu_magnus_decouple_graph", "imsrg_gpu_magnus_decouple_batch", "imsrg_gpu_magnus_decouple_tangent",
-    "imsrg_gpu_split_schedule", "imsrg_gpu_split_schedule_set", "imsrg_gpu_build_gs_atan", "imsrg_gpu_build_gs_w2", "imsrg_gpu_magnus_decouple_gen",
+    "imsrg_gpu_split_schedule", "imsrg_gpu_split_schedule_set", "imsrg_gpu_split_digits_set", "imsrg_gpu_build_gs_atan", "imsrg_gpu_build_gs_w2", "imsrg_gpu_magnus_decouple_gen",
     "imsrg_gpu_op_save", "imsrg_gpu_op_load", "imsrg_gpu_checkpoint_name", "imsrg_gpu_normal_order",
     "imsrg_gpu_dhds", "imsrg_gpu_transform_bch", "imsrg_gpu_ode_decouple", "imsrg_gpu_commutator_host",
     "imsrg_gpu_read_interaction", "imsrg_gpu_h0_harm_osc", "imsrg_gpu_hartree_fock", "imsrg_gpu_transform_to_hf",
@@ -112,6 +112,7 @@ def lib():
             "imsrg_gpu_magnus_decouple_tangent": [vp, vp, vp, vp, d, d, i, i, dp, dp, ip, ip],
             "imsrg_gpu_split_schedule": [vp, ip, ip, dp, i],
             "imsrg_gpu_split_schedule_set": [vp, i],
+            "imsrg_gpu_split_digits_set": [vp, i],
             "imsrg_gpu_build_gs_atan": [vp, vp],
             "imsrg_gpu_build_gs_w2": [vp, vp, i],
             "imsrg_gpu_magnus_decouple_gen": [vp, vp, i, d, d, i, i, dp, ip, ip],
@@ -232,6 +233,13 @@ class Basis:
         timing (e.g. under a profiler whose serialised launches distort the
         autotuner's event timings); results do not depend on the schedule."""
         _check(lib().imsrg_gpu_split_schedule_set(self._h, int(model)), "split_schedule_set")
+
+    def set_split_digits(self, digits: int):
+        """Digits per operand of the split engine on this basis: 6 (default,
+        21 BF16 products), 5 (15 products) or 4 (10 products); each digit
+        fewer multiplies the truncation bound by 128.  Only before the basis'
+        first split-precision call."""
+        _check(lib().imsrg_gpu_split_digits_set(self._h, int(digits)), "split_digits_set")
 
     def block_dims(self, q):
         a, b, c = C.c_int(), C.c_int(), C.c_int()

@@ -263,6 +263,12 @@ int imsrg_gpu_split_schedule(imsrg_basis_t *b, int *choice, int *ncand, double *
  * the kernel alone, such as under a profiler that serialises launches.  The
  * schedule never changes results.  Allocates and synchronises on first use. */
 int imsrg_gpu_split_schedule_set(imsrg_basis_t *b, int model);
+/* Digits per operand of IMSRG_PREC_OZAKI on this basis (no reference
+ * counterpart): 6 (the default; 21 BF16 products per term, about 2^-42
+ * K max|A| max|B| from the exact product), 5 (15 products, about 2^-35
+ * K max|A| max|B|) or 4 (10 products, about 2^-28 K max|A| max|B|).  Only before the basis' first split-precision call; later
+ * it accepts the current count only (IMSRG_ERR_INVALID otherwise). */
+int imsrg_gpu_split_digits_set(imsrg_basis_t *b, int digits);
 
 const char *imsrg_gpu_strerror(int status);
 /* Number of library kernel launches issued so far on this basis. */
