@@ -314,6 +314,8 @@ def run_gpu(args, world, rank, local):
     bf16_peak = peaks.get("bf16_tflops", 1951.5)
     comp = _compulsory_bytes(lay)
     alg_flops = _workload_flops(lay) + _cc_flops(orb)
+    # the split engine keeps digit products d_s d_t with s + t <= S + 1
+    nprod = SPLIT_DIGITS * (SPLIT_DIGITS + 1) // 2
 
     def roof_of(k, per):
         """One class against its bound: the contraction kernel against the
@@ -321,11 +323,12 @@ def run_gpu(args, world, rank, local):
         FP64-equivalent algorithmic flops beside them), the gather kernels
         against HBM with the compulsory bytes of one commutator."""
         if k.startswith("ozaki_mma"):
-            return {"bound": "tensor", "achieved": 21 * alg_flops / per / 1e12, "peak": bf16_peak,
+            return {"bound": "tensor", "achieved": nprod * alg_flops / per / 1e12, "peak": bf16_peak,
                     "unit": "TFLOP/s", "peak_source": "MEASURED_PEAKS.json bf16_tflops (of measured)",
                     "achieved_fp64_equiv_tflops": alg_flops / per / 1e12,
-                    "algorithmic_per_launch": 21 * alg_flops,
-                    "work_note": "executed BF16 flops = 21 digit products x 5.83e8 FP64-equivalent flop"}
+                    "algorithmic_per_launch": nprod * alg_flops,
+                    "work_note": f"executed BF16 flops = {nprod} digit products (S(S+1)/2, S = {SPLIT_DIGITS} "
+                                 f"digits) x {alg_flops:.3e} FP64-equivalent flop"}
         if k == "gemm_fp64":
             return {"bound": "fp64", "achieved": alg_flops / per / 1e12, "peak": _fp64_peak_tflops(),
                     "unit": "TFLOP/s", "peak_source": "cuBLAS DGEMM 8192^3 measured in this run (FP64 pipe)",
@@ -348,6 +351,17 @@ def run_gpu(args, world, rank, local):
                                   prof[k][1] / n_prof, "achieved": r["achieved"], "unit": r["unit"],
                                   "frac": r["achieved"] / r["peak"], "traffic": _traffic_from_profiles(k)}
     roof["kernel_share"] = {k: round(v / max(sum(per_comm.values()), 1e-12), 4) for k, v in per_comm.items()}
+    if precision != "fp64":
+        # the FP64 arm's classes (the denominator of split vs FP64): its
+        # contraction kernel against the live cuBLAS DGEMM rate
+        n_prof64 = min(n64, 200)
+        per64 = {k: (ms_k / 1e3) / n_prof64 for k, (ms_k, n_k) in prof64.items() if n_k}
+        extra["fp64_roofline"] = {}
+        for k, per in per64.items():
+            r = roof_of(k, per)
+            extra["fp64_roofline"][k] = {"bound": r["bound"], "per_launch_us": per * 1e6, "achieved": r["achieved"],
+                                         "unit": r["unit"], "peak": r["peak"], "frac": r["achieved"] / r["peak"],
+                                         "peak_source": r["peak_source"]}
 
     # end to end through the C ABI with pinned host buffers
     pin_o = torch.empty(lay.nfull, dtype=torch.float64, pin_memory=True).numpy()
@@ -404,14 +418,25 @@ def run_gpu(args, world, rank, local):
 
 
 def flow_emax6(api, orb, lay, digits=5):
-    """The emax = 6 Magnus flow to s = 50 (graph-captured steps) in split
-    precision and in FP64: E0 difference, steps, commutators, wall time.
-    The synthetic H is taken as already normal-ordered."""
+    """The emax = 6 Magnus flow to s = 50 (graph-captured steps) of the
+    normal-ordered seed-13 synthetic H in split precision and in FP64: steps,
+    commutators, wall time, and each flow's errors against the FP64 oracle
+    flow of the same H (tests/golden/emax6_flow.npz, written by
+    tests/golden/make_golden.py and checked against the oracle by
+    tests/test_gpu_parity_headline.py): the largest |dE0| over all steps and
+    the relative error of the final Omega's norm (mat_frob_norm)."""
+    import numpy as np
     from imsrg_gpu.synth import synth_hamiltonian
     B = api.Basis.from_dict(orb)
     B.set_split_digits(digits)
-    Hh = synth_hamiltonian(lay, 13)
-    out = {"emax": EMAX, "s_max": 50.0, "ds": 0.5, "graph_steps": True, "split_digits": digits}
+    H0 = api.Operator(B, 1, synth_hamiltonian(lay, 13))
+    api.normal_order(H0)
+    Hh = H0.download()
+    ref = np.load(os.path.join(ROOT, "tests", "golden", "emax6_flow.npz"))
+    out = {"emax": EMAX, "s_max": 50.0, "ds": 0.5, "graph_steps": True, "split_digits": digits,
+           "reference": "FP64 oracle flow (tests/golden/emax6_flow.npz)",
+           "oracle_steps": int(ref["steps"]), "oracle_e0_MeV": float(ref["trace"][-1, 2]),
+           "oracle_omega_norm": float(ref["omega_norm"])}
     for prec in ("ozaki", "fp64"):
         HS, G = api.Operator(B, 1, Hh), api.Operator(B, -1)
         api.magnus_decouple_graph(HS, G, s_max=0.5, ds=0.5, precision=prec)  # builds the step graph
@@ -420,9 +445,16 @@ def flow_emax6(api, orb, lay, digits=5):
         t0 = time.perf_counter()
         r = api.magnus_decouple_graph(HS, G, s_max=50.0, ds=0.5, precision=prec)
         dt = time.perf_counter() - t0
-        out[prec] = {"steps": r["steps"], "commutators": r["ncomm"], "e0_MeV": float(r["trace"][-1, 2]),
-                     "seconds": dt, "commutators_per_s": r["ncomm"] / dt}
-    out["abs_dE0_MeV"] = abs(out["ozaki"]["e0_MeV"] - out["fp64"]["e0_MeV"])
+        tr = r["trace"]
+        same = tr.shape == ref["trace"].shape
+        nrm = api.mat_frob_norm(G)
+        out[prec] = {"steps": r["steps"], "commutators": r["ncomm"], "e0_MeV": float(tr[-1, 2]),
+                     "seconds": dt, "commutators_per_s": r["ncomm"] / dt,
+                     "max_abs_dE0_vs_oracle_MeV": float(np.max(np.abs(tr[:, 2] - ref["trace"][:, 2])))
+                     if same else None,
+                     "omega_norm": nrm,
+                     "omega_norm_rel_err_vs_oracle": abs(nrm - float(ref["omega_norm"])) / float(ref["omega_norm"])}
+    out["abs_dE0_split_vs_fp64_MeV"] = abs(out["ozaki"]["e0_MeV"] - out["fp64"]["e0_MeV"])
     return out
 
 
@@ -567,11 +599,14 @@ def batch_flows(api, n):
                     "converge stop with IMSRG_ERR_NOT_CONVERGED as the reference STOPs"}
 
 
-def prof_work_ozaki(lay, orb):
-    return _workload_flops(lay) + _cc_flops(orb)
+_FP64_PEAK = []
 
 
 def _fp64_peak_tflops():
+    """cuBLAS DGEMM 8192^3 through torch.matmul, best of three (measured once
+    per run): the FP64 pipe's rate on this GPU."""
+    if _FP64_PEAK:
+        return _FP64_PEAK[0]
     import torch
     n = 8192
     a = torch.randn(n, n, dtype=torch.float64, device="cuda")
@@ -586,7 +621,9 @@ def _fp64_peak_tflops():
         e1.record()
         e1.synchronize()
         best = min(best, e0.elapsed_time(e1))
-    return 2 * n ** 3 / (best / 1e3) / 1e12
+    del a, b
+    _FP64_PEAK.append(2 * n ** 3 / (best / 1e3) / 1e12)
+    return _FP64_PEAK[0]
 
 
 def _traffic_from_profiles(kname):

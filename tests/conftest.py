@@ -58,3 +58,18 @@ def make_case(emax, seed=1):
 def rel_err(got, ref):
     scale = max(np.max(np.abs(ref)), 1e-300)
     return float(np.max(np.abs(got - ref)) / scale)
+
+
+def elem_err(got, ref, tol, floor=1e-14):
+    """Element-wise comparison: every element must satisfy
+    |got_i - ref_i| <= tol * |ref_i| + floor * max|ref|.
+    Returns (worst ratio of |got_i - ref_i| to that bound (<= 1 passes),
+    worst relative error |got_i - ref_i| / |ref_i| over the elements with
+    |ref_i| >= 1e-6 max|ref|)."""
+    got, ref = np.asarray(got, np.float64), np.asarray(ref, np.float64)
+    scale = max(float(np.max(np.abs(ref))), 1e-300)
+    d = np.abs(got - ref)
+    bound = tol * np.abs(ref) + floor * scale
+    sig = np.abs(ref) >= 1e-6 * scale
+    worst_rel = float(np.max(d[sig] / np.abs(ref[sig]))) if np.any(sig) else 0.0
+    return float(np.max(d / bound)), worst_rel

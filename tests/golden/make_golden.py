@@ -6,6 +6,12 @@ Writes emax2_golden.npz: the 4He emax=2 basis, seeded synthetic Omega and H
 transform, and the Magnus-flow trace (step, s, E0, E0+mbpt2, |mbpt2|) to s=50;
 plus a uniform-[-5,5] operator pair (brute_force_testing.f90 style) and its
 commutator.
+Writes emax6_flow.npz: the oracle's Magnus flow (White generator, ds = 0.5,
+s_max = 50) of the normal-ordered seed-13 synthetic Hamiltonian in the 16O
+emax=6 basis: the trace rows (step, s, E0, E0+mbpt2, |mbpt2|), the step and
+commutator counts and mat_frob_norm of the final Omega.  bench.py reports its
+emax=6 flows against this trace.  Only the emax=6 fixture:
+python tests/golden/make_golden.py emax6
 """
 import os
 import sys
@@ -19,6 +25,21 @@ sys.path.insert(0, os.path.join(ROOT, "eom-imsrg_full_gb300"))
 from imsrg_gpu.layout import Layout, ho_basis  # noqa: E402
 from imsrg_gpu.synth import random_operator, synth_hamiltonian, synth_omega  # noqa: E402
 from oracle.oracle import Oracle  # noqa: E402
+
+
+def emax6_flow():
+    import os as _os
+    from oracle.oracle import set_threads
+    set_threads(_os.cpu_count())
+    bas = ho_basis(6)
+    lay = Layout(**bas)
+    orc = Oracle(**bas)
+    H = orc.normal_order(synth_hamiltonian(lay, 13))
+    flow = orc.magnus_decouple(H, s_max=50.0, ds=0.5)
+    out = os.path.join(os.path.dirname(os.path.abspath(__file__)), "emax6_flow.npz")
+    np.savez_compressed(out, trace=flow["trace"], steps=flow["steps"], ncomm=flow["ncomm"],
+                        omega_norm=orc.norm(flow["Omega"]), seed=13, s_max=50.0, ds=0.5)
+    print("wrote", out, "flow steps", flow["steps"], "E0", flow["trace"][-1, 2])
 
 
 def main():
@@ -42,4 +63,8 @@ def main():
 
 
 if __name__ == "__main__":
-    main()
+    if sys.argv[1:] == ["emax6"]:
+        emax6_flow()
+    else:
+        main()
+        emax6_flow()
