@@ -363,6 +363,10 @@ struct Workspace {
 };
 int launch_commutator_fp64_ws(imsrg_basis *b, const Workspace &ws, const double *L, int hL, const double *R, int hR,
                               double *RES, int hRES, int with_e0, cudaStream_t st);
+// Loads the device code of every kernel launch_commutator_fp64_ws launches on
+// the current device (with lazy module loading a kernel's module is otherwise
+// loaded, and may allocate, at its first launch).
+int preload_commutator_fp64_ws();
 
 // Ozaki split-precision contraction engine (ozaki.cu)
 int ozaki_prepare(imsrg_basis *b);  // plans and allocates the engine once; errors if unavailable

@@ -722,4 +722,15 @@ int launch_commutator_fp64_ws(imsrg_basis *b, const Workspace &ws, const double 
   return cuda_status(cudaGetLastError());
 }
 
+int preload_commutator_fp64_ws() {
+  cudaFuncAttributes a;
+  const void *fns[] = {(const void *)k_cc_forward<3>, (const void *)k_gemm_fp64, (const void *)k_ph_inputs,
+                       (const void *)k_assemble_2body<false>, (const void *)k_assemble_1body, (const void *)k_energy};
+  for (const void *f : fns) {
+    cudaError_t e = cudaFuncGetAttributes(&a, f);
+    if (e != cudaSuccess) return cuda_status(e);
+  }
+  return IMSRG_OK;
+}
+
 }  // namespace imsrg

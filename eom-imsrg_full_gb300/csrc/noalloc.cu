@@ -8,6 +8,7 @@
 // g_noalloc_scratch is only a stand-in symbol, never a device address: its
 // address is looked up with cudaGetSymbolAddress once per device, with that
 // device current, and passed to the kernels.
+#include <cstdint>
 #include <mutex>
 
 #include "internal.h"
@@ -22,8 +23,10 @@ constexpr int kMaxDevices = 64;
 std::mutex g_mutex;
 double *g_scratch_ptr[kMaxDevices] = {nullptr};
 
-// Device address of the scratch array on the current device (looked up on
-// the first call for that device).
+// Device address of the scratch array on the current device.  The first call
+// for a device is its set-up: it looks the address up and loads the device
+// code of every kernel this path launches (with lazy module loading both
+// would otherwise happen, and could allocate, inside a later call).
 int scratch_address(int dev, double **out) {
   if (dev < 0 || dev >= kMaxDevices) return IMSRG_ERR_INVALID;
   std::lock_guard<std::mutex> lock(g_mutex);
@@ -31,10 +34,18 @@ int scratch_address(int dev, double **out) {
     void *p = nullptr;
     cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
     if (e != cudaSuccess) return cuda_status(e);
+    int s = preload_commutator_fp64_ws();
+    if (s != IMSRG_OK) return s;
     g_scratch_ptr[dev] = (double *)p;
   }
   *out = g_scratch_ptr[dev];
   return IMSRG_OK;
+}
+
+// True when [a, a + n) and [b, b + n) share an element.
+bool overlaps(const double *a, const double *b, long n) {
+  const uintptr_t x = (uintptr_t)a, y = (uintptr_t)b, len = (uintptr_t)n * sizeof(double);
+  return x < y + len && y < x + len;
 }
 
 long round_up(long n) { return (n + 31) / 32 * 32; }
@@ -47,7 +58,7 @@ extern "C" int imsrg_gpu_commutator_noalloc(imsrg_basis_t *b, const double *d_L,
   using namespace imsrg;
   if (!b || !d_L || !d_R || !d_RES) return IMSRG_ERR_INVALID;
   if ((herm_L != 1 && herm_L != -1) || (herm_R != 1 && herm_R != -1)) return IMSRG_ERR_INVALID;
-  if (d_RES == d_L || d_RES == d_R) return IMSRG_ERR_INVALID;
+  if (overlaps(d_RES, d_L, b->nfull) || overlaps(d_RES, d_R, b->nfull)) return IMSRG_ERR_INVALID;
   long ne0p = round_up(imsrg::asm2_ctas(b));
   long need = 2 * round_up(b->nfull) + 2 * round_up(b->cc_total) + round_up(b->wcc_total) + round_up(b->T.n_ph) + ne0p;
   if (need > IMSRG_NOALLOC_SCRATCH_DOUBLES) return IMSRG_ERR_TOO_LARGE;

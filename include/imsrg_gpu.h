@@ -370,8 +370,13 @@ int imsrg_gpu_transform_to_hf(imsrg_op_t *Op, const double *coefs);
  * (emax <= 4 fits; emax = 6 does not).
  *  - The basis must have been created beforehand (creating it allocates the
  *    device tables once) and its device must be current.
- *  - The first call on each device looks up the array's device address; make
- *    that first call before any stream capture.
+ *  - The first call on each device is its set-up: it looks up the array's
+ *    device address and loads the device code of the kernels this call
+ *    launches (with CUDA's lazy module loading that would otherwise happen at
+ *    their first launch, and loading can allocate and synchronise).  Make that
+ *    first call before any stream capture and before the part of the program
+ *    that must not allocate; later calls allocate nothing.
+ *  - d_RES must not share any element with d_L or d_R (IMSRG_ERR_INVALID).
  *  - Work is enqueued on `stream` (NULL: the basis stream).  All calls share
  *    the one array, so calls that overlap on the GPU race; serialise them.
  *    The array keeps the last call's contents; every element a call reads is
