@@ -292,6 +292,18 @@ int flow_graph_begin(imsrg_op *HS, imsrg_op *G, int precision, double ds, double
   return IMSRG_OK;
 }
 
+// Sets the flow parameter s of the step graph's state (a flow restarted from
+// a checkpoint at s).
+int flow_graph_set_s(imsrg_basis *b, double s) {
+  FlowGraph *fg = flow_of(b);
+  if (!fg) return IMSRG_ERR_INVALID;
+  fg->h_state->s = s;
+  IMSRG_CUDA_TRY(cudaMemcpyAsync(&fg->d_state->s, &fg->h_state->s, sizeof(double), cudaMemcpyHostToDevice,
+                                 b->stream));
+  IMSRG_CUDA_TRY(cudaStreamSynchronize(b->stream));
+  return IMSRG_OK;
+}
+
 // Enqueues one step graph and the read-back of its scalars (no wait).
 int flow_graph_launch(imsrg_basis *b) {
   FlowGraph *fg = flow_of(b);

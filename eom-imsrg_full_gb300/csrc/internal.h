@@ -350,6 +350,8 @@ int launch_mbpt2(imsrg_basis *b, const double *H, int herm, double *d_out);
 int launch_white(imsrg_basis *b, const double *H, int hH, double *ETA);
 int launch_generator(imsrg_basis *b, const double *Hden, int hH, const double *Hnum, int use_atan, double *ETA);
 int launch_white_tangent(imsrg_basis *b, const double *H, const double *dH, int hH, double *dETA);
+// Hb += (d White / d H)^T ETAb (reverse mode; monob: norb x norb scratch)
+int launch_white_adjoint(imsrg_basis *b, const double *H, int hH, const double *ETAb, double *Hb, double *monob);
 int launch_pack(imsrg_basis *b, const double *flat, double *packed);
 int launch_unpack(imsrg_basis *b, const double *packed, int herm, double *flat);
 int launch_check_finite(imsrg_basis *b, const double *op, int *d_flag);
@@ -406,6 +408,7 @@ int work_op(imsrg_basis *b, int k, imsrg_op **out);
 // dHds (IMSRG_ODE.f90:416-463): DH = [eta(HS), HS] with generator IMSRG_GEN_*
 int dhds_dev(imsrg_basis *b, const double *HS, int hH, double *DH, int generator, int precision);
 int flow_graph_begin(imsrg_op *HS, imsrg_op *G, int precision, double ds, double *e0, double *emp2);
+int flow_graph_set_s(imsrg_basis *b, double s);  // a flow restarted at s
 int flow_graph_launch(imsrg_basis *b);
 int flow_graph_finish(imsrg_basis *b, double *s, double *e0, double *emp2, int *nc, int *status);
 void flow_graph_free(imsrg_basis *b);

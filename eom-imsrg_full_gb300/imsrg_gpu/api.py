@@ -40,6 +40,7 @@ SYMBOLS = (
     "imsrg_gpu_dhds", "imsrg_gpu_transform_bch", "imsrg_gpu_ode_decouple", "imsrg_gpu_commutator_host",
     "imsrg_gpu_read_interaction", "imsrg_gpu_h0_harm_osc", "imsrg_gpu_hartree_fock", "imsrg_gpu_transform_to_hf",
     "imsrg_gpu_batch_create", "imsrg_gpu_batch_commutator", "imsrg_gpu_batch_destroy",
+    "imsrg_gpu_magnus_rules", "imsrg_gpu_magnus_decouple_checkpoint",
 )
 
 KERNELS = ("cc_forward", "gemm_fp64", "assemble_2body", "assemble_1body", "ozaki_slice", "ozaki_mma",
@@ -130,6 +131,9 @@ def lib():
             "imsrg_gpu_batch_create": [i, C.POINTER(vp), C.POINTER(vp)],
             "imsrg_gpu_batch_commutator": [vp, C.POINTER(vp), C.POINTER(vp), C.POINTER(vp), i, i],
             "imsrg_gpu_batch_destroy": [vp],
+            "imsrg_gpu_magnus_rules": [vp, d, dp, ip],
+            "imsrg_gpu_magnus_decouple_checkpoint": [vp, vp, i, d, d, i, i, i, C.c_char_p, C.c_char_p, i, dp, ip,
+                                                     ip, dp],
         }
         for name, args in sig.items():
             f = getattr(L, name)
@@ -449,6 +453,34 @@ def magnus_decouple_graph(HS: Operator, G: Operator, s_max: float = 50.0, ds: fl
            "magnus_decouple_graph")
     n = steps.value + 1
     return dict(steps=steps.value, ncomm=nc.value, trace=trace[:5 * n].reshape(n, 5))
+
+
+def magnus_rules(basis: Basis, lawson_beta: float = 0.0):
+    """The reference's ds and checkpoint period of magnus_decouple
+    (IMSRG_MAGNUS.f90:45-62) for this basis: (ds, chk)."""
+    ds, chk = C.c_double(), C.c_int()
+    _check(lib().imsrg_gpu_magnus_rules(basis.handle, float(lawson_beta), C.byref(ds), C.byref(chk)),
+           "magnus_rules")
+    return ds.value, chk.value
+
+
+def magnus_decouple_checkpoint(HS: Operator, G: Operator, directory: str | None, prefix: str | None,
+                               chk: int = 0, generator: str = "white", s_max: float = 50.0, ds: float = 0.5,
+                               max_steps: int = 1000, precision: str = "fp64", graph: bool = False):
+    """magnus_decouple writing Omega checkpoints every chk steps into
+    directory (file names of checkpoint_name) and restarting from the newest
+    one found there (IMSRG_MAGNUS.f90:56-110).  Returns steps (the final step
+    counter), ncomm, s_restart (-1 without a restart) and the trace rows up to
+    the final step (rows before a restart are left zero)."""
+    gen = {"white": 0, "atan": 1, "w2": 2}[generator]
+    trace = np.zeros(5 * (max_steps + 1))
+    steps, nc, sx = C.c_int(0), C.c_int(0), C.c_double(0.0)
+    _check(lib().imsrg_gpu_magnus_decouple_checkpoint(
+        HS.handle, G.handle, gen, float(s_max), float(ds), int(max_steps), PREC[precision], int(bool(graph)),
+        directory.encode() if directory is not None else None, prefix.encode() if prefix is not None else None,
+        int(chk), _dp(trace), C.byref(steps), C.byref(nc), C.byref(sx)), "magnus_decouple_checkpoint")
+    n = steps.value + 1
+    return dict(steps=steps.value, ncomm=nc.value, s_restart=sx.value, trace=trace[:5 * n].reshape(n, 5))
 
 
 def magnus_decouple_batch(HS: list, G: list, s_max: float = 50.0, ds: float = 0.5, max_steps: int = 1000,

@@ -237,6 +237,40 @@ int imsrg_gpu_magnus_decouple_graph(imsrg_op_t *HS, imsrg_op_t *G, double s_max,
 int imsrg_gpu_magnus_decouple_batch(int n, imsrg_op_t *const *HS, imsrg_op_t *const *G, double s_max, double ds,
                                     int max_steps, int precision, double *const *traces, int *steps, int *ncomm,
                                     int *status);
+/* The reference's step-size and checkpoint-period rules of magnus_decouple
+ * (IMSRG_MAGNUS.f90:45-51, 56-62), which the flow entry points leave to the
+ * caller: ds = 0.5 for lawson_beta < 6, else 0.1; a checkpoint every chk = 4
+ * steps at eMax = 14, every step above, every 24 below (eMax = max 2n+l of
+ * the basis).  Either output may be NULL.  Host only. */
+int imsrg_gpu_magnus_rules(const imsrg_basis_t *b, double lawson_beta, double *ds, int *chk);
+/* magnus_decouple with the reference's Omega checkpoints
+ * (IMSRG_MAGNUS.f90:56-110; write_omega_checkpoint and read_omega_checkpoint,
+ * basic_IMSRG.f90:3132-3312).  With dir and prefix non-NULL:
+ *  - at the start the newest checkpoint is looked for as the reference does
+ *    (s = 95.5, 95.0, ... down to 1.5, file names of
+ *    imsrg_gpu_checkpoint_name); when one is found the flow restarts from it:
+ *    G = Omega(sx), HS = BCH_EXPAND(G, H) with H the HS passed in, the
+ *    generator of HS, s = sx, step counter nint(sx/ds), and *s_restart = sx
+ *    (else -1);
+ *  - before the Magnus step of every step count divisible by chk (chk <= 0:
+ *    the imsrg_gpu_magnus_rules value) Omega(s) is written to its file, except
+ *    the first one due after a restart, and the file of s - 12 (eMax = 14:
+ *    s - 4) is removed;
+ *  - prefixes beginning with "testcase" write and read nothing.
+ * The step is the host-driven one of imsrg_gpu_magnus_decouple_gen
+ * (use_graph = 0; generator IMSRG_GEN_*) or the graph launch of
+ * imsrg_gpu_magnus_decouple_graph (use_graph = 1; White generator only), so a
+ * restarted flow takes the uninterrupted one's steps; H and Omega agree with
+ * it to rounding (the file format keeps upper triangles and writes square
+ * diagonals as herm x stored value, which flips the sign of the rounding
+ * residue on the diagonals of the anti-Hermitian Omega).  trace rows
+ * are indexed by the step counter (a restarted flow leaves the rows up to its
+ * restart step untouched, as the reference appends to its flow file);
+ * *steps is the final step counter, *ncomm the commutators of this call. */
+int imsrg_gpu_magnus_decouple_checkpoint(imsrg_op_t *HS, imsrg_op_t *G, int generator, double s_max, double ds,
+                                         int max_steps, int precision, int use_graph, const char *dir,
+                                         const char *prefix, int chk, double *trace, int *steps, int *ncomm,
+                                         double *s_restart);
 /* Derivative of the flow along one direction of the input Hamiltonian
  * (forward mode; no reference counterpart).  dHS: in = dH(0) (for
  * H(c) = T + sum_k c_k V_k, the normal-ordered V_k gives dE0/dc_k), out =
