@@ -887,6 +887,7 @@ void free_basis_device(imsrg_basis *b) {
   if (b->stream) cudaStreamSynchronize(b->stream);
   profile_free(b);
   flow_graph_free(b);
+  adjoint_free(b);
   for (imsrg_basis::CommGraph &g : b->comm_graphs) cudaGraphExecDestroy(g.exec);
   b->comm_graphs.clear();
   ozaki_free(b);

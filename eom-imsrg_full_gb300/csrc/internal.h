@@ -280,6 +280,8 @@ struct imsrg_basis {
   // Ozaki split-precision engine state (allocated on first use)
   void *ozaki = nullptr;
   int split_digits = 6;  // digits per operand of the split engine (4, 5 or 6), fixed once its plan exists
+  // Reverse-mode (adjoint) workspace (adjoint.cu), allocated on first use
+  void *adjoint = nullptr;
   // Graph of one Magnus flow step (graph.cu), built on first use
   void *flowgraph = nullptr;
   // Captured commutator launch sequences, one per argument set (api.cpp)
@@ -400,6 +402,15 @@ int ozaki_batch_create(imsrg_basis *const *bases, int n, void **out);
 int ozaki_batch_mma(void *batch, cudaStream_t st, int hL, int hR);
 int ozaki_batch_error(void *batch, cudaStream_t st);
 void ozaki_batch_free(void *batch);
+
+// Reverse mode (adjoint.cu): Yb = d<Cb, [X, Y]> / dY (herm(X) = hX,
+// herm(Y) = hY; with_e0 = 0 ignores Cb[0]); FP64, overwrites Yb.
+int adjoint_prepare(imsrg_basis *b);
+void adjoint_free(imsrg_basis *b);
+int commutator_adjoint_dev(imsrg_basis *b, const double *X, int hX, const double *Cb, int hY, int with_e0,
+                           double *Yb);
+int dot_dev(imsrg_basis *b, const double *x, const double *y, long n, double *out);  // fixed order
+double *adjoint_monob(imsrg_basis *b);  // norb x norb scratch of the White adjoint
 
 // Magnus flow step as a CUDA graph (graph.cu)
 int flow_tmp_ops(imsrg_basis *b, imsrg_op **H0, imsrg_op **DG, imsrg_op **X0, imsrg_op **X1);  // api.cpp

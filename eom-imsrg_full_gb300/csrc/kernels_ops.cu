@@ -180,6 +180,93 @@ __global__ void __launch_bounds__(256) k_white_tangent(DevTables T, const double
   }
 }
 
+// Adjoint of the White generator (reverse mode): given ETAb, the gradient of a
+// scalar with respect to ETA = White(H), add its gradient with respect to H
+// into Hb.  eta = N / D with N = H[e] and D linear in H (white_den), so
+// Hb[e] += etab / D and D's adjoint Db = -etab eta / D flows back through
+// white_den's linear map: one-body diagonals directly, the particle-hole
+// diagonals of fph denominators through their J sums, and the pphh
+// denominators' six monopoles through the table monob (k_white_adjoint2 takes
+// it back to the two-body diagonals).  FP64 atomics: the order of the
+// additions varies, so results agree to rounding, not bit for bit.
+__device__ __forceinline__ void v_scatter(const DevTables &T, double *Hb, int herm, int a, int b, int c, int d,
+                                          int J2, double w) {
+  const VLoc l = v_loc(T, a, b, c, d, J2);
+  if (l.idx < 0) return;
+  double x = dflip(w, l.neg ^ (l.trans & (herm < 0)));
+  if (l.nsq) x = x * (l.nsq == 1 ? IMSRG_SQRT2 : 2.0000000000000004);
+  atomicAdd(Hb + l.idx, x);
+}
+
+__device__ __forceinline__ long fdiag(const DevTables &T, int a) {
+  const int pa = T.orbpos[a];
+  return T.orb[a].w ? T.off_fhh + pa + (long)pa * T.A : T.off_fpp + pa + (long)pa * T.P;
+}
+
+__global__ void __launch_bounds__(256) k_white_adjoint1(DevTables T, const double *__restrict__ H, int herm,
+                                                        const double *__restrict__ mono,
+                                                        const double *__restrict__ etab, double *Hb,
+                                                        double *monob) {
+  const long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  double den = 1.0;
+  const long e = white_den(T, H, herm, mono, t, &den);
+  if (e < 0) return;
+  const double gb = etab[e];
+  if (gb == 0.0) return;
+  const double eta = H[e] / den;
+  atomicAdd(Hb + e, gb / den);
+  const double db = -gb * eta / den;
+  const long nph1 = (long)T.P * T.A;
+  if (t < nph1) {
+    const int a = (int)(t % T.P), i = (int)(t / T.P);
+    const int ak = T.part_orb[a], ik = T.hole_orb[i];
+    const int ji = T.orb[ik].x;
+    atomicAdd(Hb + T.off_fpp + a + (long)a * T.P, db);
+    atomicAdd(Hb + T.off_fhh + i + (long)i * T.A, -db);
+    for (int JT = 0; JT <= 2 * ji; JT += 2)
+      v_scatter(T, Hb, herm, ak, ik, ak, ik, JT, -db * (JT + 1) / (ji + 1.0) / (ji + 1.0));
+    return;
+  }
+  // pphh element: recover its orbits as white_den walked them
+  long u = t - nph1;
+  for (int q = 0; q < T.nblocks; q++) {
+    const int s = q * 6 + 2;
+    const long n = (long)T.gam_n1[s] * T.gam_n2[s];
+    if (u >= n) {
+      u -= n;
+      continue;
+    }
+    const int np = T.gam_n1[s];
+    const int *qp = T.qn + T.qn_start[q * 3 + 0] + 2 * (int)(u % np);
+    const int *qh = T.qn + T.qn_start[q * 3 + 2] + 2 * (int)(u / np);
+    const int a = qp[0], b = qp[1], i = qh[0], j = qh[1], N = T.norb;
+    atomicAdd(monob + a * N + b, db);
+    atomicAdd(monob + i * N + j, db);
+    atomicAdd(monob + a * N + i, -db);
+    atomicAdd(monob + a * N + j, -db);
+    atomicAdd(monob + i * N + b, -db);
+    atomicAdd(monob + j * N + b, -db);
+    atomicAdd(Hb + fdiag(T, a), db);
+    atomicAdd(Hb + fdiag(T, b), db);
+    atomicAdd(Hb + fdiag(T, i), -db);
+    atomicAdd(Hb + fdiag(T, j), -db);
+    return;
+  }
+}
+
+// monopole table adjoint -> the two-body diagonals <ab|V|ab>_J (k_monopole's
+// transpose)
+__global__ void k_white_adjoint2(DevTables T, int herm, const double *__restrict__ monob, double *Hb) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= T.norb * T.norb) return;
+  const double mb = monob[t];
+  if (mb == 0.0) return;
+  const int a = t / T.norb, b = t % T.norb;
+  const int ja = T.orb[a].x, jb = T.orb[b].x;
+  for (int JT = abs(ja - jb); JT <= ja + jb; JT += 2)
+    v_scatter(T, Hb, herm, a, b, a, b, JT, mb * (JT + 1) / (ja + 1.0) / (jb + 1.0));
+}
+
 // normal_order (basic_IMSRG.f90:2375-2506) from T (the operator before
 // normal ordering) into H.  Threads [0, A*A + P*A + P*P) take one one-body
 // element each (upper triangles of fhh and fpp, mirrored; fph whole):
@@ -338,6 +425,22 @@ int launch_white_tangent(imsrg_basis *b, const double *H, const double *dH, int 
   long n = (long)b->P * b->A + n3;
   if (n > 0)
     k_white_tangent<<<(unsigned)((n + 255) / 256), 256, 0, b->stream>>>(b->T, H, dH, hH, mono, dmono, dETA);
+  b->launches += 3;
+  return cuda_status(cudaGetLastError());
+}
+
+int launch_white_adjoint(imsrg_basis *b, const double *H, int hH, const double *ETAb, double *Hb, double *monob) {
+  double *mono = b->mono;
+  const int nn = b->norb * b->norb;
+  ProfScope ps(b, IMSRG_KERNEL_OPS);
+  IMSRG_CUDA_TRY(cudaMemsetAsync(monob, 0, nn * sizeof(double), b->stream));
+  k_monopole<<<(nn + 127) / 128, 128, 0, b->stream>>>(b->T, H, hH, mono);
+  long n3 = 0;
+  for (int q = 0; q < b->nblocks; q++) n3 += (long)b->gam_n1[q * 6 + 2] * b->gam_n2[q * 6 + 2];
+  const long n = (long)b->P * b->A + n3;
+  if (n > 0)
+    k_white_adjoint1<<<(unsigned)((n + 255) / 256), 256, 0, b->stream>>>(b->T, H, hH, mono, ETAb, Hb, monob);
+  k_white_adjoint2<<<(nn + 127) / 128, 128, 0, b->stream>>>(b->T, hH, monob, Hb);
   b->launches += 3;
   return cuda_status(cudaGetLastError());
 }

@@ -41,6 +41,8 @@ SYMBOLS = (
     "imsrg_gpu_read_interaction", "imsrg_gpu_h0_harm_osc", "imsrg_gpu_hartree_fock", "imsrg_gpu_transform_to_hf",
     "imsrg_gpu_batch_create", "imsrg_gpu_batch_commutator", "imsrg_gpu_batch_destroy",
     "imsrg_gpu_magnus_rules", "imsrg_gpu_magnus_decouple_checkpoint",
+    "imsrg_gpu_commutator_adjoint", "imsrg_gpu_white_adjoint", "imsrg_gpu_op_dot",
+    "imsrg_gpu_magnus_decouple_adjoint",
 )
 
 KERNELS = ("cc_forward", "gemm_fp64", "assemble_2body", "assemble_1body", "ozaki_slice", "ozaki_mma",
@@ -132,6 +134,10 @@ def lib():
             "imsrg_gpu_batch_commutator": [vp, C.POINTER(vp), C.POINTER(vp), C.POINTER(vp), i, i],
             "imsrg_gpu_batch_destroy": [vp],
             "imsrg_gpu_magnus_rules": [vp, d, dp, ip],
+            "imsrg_gpu_commutator_adjoint": [vp, vp, i, i, vp],
+            "imsrg_gpu_white_adjoint": [vp, vp, vp],
+            "imsrg_gpu_op_dot": [vp, vp, dp],
+            "imsrg_gpu_magnus_decouple_adjoint": [vp, vp, vp, d, d, i, i, i, C.POINTER(vp), dp, dp, ip, ip],
             "imsrg_gpu_magnus_decouple_checkpoint": [vp, vp, i, d, d, i, i, i, C.c_char_p, C.c_char_p, i, dp, ip,
                                                      ip, dp],
         }
@@ -481,6 +487,39 @@ def magnus_decouple_checkpoint(HS: Operator, G: Operator, directory: str | None,
         int(chk), _dp(trace), C.byref(steps), C.byref(nc), C.byref(sx)), "magnus_decouple_checkpoint")
     n = steps.value + 1
     return dict(steps=steps.value, ncomm=nc.value, s_restart=sx.value, trace=trace[:5 * n].reshape(n, 5))
+
+
+def commutator_adjoint(X: Operator, Cbar: Operator, herm_Y: int, Ybar: Operator, with_e0: bool = True):
+    """Ybar = d<Cbar, [X, Y]>/dY for Y of hermiticity herm_Y (FP64)."""
+    _check(lib().imsrg_gpu_commutator_adjoint(X.handle, Cbar.handle, int(herm_Y), int(bool(with_e0)),
+                                              Ybar.handle), "commutator_adjoint")
+
+
+def white_adjoint(H: Operator, ETAbar: Operator, Hbar: Operator):
+    """Hbar = (d White(H) / dH)^T ETAbar."""
+    _check(lib().imsrg_gpu_white_adjoint(H.handle, ETAbar.handle, Hbar.handle), "white_adjoint")
+
+
+def op_dot(A: Operator, B: Operator) -> float:
+    v = C.c_double()
+    _check(lib().imsrg_gpu_op_dot(A.handle, B.handle, C.byref(v)), "op_dot")
+    return v.value
+
+
+def magnus_decouple_adjoint(HS: Operator, G: Operator, dirs: list, Hbar: Operator | None = None,
+                            s_max: float = 50.0, ds: float = 0.5, max_steps: int = 1000, precision: str = "fp64"):
+    """The Magnus flow (as magnus_decouple) and one backward sweep: grad[j] =
+    dE0(s)/d(HS along dirs[j]); Hbar (optional) receives the whole gradient."""
+    trace = np.zeros(5 * (max_steps + 1))
+    steps, nc = C.c_int(0), C.c_int(0)
+    n = len(dirs)
+    arr = (C.c_void_p * max(n, 1))(*[x.handle for x in dirs])
+    grad = np.zeros(max(n, 1))
+    _check(lib().imsrg_gpu_magnus_decouple_adjoint(
+        HS.handle, G.handle, Hbar.handle if Hbar is not None else None, float(s_max), float(ds), int(max_steps),
+        PREC[precision], n, arr, _dp(grad), _dp(trace), C.byref(steps), C.byref(nc)), "magnus_decouple_adjoint")
+    k = steps.value + 1
+    return dict(steps=steps.value, ncomm=nc.value, grad=grad[:n], trace=trace[:5 * k].reshape(k, 5))
 
 
 def magnus_decouple_batch(HS: list, G: list, s_max: float = 50.0, ds: float = 0.5, max_steps: int = 1000,

@@ -284,6 +284,41 @@ int imsrg_gpu_magnus_decouple_tangent(imsrg_op_t *HS, imsrg_op_t *dHS, imsrg_op_
                                       double ds, int max_steps, int precision, double *trace, double *dtrace,
                                       int *steps, int *ncomm);
 
+/* --- reverse-mode derivatives (no reference counterpart: the reference has no
+ *     derivative code; its checks are finite differences of the flow) ------
+ * Adjoint of the two-body commutator: for a fixed X, the commutator RES =
+ * [X, Y] of imsrg_gpu_commutator (the sequence of IMSRG_MAGNUS.f90:207-219)
+ * is linear in Y, and
+ *     Ybar = d <Cbar, [X, Y]> / dY      (<A, B> = sum over the flat layout)
+ * is its transpose applied to Cbar, for Y of hermiticity herm_Y (Ybar herm
+ * herm_Y, overwritten).  Every forward piece (Pandya transform, ladder and
+ * WCC products, recoupling, 122/121/221/111 insertions, 110/220 energy) is
+ * transposed on the forward's own gather lists; FP64.  with_e0 = 0 is the
+ * commutator that leaves RES E0 alone (MAGNUS_EXPAND's), so Cbar E0 is
+ * ignored.  The derivative with respect to X is -(the same call with X and Y
+ * swapped), since [X, Y] = -[Y, X].  Scatters use FP64 atomics: results agree
+ * run to run to rounding, not bit for bit. */
+int imsrg_gpu_commutator_adjoint(const imsrg_op_t *X, const imsrg_op_t *Cbar, int herm_Y, int with_e0,
+                                 imsrg_op_t *Ybar);
+/* Adjoint of build_gs_white (generators.f90:4-106) at H: Hbar = (d eta / dH)^T
+ * ETAbar (overwritten, herm of H).  FP64 atomics, as above. */
+int imsrg_gpu_white_adjoint(const imsrg_op_t *H, const imsrg_op_t *ETAbar, imsrg_op_t *Hbar);
+/* <A, B> over the flat layout (fixed summation order). */
+int imsrg_gpu_op_dot(const imsrg_op_t *A, const imsrg_op_t *B, double *out);
+/* The Magnus flow of imsrg_gpu_magnus_decouple (White generator; same
+ * arguments, results and trace) followed by one backward sweep of its
+ * adjoint: Hbar (may be NULL; herm +1) receives the gradient of the final E0
+ * with respect to every element of the input HS (flat layout), and grad[j] =
+ * <Hbar, dirs[j]> for j < ndir.  For H(c) = T + sum_k c_k V_k with HS =
+ * normal_order(H(c)), dirs[k] = normal_order(V_k) gives grad[k] = dE0/dc_k
+ * for every k from one sweep.  The forward keeps every Magnus and BCH term
+ * in device memory (one operator each; about the flow's commutator count x
+ * nfull doubles) and runs in `precision`; the backward sweep's transposed
+ * commutators are FP64.  The series keep the forward flow's term counts. */
+int imsrg_gpu_magnus_decouple_adjoint(imsrg_op_t *HS, imsrg_op_t *G, imsrg_op_t *Hbar, double s_max, double ds,
+                                      int max_steps, int precision, int ndir, const imsrg_op_t *const *dirs,
+                                      double *grad, double *trace, int *steps, int *ncomm);
+
 /* The split-precision engine's CTA schedule (no reference counterpart): when
  * a basis first runs a split-precision commutator, the engine times its
  * persistent tensor-core kernel under *ncand candidate tile-cost models and
