@@ -405,6 +405,7 @@ def run_gpu(args, world, rank, local):
             line["hartree_fock"] = hf_emax6(api, orb, lay)
             line["batch"] = batch_flows(api, args.batch)
             line["batched_commutators"] = batched_commutators(api)
+            line["adjoint"] = adjoint_extra(api)
         if world == 1 and not args.no_cpu_baseline:
             line["cpu_baseline"] = cpu_baseline(orb, lay, seconds=args.cpu_seconds)
             # the same oracle on one core (the reference itself threads only
@@ -455,6 +456,61 @@ def flow_emax6(api, orb, lay, digits=5):
                      "omega_norm": nrm,
                      "omega_norm_rel_err_vs_oracle": abs(nrm - float(ref["omega_norm"])) / float(ref["omega_norm"])}
     out["abs_dE0_split_vs_fp64_MeV"] = abs(out["ozaki"]["e0_MeV"] - out["fp64"]["e0_MeV"])
+    return out
+
+
+def adjoint_extra(api):
+    """dE0/dc_k for H(c) = T + sum_k c_k V_k (imsrg_gpu.synth.adjoint_terms,
+    c = 1) of the Magnus flow to |E_mbpt2| < 1e-6 (s_max 50, ds 0.5): one
+    backward sweep of imsrg_gpu_magnus_decouple_adjoint for all four c_k
+    against four tangent-linear flows, at emax = 4 (gradients compared with the
+    oracle's central differences, tests/golden/adjoint_fd_emax4.npz) and
+    emax = 6 (timing).  Wall times after a short warm-up flow of each kind."""
+    import numpy as np
+    from imsrg_gpu.layout import Layout, ho_basis
+    from imsrg_gpu.synth import adjoint_terms
+    ref = np.load(os.path.join(ROOT, "tests", "golden", "adjoint_fd_emax4.npz"))
+    out = {"workload": "H(c) = T + sum_k c_k V_k, four N(0,1) MeV two-body V_k, c = 1",
+           "reference": "FP64 oracle central differences, h = 1e-4 (tests/golden/adjoint_fd_emax4.npz)"}
+    for emax in (4, 6):
+        orb = ho_basis(emax)
+        lay = Layout(**orb)
+        B = api.Basis.from_dict(orb)
+        B.set_split_digits(SPLIT_DIGITS)
+        T, V = adjoint_terms(lay)
+        H = api.Operator(B, 1, T + sum(V))
+        api.normal_order(H)
+        H0 = H.download()
+        dirs = []
+        for v in V:
+            d = api.Operator(B, 1, v)
+            api.normal_order(d)
+            dirs.append(d)
+        for prec in ("fp64", "ozaki"):
+            api.magnus_decouple_adjoint(api.Operator(B, 1, H0), api.Operator(B, -1), dirs, s_max=1.0,
+                                        precision=prec)
+            api.magnus_decouple_tangent(api.Operator(B, 1, H0), api.Operator(B, 1, dirs[0].download()),
+                                        api.Operator(B, -1), api.Operator(B, -1), s_max=1.0, precision=prec)
+            B.synchronize()
+            t0 = time.perf_counter()
+            adj = api.magnus_decouple_adjoint(api.Operator(B, 1, H0), api.Operator(B, -1), dirs, s_max=50.0,
+                                              precision=prec)
+            t_adj = time.perf_counter() - t0
+            tan = []
+            t0 = time.perf_counter()
+            for d in dirs:
+                r = api.magnus_decouple_tangent(api.Operator(B, 1, H0), api.Operator(B, 1, d.download()),
+                                                api.Operator(B, -1), api.Operator(B, -1), s_max=50.0,
+                                                precision=prec)
+                tan.append(float(r["dtrace"][-1, 2]))
+            t_tan = time.perf_counter() - t0
+            rec = {"steps": adj["steps"], "flow_commutators": adj["ncomm"], "adjoint_s": t_adj,
+                   "tangent_x4_s": t_tan, "adjoint_speedup": t_tan / t_adj,
+                   "dE0_dc": [float(x) for x in adj["grad"]],
+                   "max_rel_diff_adjoint_vs_tangent": float(np.max(np.abs(adj["grad"] - tan) / np.abs(tan)))}
+            if emax == 4:
+                rec["max_rel_err_vs_oracle_fd"] = float(np.max(np.abs(adj["grad"] - ref["fd"]) / np.abs(ref["fd"])))
+            out[f"emax{emax}_{prec}"] = rec
     return out
 
 

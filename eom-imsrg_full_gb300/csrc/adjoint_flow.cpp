@@ -30,18 +30,25 @@ const double kCof[7] = {1.0, -0.5, .0833333333, 0.0, -0.00138888888, 0.0, 3.3068
 
 int chk(const imsrg_op *op) { return (op && op->b && op->d) ? IMSRG_OK : IMSRG_ERR_INVALID; }
 
-// Device copies of the flow's series terms, freed with the recorder.
+// Device copies of the flow's series terms, in chunks of kChunk operators
+// (one allocation per chunk), freed with the recorder.
 struct Store {
-  std::vector<double *> bufs;
-  long n = 0;
+  static constexpr int kChunk = 64;
+  std::vector<double *> chunks;
+  int used = kChunk;  // operators taken from the last chunk
+  long n = 0;         // doubles per operator (padded to 32 for alignment)
   ~Store() {
-    for (double *p : bufs) cudaFree(p);
+    for (double *p : chunks) cudaFree(p);
   }
-  int keep(imsrg_basis *b, const double *src, double **out) {
-    double *p = nullptr;
-    IMSRG_CUDA_TRY(cudaMalloc((void **)&p, n * sizeof(double)));
-    bufs.push_back(p);
-    IMSRG_CUDA_TRY(cudaMemcpyAsync(p, src, n * sizeof(double), cudaMemcpyDeviceToDevice, b->stream));
+  int keep(imsrg_basis *b, const double *src, long nf, double **out) {
+    if (used == kChunk) {
+      double *p = nullptr;
+      IMSRG_CUDA_TRY(cudaMalloc((void **)&p, (size_t)kChunk * n * sizeof(double)));
+      chunks.push_back(p);
+      used = 0;
+    }
+    double *p = chunks.back() + (long)used++ * n;
+    IMSRG_CUDA_TRY(cudaMemcpyAsync(p, src, nf * sizeof(double), cudaMemcpyDeviceToDevice, b->stream));
     *out = p;
     return IMSRG_OK;
   }
@@ -135,7 +142,7 @@ int imsrg_gpu_magnus_decouple_adjoint(imsrg_op_t *HS, imsrg_op_t *G, imsrg_op_t 
   IMSRG_TRY(imsrg::flow_tmp_ops(b, &H0, &DG, &X0, &X1));
   imsrg_op *X[2] = {X0, X1};
   Store store;
-  store.n = nf;
+  store.n = (nf + 31) / 32 * 32;
   std::vector<StepRecord> rec;
 
   // --- forward: magnus_decouple with the White generator, recorded ---------
@@ -166,10 +173,10 @@ int imsrg_gpu_magnus_decouple_adjoint(imsrg_op_t *HS, imsrg_op_t *G, imsrg_op_t 
   while (crit > 1e-6 && s < s_max - 1e-12 && steps < max_steps) {
     steps++;
     StepRecord r;
-    IMSRG_TRY(store.keep(b, G->d, &r.omega_prev));
-    IMSRG_TRY(store.keep(b, HS->d, &r.hs_prev));
+    IMSRG_TRY(store.keep(b, G->d, nf, &r.omega_prev));
+    IMSRG_TRY(store.keep(b, HS->d, nf, &r.hs_prev));
     double *a1 = nullptr;
-    IMSRG_TRY(store.keep(b, DG->d, &a1));
+    IMSRG_TRY(store.keep(b, DG->d, nf, &a1));
     r.A.push_back(a1);
     // MAGNUS_EXPAND (the sequence of imsrg_gpu_magnus_expand)
     {
@@ -197,7 +204,7 @@ int imsrg_gpu_magnus_decouple_adjoint(imsrg_op_t *HS, imsrg_op_t *G, imsrg_op_t 
           if (!std::isfinite(nrm)) return IMSRG_ERR_NONFINITE;
           advals[i] = nrm * std::fabs(kCof[i - 1]);
           double *ai = nullptr;
-          IMSRG_TRY(store.keep(b, INT2->d, &ai));
+          IMSRG_TRY(store.keep(b, INT2->d, nf, &ai));
           r.A.push_back(ai);
           cur = 1 - cur;
         }
@@ -206,7 +213,7 @@ int imsrg_gpu_magnus_decouple_adjoint(imsrg_op_t *HS, imsrg_op_t *G, imsrg_op_t 
     // euler_step
     IMSRG_TRY(imsrg::launch_axpby(b, G->d, 1.0, DG->d, ds, G->d));
     s += ds;
-    IMSRG_TRY(store.keep(b, G->d, &r.omega));
+    IMSRG_TRY(store.keep(b, G->d, nf, &r.omega));
     // BCH_EXPAND (the sequence of imsrg_gpu_bch_expand)
     {
       HS->herm = H0->herm;
@@ -227,7 +234,7 @@ int imsrg_gpu_magnus_decouple_adjoint(imsrg_op_t *HS, imsrg_op_t *G, imsrg_op_t 
         IMSRG_TRY(norm_dev(b, INT2->d, &nrm));
         if (!std::isfinite(nrm)) return IMSRG_ERR_NONFINITE;
         double *bn = nullptr;
-        IMSRG_TRY(store.keep(b, INT2->d, &bn));
+        IMSRG_TRY(store.keep(b, INT2->d, nf, &bn));
         r.B.push_back(bn);
         r.bcoef.push_back(coef);
         cur = 1 - cur;

@@ -173,3 +173,18 @@ def write_vrenorm(lay: Layout, op, path: str, seed: int | None = None) -> int:
                         f.write(f"{b.tz} {b.par} {b.J2} {a} {bb} {c} {d} {v!r}\n")
                         n += 1
     return n
+
+
+def adjoint_terms(lay: Layout):
+    """The derivative workload H(c) = T + sum_k c_k V_k: T is the E0 and
+    one-body part of the seed-300 synthetic Hamiltonian, V_1..V_4 the two-body
+    parts of the seed-301..304 ones (independent N(0, 1) MeV elements)."""
+    one = lay.off_fpp + lay.P * lay.P
+    T = synth_hamiltonian(lay, 300)
+    T[one:] = 0.0
+    V = []
+    for k in range(4):
+        v = synth_hamiltonian(lay, 301 + k)
+        v[:one] = 0.0
+        V.append(v)
+    return T, V

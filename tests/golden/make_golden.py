@@ -12,6 +12,12 @@ emax=6 basis: the trace rows (step, s, E0, E0+mbpt2, |mbpt2|), the step and
 commutator counts and mat_frob_norm of the final Omega.  bench.py reports its
 emax=6 flows against this trace.  Only the emax=6 fixture:
 python tests/golden/make_golden.py emax6
+Writes adjoint_fd_emax4.npz: dE0/dc_k of the oracle's Magnus flow (White
+generator, ds = 0.5, to |E_mbpt2| < 1e-6) for H(c) = T + sum_k c_k V_k in the
+16O emax=4 basis (T the seed-300 one-body part, V_k the seed-301..304
+two-body parts, c = 1) by central differences with h = 1e-4; bench.py
+reports its adjoint gradients against them.  Only this fixture:
+python tests/golden/make_golden.py adjoint
 """
 import os
 import sys
@@ -23,7 +29,7 @@ sys.path.insert(0, ROOT)
 sys.path.insert(0, os.path.join(ROOT, "eom-imsrg_full_gb300"))
 
 from imsrg_gpu.layout import Layout, ho_basis  # noqa: E402
-from imsrg_gpu.synth import random_operator, synth_hamiltonian, synth_omega  # noqa: E402
+from imsrg_gpu.synth import adjoint_terms, random_operator, synth_hamiltonian, synth_omega  # noqa: E402
 from oracle.oracle import Oracle  # noqa: E402
 
 
@@ -40,6 +46,32 @@ def emax6_flow():
     np.savez_compressed(out, trace=flow["trace"], steps=flow["steps"], ncomm=flow["ncomm"],
                         omega_norm=orc.norm(flow["Omega"]), seed=13, s_max=50.0, ds=0.5)
     print("wrote", out, "flow steps", flow["steps"], "E0", flow["trace"][-1, 2])
+
+
+def adjoint_fd():
+    import os as _os
+    from oracle.oracle import set_threads
+    set_threads(_os.cpu_count())
+    bas = ho_basis(4)
+    lay = Layout(**bas)
+    orc = Oracle(**bas)
+    T, V = adjoint_terms(lay)
+    c = np.ones(4)
+    h = 1e-4
+
+    def e0(cv):
+        f = orc.magnus_decouple(orc.normal_order(T + sum(ck * vk for ck, vk in zip(cv, V))), s_max=50.0, ds=0.5)
+        return f["trace"][-1, 2], f["steps"]
+
+    base, steps = e0(c)
+    fd = []
+    for k in range(4):
+        (ep, sp), (em, sm) = e0(c + h * np.eye(4)[k]), e0(c - h * np.eye(4)[k])
+        assert sp == sm == steps
+        fd.append((ep - em) / (2 * h))
+    out = os.path.join(os.path.dirname(os.path.abspath(__file__)), "adjoint_fd_emax4.npz")
+    np.savez_compressed(out, fd=np.array(fd), e0=base, steps=steps, h=h, c=c)
+    print("wrote", out, "dE0/dc", fd)
 
 
 def main():
@@ -65,6 +97,9 @@ def main():
 if __name__ == "__main__":
     if sys.argv[1:] == ["emax6"]:
         emax6_flow()
+    elif sys.argv[1:] == ["adjoint"]:
+        adjoint_fd()
     else:
         main()
         emax6_flow()
+        adjoint_fd()

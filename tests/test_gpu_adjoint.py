@@ -12,10 +12,12 @@
   against central finite differences (h = 1e-4) of the oracle's FP64 flow to
   convergence (|E_mbpt2| < 1e-6, the reference's stop) and against the
   tangent-linear flow, in FP64 and split precision."""
+import os
+
 import numpy as np
 import pytest
 
-from conftest import make_case
+from conftest import ROOT, make_case
 
 pytestmark = pytest.mark.gpu
 
@@ -70,25 +72,13 @@ def test_white_adjoint_against_central_differences(gpu_lib, oracle_mod):
     assert abs(got - fd) <= 1e-7 * max(1.0, abs(fd)), (got, fd)
 
 
-def _terms(lay):
-    from imsrg_gpu.synth import synth_hamiltonian
-    one = lay.off_fpp + lay.P * lay.P  # E0 + one-body part of the flat layout
-    T = synth_hamiltonian(lay, 300)
-    T[one:] = 0.0
-    V = []
-    for k in range(4):
-        v = synth_hamiltonian(lay, 301 + k)
-        v[:one] = 0.0
-        V.append(v)
-    return T, V
-
-
 @pytest.fixture(scope="module")
 def fd_case(oracle_mod):
     """The oracle's central differences of E0(s) at convergence."""
     bas, lay = make_case(4)
     orc = oracle_mod.Oracle(**bas)
-    T, V = _terms(lay)
+    from imsrg_gpu.synth import adjoint_terms
+    T, V = adjoint_terms(lay)
     c = np.ones(4)
 
     def H_of(cv):
@@ -142,3 +132,11 @@ def test_flow_adjoint_equals_tangent_flow(gpu_lib, fd_case):
     # the whole gradient: its dot product with each direction is grad
     hb = Hbar.download()
     np.testing.assert_allclose([np.dot(hb, d) for d in dirs], adj["grad"], rtol=1e-12, atol=1e-12)
+
+
+def test_committed_fd_fixture_is_the_oracles(fd_case):
+    """The oracle gradients bench.py reports the adjoint against
+    (tests/golden/adjoint_fd_emax4.npz) are the oracle's central differences."""
+    g = np.load(os.path.join(ROOT, "tests", "golden", "adjoint_fd_emax4.npz"))
+    np.testing.assert_allclose(g["fd"], fd_case[4], rtol=1e-9, atol=0)
+    assert int(g["steps"]) == fd_case[5]["steps"]
