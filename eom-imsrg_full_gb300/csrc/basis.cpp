@@ -343,10 +343,19 @@ int build_basis(imsrg_basis *b) {
     pb.add(r, r, nb, SRC_WCC, b->wcc_off[q1], r,
            {term(SRC_LCC, b->cc_off[q1], r, 0, SRC_RCC, b->cc_off[q1], r, 1, 1.0)});
   }
+  // FP64 tiles: 64 x 64, or 256 x 8 for the problems whose output has at
+  // most eight columns (the hole-pair-wide ladder products), which a 64-wide
+  // tile would mostly pad
   int tiles = 0;
   for (GemmProb &p : pb.probs) {
-    p.tiles_m = (p.M + 63) / 64;
-    p.tiles = p.tiles_m * ((p.N + 63) / 64);
+    p.shape = p.N <= 8 ? 1 : 0;
+    if (p.shape == 1) {
+      p.tiles_m = (p.M + 255) / 256;
+      p.tiles = p.tiles_m;
+    } else {
+      p.tiles_m = (p.M + 63) / 64;
+      p.tiles = p.tiles_m * ((p.N + 63) / 64);
+    }
     p.tile0 = tiles;
     tiles += p.tiles;
   }

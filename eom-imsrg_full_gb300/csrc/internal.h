@@ -154,6 +154,7 @@ struct GemmProb {
   int tile0;    // first tile id of this problem
   int tiles_m;  // tiles along M
   int tiles;    // tiles of this problem
+  int shape;    // FP64 tile: 0 = 64 x 64, 1 = 256 x 8 (problems with N <= 8)
 };
 
 struct Operands {

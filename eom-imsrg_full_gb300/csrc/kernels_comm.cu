@@ -77,9 +77,79 @@ __global__ void __launch_bounds__(256) k_cc_forward(DevTables T, const double *_
 }
 
 // ---------------------------------------------------------------------------
-// 2. Grouped FP64 GEMM: C = sum_t alpha_t op(A_t) op(B_t), 64x64 tiles.
+// 2. Grouped FP64 GEMM: C = sum_t alpha_t op(A_t) op(B_t), one problem
+//    list, tiles of 64 x 64 (4 x 4 outputs per thread: rows tx + 16 i,
+//    columns 4 ty + j, so warp w owns columns 8w .. 8w + 7 and skips the
+//    products when they all lie past N) or, for outputs of at most eight
+//    columns, 256 x 8 (one row of eight outputs per thread; warps whose rows
+//    all lie past M skip the products).  A last K chunk shorter than BK runs
+//    only its valid k.
 // ---------------------------------------------------------------------------
 constexpr int BM = 64, BN = 64, BK = 16;
+constexpr int TBM = 256, TBN = 8, TBK = 8;
+
+__device__ __forceinline__ void gemm_thin_tile(const GemmProb &P, int lt, const Operands &ops, int hL, int hR) {
+  __shared__ double As[TBK][TBM];
+  __shared__ double Bs[TBK][TBN];
+  const int tid = threadIdx.x;
+  const int m0 = lt * TBM;
+  const bool live = m0 + (tid & ~31) < P.M;  // warp-uniform
+  double acc[TBN];
+#pragma unroll
+  for (int j = 0; j < TBN; j++) acc[j] = 0.0;
+  for (int it = 0; it < P.nterms; it++) {
+    const GemmTerm &Tm = P.t[it];
+    const double *A = ops.src[Tm.a_src] + Tm.a_off;
+    const double *B = ops.src[Tm.b_src] + Tm.b_off;
+    const double alpha = Tm.coef * (Tm.use_hl ? hL : 1) * (Tm.use_hr ? hR : 1);
+    double part[TBN];
+#pragma unroll
+    for (int j = 0; j < TBN; j++) part[j] = 0.0;
+    for (int k0 = 0; k0 < P.K; k0 += TBK) {
+#pragma unroll
+      for (int l = 0; l < TBK; l++) {
+        const int idx = l * TBM + tid;
+        int m, k;
+        if (!Tm.ta) { m = idx % TBM; k = idx / TBM; }
+        else { k = idx % TBK; m = idx / TBK; }
+        const int gm = m0 + m, gk = k0 + k;
+        double v = 0.0;
+        if (gm < P.M && gk < P.K) v = Tm.ta ? A[gk + (long)gm * Tm.lda] : A[gm + (long)gk * Tm.lda];
+        As[k][m] = v;
+      }
+      if (tid < TBK * TBN) {
+        int n, k;
+        if (!Tm.tb) { k = tid % TBK; n = tid / TBK; }
+        else { n = tid % TBN; k = tid / TBN; }
+        const int gk = k0 + k;
+        double v = 0.0;
+        if (n < P.N && gk < P.K) v = Tm.tb ? B[n + (long)gk * Tm.ldb] : B[gk + (long)n * Tm.ldb];
+        Bs[k][n] = v;
+      }
+      __syncthreads();
+      if (live) {
+        const int kn = min(TBK, P.K - k0);
+#pragma unroll
+        for (int k = 0; k < TBK; k++) {
+          if (k < kn) {
+            const double a = As[k][tid];
+#pragma unroll
+            for (int j = 0; j < TBN; j++) part[j] = fma(a, Bs[k][j], part[j]);
+          }
+        }
+      }
+      __syncthreads();
+    }
+#pragma unroll
+    for (int j = 0; j < TBN; j++) acc[j] += alpha * part[j];
+  }
+  const int gm = m0 + tid;
+  if (gm >= P.M) return;
+  double *Cp = ops.dst[P.c_dst] + P.c_off;
+#pragma unroll
+  for (int j = 0; j < TBN; j++)
+    if (j < P.N) Cp[gm + (long)j * P.ldc] = acc[j];
+}
 
 __global__ void __launch_bounds__(256) k_gemm_fp64(const GemmProb *__restrict__ probs, int nprobs, Operands ops,
                                                    int hL, int hR) {
@@ -95,8 +165,13 @@ __global__ void __launch_bounds__(256) k_gemm_fp64(const GemmProb *__restrict__ 
   }
   const GemmProb &P = probs[lo - 1];
   int lt = tile - P.tile0;
+  if (P.shape == 1) {  // block-uniform
+    gemm_thin_tile(P, lt, ops, hL, hR);
+    return;
+  }
   int m0 = (lt % P.tiles_m) * BM, n0 = (lt / P.tiles_m) * BN;
   int tid = threadIdx.x, tx = tid & 15, ty = tid >> 4;
+  const bool live = n0 + 8 * (tid >> 5) < P.N;  // warp-uniform: the warp's eight columns
   double acc[4][4];
 #pragma unroll
   for (int i = 0; i < 4; i++)
@@ -136,17 +211,20 @@ __global__ void __launch_bounds__(256) k_gemm_fp64(const GemmProb *__restrict__ 
         Bs[k][n] = v;
       }
       __syncthreads();
+      const int kn = live ? min(BK, P.K - k0) : 0;
 #pragma unroll
       for (int k = 0; k < BK; k++) {
-        double a[4], bv[4];
+        if (k < kn) {
+          double a[4], bv[4];
 #pragma unroll
-        for (int i = 0; i < 4; i++) a[i] = As[k][tx + 16 * i];
+          for (int i = 0; i < 4; i++) a[i] = As[k][tx + 16 * i];
 #pragma unroll
-        for (int j = 0; j < 4; j++) bv[j] = Bs[k][ty + 16 * j];
+          for (int j = 0; j < 4; j++) bv[j] = Bs[k][4 * ty + j];
 #pragma unroll
-        for (int i = 0; i < 4; i++)
+          for (int i = 0; i < 4; i++)
 #pragma unroll
-          for (int j = 0; j < 4; j++) part[i][j] = fma(a[i], bv[j], part[i][j]);
+            for (int j = 0; j < 4; j++) part[i][j] = fma(a[i], bv[j], part[i][j]);
+        }
       }
       __syncthreads();
     }
@@ -158,7 +236,7 @@ __global__ void __launch_bounds__(256) k_gemm_fp64(const GemmProb *__restrict__ 
   double *Cp = ops.dst[P.c_dst] + P.c_off;
 #pragma unroll
   for (int j = 0; j < 4; j++) {
-    int gn = n0 + ty + 16 * j;
+    int gn = n0 + 4 * ty + j;
     if (gn >= P.N) continue;
 #pragma unroll
     for (int i = 0; i < 4; i++) {
