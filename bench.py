@@ -157,13 +157,45 @@ def dist_setup():
     return world, rank, local
 
 
-def cpu_baseline(orb, lay, seconds: float = 12.0, threads: int | None = None):
-    """The oracle (C restatement of the reference CPU path) on host cores."""
+def cpu_oracle(orb, threads: int):
+    """The fastest CPU configuration of the oracle (the C restatement of the
+    reference's CPU path) on `threads` OpenMP threads: its timed build
+    (-O3, contraction allowed) with its own blocked GEMM, or with numpy's
+    bundled OpenBLAS dgemm (the reference links a system BLAS).  Each is timed
+    for about two seconds on the emax=6 commutator; returns (oracle, label,
+    {label: commutators/s})."""
     from oracle import oracle
+    from imsrg_gpu.layout import Layout
+    from imsrg_gpu.synth import synth_hamiltonian, synth_omega
+    oracle.set_threads(threads)
+    lay = Layout(**orb)
+    Hh, Oh = synth_hamiltonian(lay, 1), synth_omega(lay, 1)
+    rates = {}
+    for label in ("own blocked GEMM", "OpenBLAS"):
+        if label == "OpenBLAS":
+            desc = oracle.use_blas(threads)
+            if desc is None:
+                break
+            label = "OpenBLAS dgemm (" + " ".join(desc.split()[:2]) + ", numpy's ILP64 build)"
+        orc = oracle.Oracle(**orb, variant="fast")
+        orc.commutator(Oh, -1, Hh, 1)
+        n, t0 = 0, time.perf_counter()
+        while time.perf_counter() - t0 < 2.0:
+            orc.commutator(Oh, -1, Hh, 1)
+            n += 1
+        rates[label] = n / (time.perf_counter() - t0)
+    best = max(rates, key=rates.get)
+    if not best.startswith("OpenBLAS"):
+        oracle.lib("fast").orc_set_dgemm(None)
+    return oracle.Oracle(**orb, variant="fast"), best, rates
+
+
+def cpu_baseline(orb, lay, seconds: float = 12.0, threads: int | None = None):
+    """The oracle (C restatement of the reference CPU path) on host cores, in
+    its fastest configuration (cpu_oracle)."""
     from imsrg_gpu.synth import synth_hamiltonian, synth_omega
     threads = threads or os.cpu_count()
-    oracle.set_threads(threads)
-    orc = oracle.Oracle(**orb)
+    orc, blas, rates = cpu_oracle(orb, threads)
     Hh, Oh = synth_hamiltonian(lay, 1), synth_omega(lay, 1)
     orc.commutator(Oh, -1, Hh, 1)  # warm
     n, t0 = 0, time.perf_counter()
@@ -174,7 +206,9 @@ def cpu_baseline(orb, lay, seconds: float = 12.0, threads: int | None = None):
         if dt >= seconds or n >= 400:
             break
     return {"value": n / dt, "unit": UNIT, "cores": threads, "kind": "port",
-            "sample": f"{n} emax=6 [Omega,H] commutators in {dt:.1f} s (OpenMP C oracle, own FP64 GEMM)"}
+            "sample": f"{n} emax=6 [Omega,H] commutators in {dt:.1f} s (OpenMP C oracle, -O3 -ffp-contract=fast, "
+                      f"{blas})",
+            "blas": blas, "calibration_rates": rates}
 
 
 def run_reference(args, world, rank):
@@ -186,8 +220,7 @@ def run_reference(args, world, rank):
     orb = ho_basis(EMAX)
     lay = Layout(**orb)
     threads = os.cpu_count()
-    oracle.set_threads(threads)
-    orc = oracle.Oracle(**orb)
+    orc, blas, rates = cpu_oracle(orb, threads)
     Hh, Oh = synth_hamiltonian(lay, 1), synth_omega(lay, 1)
     for _ in range(args.warmup):
         orc.commutator(Oh, -1, Hh, 1)
@@ -202,7 +235,8 @@ def run_reference(args, world, rank):
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
         "config": {"workload": "emax=6 [Omega,H] commutator, 16O, 56 j-orbits", "emax": EMAX},
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
-                         "sample": f"{args.steps} commutators after {args.warmup} warm-up (OpenMP C oracle)"},
+                         "sample": f"{args.steps} commutators after {args.warmup} warm-up (OpenMP C oracle, "
+                                   f"-O3 -ffp-contract=fast, {blas})", "blas": blas, "calibration_rates": rates},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)

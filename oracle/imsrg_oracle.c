@@ -524,9 +524,25 @@ static double twobody_monopole(const obasis *b, int a, int bb, int ja, int jb, c
  * reassociation). */
 #define GEMM_NB 8
 #define GEMM_MB 128
+/* An external BLAS dgemm (Fortran interface with 64-bit integers, e.g. the
+ * OpenBLAS that numpy bundles) used in place of the oracle's own GEMM when set
+ * by orc_set_dgemm: the timed CPU baseline, where the reference links a system
+ * BLAS (makefile_gfortran:14).  Calls whose arguments a BLAS would reject
+ * (empty contraction, leading dimension 0) stay with the oracle's own GEMM. */
+typedef void (*ext_dgemm_t)(const char *, const char *, const long *, const long *, const long *, const double *,
+                            const double *, const long *, const double *, const long *, const double *, double *,
+                            const long *, size_t, size_t);
+static ext_dgemm_t g_ext_dgemm = 0;
+void orc_set_dgemm(void *fn) { g_ext_dgemm = (ext_dgemm_t)fn; }
+
 static void dgemm_(char ta, char tb, int m, int n, int k, double alpha, const double *A, int lda, const double *B,
                    int ldb, double beta, double *C, int ldc) {
   if (m <= 0 || n <= 0) return;
+  if (g_ext_dgemm && k > 0 && lda >= ((ta == 'N') ? m : k) && ldb >= ((tb == 'N') ? k : n) && ldc >= m) {
+    const long M = m, N = n, K = k, LDA = lda, LDB = ldb, LDC = ldc;
+    g_ext_dgemm(&ta, &tb, &M, &N, &K, &alpha, A, &LDA, B, &LDB, &beta, C, &LDC, 1, 1);
+    return;
+  }
   double *Ap = malloc(((long)m * (k > 0 ? k : 1)) * sizeof(double));
   double *Bp = malloc(((long)k * n + 1) * sizeof(double));
   for (int l = 0; l < k; l++)
