@@ -48,7 +48,9 @@ namespace {
 // ---------------------------------------------------------------------------
 // Grouped FP64 products of the adjoint: C += sum_t alpha_t op(A_t) op(B_t),
 // each term with its own contraction length (the transposed ladder products
-// of one output array read different intermediates).
+// of one output array read different intermediates).  64 x 64 tiles laid out
+// as the forward's k_gemm_fp64: warp w owns columns 8w .. 8w + 7 and skips
+// its products when they lie past N; a short last K chunk runs only its k.
 // ---------------------------------------------------------------------------
 struct AdjTerm {
   int a_src, b_src, ta, tb;
@@ -90,6 +92,7 @@ __global__ void __launch_bounds__(256) k_gemm_adj(const AdjProb *__restrict__ pr
   const int lt = tile - P.tile0;
   const int m0 = (lt % P.tiles_m) * BM, n0 = (lt / P.tiles_m) * BN;
   const int tid = threadIdx.x, tx = tid & 15, ty = tid >> 4;
+  const bool live = n0 + 8 * (tid >> 5) < P.N;  // warp-uniform: the warp's eight columns 4 ty + j
   double acc[4][4];
 #pragma unroll
   for (int i = 0; i < 4; i++)
@@ -127,17 +130,20 @@ __global__ void __launch_bounds__(256) k_gemm_adj(const AdjProb *__restrict__ pr
         Bs[k][n] = v;
       }
       __syncthreads();
+      const int kn = live ? min(BK, Tm.K - k0) : 0;
 #pragma unroll
       for (int k = 0; k < BK; k++) {
-        double a[4], bv[4];
+        if (k < kn) {
+          double a[4], bv[4];
 #pragma unroll
-        for (int i = 0; i < 4; i++) a[i] = As[k][tx + 16 * i];
+          for (int i = 0; i < 4; i++) a[i] = As[k][tx + 16 * i];
 #pragma unroll
-        for (int j = 0; j < 4; j++) bv[j] = Bs[k][ty + 16 * j];
+          for (int j = 0; j < 4; j++) bv[j] = Bs[k][4 * ty + j];
 #pragma unroll
-        for (int i = 0; i < 4; i++)
+          for (int i = 0; i < 4; i++)
 #pragma unroll
-          for (int j = 0; j < 4; j++) part[i][j] = fma(a[i], bv[j], part[i][j]);
+            for (int j = 0; j < 4; j++) part[i][j] = fma(a[i], bv[j], part[i][j]);
+        }
       }
       __syncthreads();
     }
@@ -149,7 +155,7 @@ __global__ void __launch_bounds__(256) k_gemm_adj(const AdjProb *__restrict__ pr
   double *Cp = ops.dst[P.c_dst] + P.c_off;
 #pragma unroll
   for (int j = 0; j < 4; j++) {
-    const int gn = n0 + ty + 16 * j;
+    const int gn = n0 + 4 * ty + j;
     if (gn >= P.N) continue;
 #pragma unroll
     for (int i = 0; i < 4; i++) {

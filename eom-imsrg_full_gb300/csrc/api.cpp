@@ -1247,6 +1247,13 @@ int imsrg_gpu_split_digits_set(imsrg_basis_t *b, int digits) {
   return IMSRG_OK;
 }
 
+int imsrg_gpu_split_chunk_set(imsrg_basis_t *b, int steps) {
+  if (!b || steps < 0) return IMSRG_ERR_INVALID;
+  if (b->ozaki) return steps == b->split_chunk_steps ? IMSRG_OK : IMSRG_ERR_INVALID;  // plan already built
+  b->split_chunk_steps = steps;
+  return IMSRG_OK;
+}
+
 int imsrg_gpu_split_schedule_set(imsrg_basis_t *b, int model) {
   if (!b) return IMSRG_ERR_INVALID;
   cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;

@@ -281,6 +281,7 @@ struct imsrg_basis {
   // Ozaki split-precision engine state (allocated on first use)
   void *ozaki = nullptr;
   int split_digits = 6;  // digits per operand of the split engine (4, 5 or 6), fixed once its plan exists
+  int split_chunk_steps = 0;  // K steps per exact accumulator chunk (0: the largest exact one)
   // Reverse-mode (adjoint) workspace (adjoint.cu), allocated on first use
   void *adjoint = nullptr;
   // Graph of one Magnus flow step (graph.cu), built on first use

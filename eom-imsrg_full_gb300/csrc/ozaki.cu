@@ -67,6 +67,10 @@ constexpr int OZ_NACC = 4;                   // accumulators: levels 2, 3, 4 exa
 __host__ __device__ constexpr int oz_bplanes(int S) { return S == 6 ? 15 : S == 5 ? 9 : 4; }
 __host__ __device__ constexpr int oz_plane_off(int S, int j) { return j == 0 ? 0 : j == 1 ? S : 2 * S - 1; }
 constexpr int TM = 128, TN = 64, TK = 16;
+// Largest chunk of a tile's K steps whose FP32 level sums stay exact:
+// steps x TK x 5 x 2^12 < 2^24.
+constexpr int kOzChunkSteps = (16777216 - 1) / (TK * 5 * 4096);
+static_assert(kOzChunkSteps * TK * 5 * 4096 < 16777216, "chunk bound");
 constexpr int STAGES = 4;
 // Lines (8 elements each) per slicing CTA: small CTAs spread the ~100,000
 // lines of a part evenly over the SMs (emax=6: with 256, the SMs were busy
@@ -113,6 +117,11 @@ struct OzTerm {
 
 struct OzProb {
   int M, N, K, ksteps, nterms;
+  // The (term, K step) sequence of a tile, term-major, runs in chunks of
+  // kchunk steps, each into a fresh accumulator set: a chunk's FP32 level sums
+  // stay exact integers (kchunk TK 5 2^12 < 2^24) and the epilogue adds the
+  // chunks' int64 level sums exactly before the one conversion.
+  int kchunk, nchunks;
   OzTerm t[2];
   double *C;
   int ldc;
@@ -131,6 +140,8 @@ constexpr SchedModel kSchedModels[kNumSchedModels] = {{4, 20, 4}, {4, 0, 1}, {4,
 
 struct OzPlan {
   int S = OZ_SMAX;  // digits per operand
+  int chunk_steps = kOzChunkSteps;  // K steps per accumulator chunk (<= kOzChunkSteps)
+  bool chunked = false;             // some problem runs in more than one chunk
   std::vector<OzMatrix> mats;
   std::vector<OzChunk> chunks;
   std::vector<OzProb> probs;
@@ -417,7 +428,9 @@ __global__ void __launch_bounds__(SLICE_THREADS) k_oz_slice(const OzMatrix *__re
 // 3. tensor-core products and exact recombination
 // ---------------------------------------------------------------------------
 
-template <int S>
+// CH: the plan has contractions in several chunks (see OzProb); without any,
+// the chunk bookkeeping folds away at compile time.
+template <int S, bool CH>
 __global__ void __launch_bounds__(OZ_THREADS, 1) k_oz_mma(const OzProb *__restrict__ probs, int nprobs,
                                                           const int2 *__restrict__ sched,
                                                           const int *__restrict__ sched_off,
@@ -475,7 +488,7 @@ __global__ void __launch_bounds__(OZ_THREADS, 1) k_oz_mma(const OzProb *__restri
         for (int it = 0; it < P.nterms; it++) {
           const OzTerm &T = P.t[it];
           const CUtensorMap *amap = maps + T.a_map, *bmap = maps + T.b_map;
-          for (int kk = 0; kk < P.ksteps; kk++) {
+          for (int kk = 0; kk < P.ksteps; kk++) {  // the chunks only regroup these steps
             if (!mbar_wait(&empty[stage], phase ^ 1, abort_flag)) {
               atomicExch(err, 1);
               *abort_flag = 1;
@@ -507,24 +520,32 @@ __global__ void __launch_bounds__(OZ_THREADS, 1) k_oz_mma(const OzProb *__restri
       for (int ti = t_begin; ti < t_end && !*abort_flag; ti++) {
         const OzProb &P = probs[sched[ti].x];
         if (P.ksteps == 0) continue;
-        int buf = nt & 1;
-        uint32_t use = (uint32_t)(nt >> 1);
-        nt++;
-        if (!mbar_wait(&acc_empty[buf], (use & 1) ^ 1, abort_flag)) {
-          atomicExch(err, 2);
-          *abort_flag = 1;
-          break;
-        }
-        tc_fence_after();
-        const uint32_t dbase = tmem + (uint32_t)(buf * ACC_BUF_COLS);
-        bool first = true;  // first K step of the tile overwrites the accumulators
         const uint64_t desc0 = smem_desc(smem_u32(smem), 128, 256);
+        const int kchunk = CH ? P.kchunk : 0x40000000;
+        int left = 0;                          // steps left in the current chunk
+        int total = P.nterms * P.ksteps;       // steps left in the tile
+        uint32_t dbase = 0;
+        bool first = true;  // first K step of a chunk overwrites the accumulators
         for (int it = 0; it < P.nterms && !*abort_flag; it++) {
           const OzTerm &T = P.t[it];
           int neg = T.neg ^ (T.use_hl & (hL < 0)) ^ (T.use_hr & (hR < 0));
           const uint32_t idesc = idesc_bf16(TM, TN, neg);
           const uint32_t idesc2 = idesc_bf16(TM, 2 * TN, neg), idesc3 = idesc_bf16(TM, 3 * TN, neg);
           for (int kk = 0; kk < P.ksteps; kk++) {
+            if (left == 0) {  // a chunk starts: take the next accumulator set
+              const int buf = nt & 1;
+              const uint32_t use = (uint32_t)(nt >> 1);
+              nt++;
+              if (!mbar_wait(&acc_empty[buf], (use & 1) ^ 1, abort_flag)) {
+                atomicExch(err, 2);
+                *abort_flag = 1;
+                break;
+              }
+              tc_fence_after();
+              dbase = tmem + (uint32_t)(buf * ACC_BUF_COLS);
+              first = true;
+              left = kchunk;
+            }
             if (!mbar_wait(&full[stage], phase, abort_flag)) {
               atomicExch(err, 3);
               *abort_flag = 1;
@@ -560,9 +581,12 @@ __global__ void __launch_bounds__(OZ_THREADS, 1) k_oz_mma(const OzProb *__restri
               stage = 0;
               phase ^= 1;
             }
+            // a chunk ends: its accumulator set goes to the epilogue
+            --left;
+            --total;
+            if (left == 0 || total == 0) mma_commit(&acc_full[(nt - 1) & 1]);
           }
         }
-        mma_commit(&acc_full[buf]);
       }
     }
   } else {
@@ -578,6 +602,7 @@ __global__ void __launch_bounds__(OZ_THREADS, 1) k_oz_mma(const OzProb *__restri
       // problem fields in registers: the stores below could alias the problem
       // table as far as the compiler knows, which would force a reload per column
       const int Mp = P.M, Np = P.N, ldc = P.ldc, ksteps = P.ksteps, gA = P.gA, gB = P.gB;
+      const int nch = CH ? P.nchunks : 1, raw = P.raw;
       const int tiles_m = P.tiles_m;
       double *const Cbase = P.C;
       const int m0 = (lt % tiles_m) * TM;
@@ -590,70 +615,92 @@ __global__ void __launch_bounds__(OZ_THREADS, 1) k_oz_mma(const OzProb *__restri
           for (int c = 0; c < 16 && n0 + c < Np; c++) crow[(long)(n0 + c) * ldc] = 0.0;
         continue;
       }
-      int buf = nt & 1;
-      uint32_t use = (uint32_t)(nt >> 1);
-      nt++;
-      if (*abort_flag) break;
-      if (!mbar_wait(&acc_full[buf], use & 1, abort_flag)) {
-        atomicExch(err, 4);
-        *abort_flag = 1;
-        break;
-      }
-      tc_fence_after();
       // warp-uniform: a piece entirely past M or N is neither read nor converted
       const bool live = m0 + quad * 32 < Mp && n0 < Np;
-      uint32_t acc[OZ_NACC][16];
-      if (live) {
+      // A tile in several chunks adds the chunks' exact level sums in the
+      // output's own 8-byte slots (each thread owns its elements), as int64,
+      // until the last chunk converts
+      long long *irow = reinterpret_cast<long long *>(crow);
+      for (int ch = 0; ch < nch; ch++) {
+        const int buf = nt & 1;
+        const uint32_t use = (uint32_t)(nt >> 1);
+        nt++;
+        if (*abort_flag || !mbar_wait(&acc_full[buf], use & 1, abort_flag)) {
+          if (!*abort_flag) atomicExch(err, 4);
+          *abort_flag = 1;
+          break;
+        }
+        tc_fence_after();
+        uint32_t acc[OZ_NACC][16];
+        if (live) {
 #pragma unroll
-        for (int l = 0; l < OZ_NACC; l++)
-          tmem_ld16(tmem + ((uint32_t)(quad * 32) << 16) + (uint32_t)(buf * ACC_BUF_COLS + l * TN + 16 * chunk),
-                    acc[l]);
-      }
-      tmem_ld_wait();
-      // the accumulators are in registers: hand the TMEM set back to the MMA issuer
-      tc_fence_before();
-      __syncwarp();
-      if (lane == 0) mbar_arrive(&acc_empty[buf]);
-      if (!live) continue;
-      if (P.raw) {
-        // WCC: the exact level sum stays an integer (the 222_ph recoupling
+          for (int l = 0; l < OZ_NACC; l++)
+            tmem_ld16(tmem + ((uint32_t)(quad * 32) << 16) + (uint32_t)(buf * ACC_BUF_COLS + l * TN + 16 * chunk),
+                      acc[l]);
+        }
+        tmem_ld_wait();
+        // the accumulators are in registers: hand the TMEM set back to the MMA issuer
+        tc_fence_before();
+        __syncwarp();
+        if (lane == 0) mbar_arrive(&acc_empty[buf]);
+        if (!live) continue;
+        // exact integer levels 2..4 and the rounded tail, in units of level
+        // S + 1 (hardware conversions: measured faster here than assembling
+        // the double from integer bit operations)
+#define OZ_LEVEL_SUM(c)                                                                   \
+  (((long long)__float2int_rn(__uint_as_float(acc[0][c])) << (7 * (LMAX - 2))) +         \
+   ((long long)__float2int_rn(__uint_as_float(acc[1][c])) << (7 * (LMAX - 3))) +         \
+   ((long long)__float2int_rn(__uint_as_float(acc[2][c])) << (7 * (LMAX - 4))) +         \
+   __float2ll_rn(__uint_as_float(acc[3][c])))
+        if (nch == 1 && !raw) {
+          const int k = (exps[gA] - 1022) + (exps[gB] - 1022) - 7 * LMAX;  // result = v * 2^k
+#pragma unroll
+          for (int c = 0; c < 16; c++) {
+            double d = (double)OZ_LEVEL_SUM(c);
+            // scale by 2^k: add k to the exponent field on the integer pipe
+            unsigned long long bits = (unsigned long long)__double_as_longlong(d);
+            const int E = (int)((bits >> 52) & 0x7FF);
+            if (E != 0 && E + k > 0 && E + k < 2047) {
+              bits += (unsigned long long)(long long)k << 52;
+              d = __longlong_as_double((long long)bits);
+            } else if (E != 0) {
+              d = ldexp(d, k);
+            }
+            const int n = n0 + c;
+            if (row_ok && n < Np) crow[(long)n * ldc] = d;
+          }
+          continue;
+        }
+        // WCC keeps the exact level sum as an integer (the 222_ph recoupling
         // combines four entries of one block, which share 2^k, before its one
-        // conversion to FP64)
-        long long *irow = reinterpret_cast<long long *>(crow);
+        // conversion to FP64); a long contraction adds its chunks there
 #pragma unroll
         for (int c = 0; c < 16; c++) {
-          const long long v = ((long long)__float2int_rn(__uint_as_float(acc[0][c])) << (7 * (LMAX - 2))) +
-                              ((long long)__float2int_rn(__uint_as_float(acc[1][c])) << (7 * (LMAX - 3))) +
-                              ((long long)__float2int_rn(__uint_as_float(acc[2][c])) << (7 * (LMAX - 4))) +
-                              __float2ll_rn(__uint_as_float(acc[3][c]));
+          long long v = OZ_LEVEL_SUM(c);
           const int n = n0 + c;
-          if (row_ok && n < Np) irow[(long)n * ldc] = v;
+          if (row_ok && n < Np) {
+            if (ch > 0) v += irow[(long)n * ldc];
+            irow[(long)n * ldc] = v;
+          }
         }
-        continue;
-      }
-      const int k = (exps[gA] - 1022) + (exps[gB] - 1022) - 7 * LMAX;  // result = v * 2^k
-#pragma unroll
-      for (int c = 0; c < 16; c++) {
-        // exact integer levels 2..4 and the rounded tail, in units of level S + 1
-        // (hardware conversions: measured faster here than assembling the
-        // double from integer bit operations)
-        long long v = ((long long)__float2int_rn(__uint_as_float(acc[0][c])) << (7 * (LMAX - 2))) +
-                      ((long long)__float2int_rn(__uint_as_float(acc[1][c])) << (7 * (LMAX - 3))) +
-                      ((long long)__float2int_rn(__uint_as_float(acc[2][c])) << (7 * (LMAX - 4))) +
-                      __float2ll_rn(__uint_as_float(acc[3][c]));
-        double d = (double)v;
-        // scale by 2^k: add k to the exponent field on the integer pipe
-        unsigned long long bits = (unsigned long long)__double_as_longlong(d);
-        const int E = (int)((bits >> 52) & 0x7FF);
-        if (E != 0 && E + k > 0 && E + k < 2047) {
-          bits += (unsigned long long)(long long)k << 52;
-          d = __longlong_as_double((long long)bits);
-        } else if (E != 0) {
-          d = ldexp(d, k);
+        if (raw || ch < nch - 1 || !row_ok) continue;
+        // the last chunk of a long FP64 contraction: convert the summed integers
+        const int k = (exps[gA] - 1022) + (exps[gB] - 1022) - 7 * LMAX;
+        for (int c = 0; c < 16 && n0 + c < Np; c++) {
+          double d = (double)irow[(long)(n0 + c) * ldc];
+          unsigned long long bits = (unsigned long long)__double_as_longlong(d);
+          const int E = (int)((bits >> 52) & 0x7FF);
+          if (E != 0 && E + k > 0 && E + k < 2047) {
+            bits += (unsigned long long)(long long)k << 52;
+            d = __longlong_as_double((long long)bits);
+          } else if (E != 0) {
+            d = ldexp(d, k);
+          }
+          crow[(long)(n0 + c) * ldc] = d;
         }
-        const int n = n0 + c;
-        if (row_ok && n < Np) crow[(long)n * ldc] = d;
+#undef OZ_LEVEL_SUM
       }
+      if (*abort_flag) break;
     }
   }
   tc_fence_before();
@@ -666,14 +713,21 @@ __global__ void __launch_bounds__(OZ_THREADS, 1) k_oz_mma(const OzProb *__restri
 
 OzPlan *plan_of(imsrg_basis *b) { return (OzPlan *)b->ozaki; }
 
-void launch_mma(int S, int grid, cudaStream_t st, const OzProb *probs, int nprobs, const int2 *sched,
+void launch_mma(int S, bool chunked, int grid, cudaStream_t st, const OzProb *probs, int nprobs, const int2 *sched,
                 const int *sched_off, const int *exps, int hL, int hR, int *err, const CUtensorMap *maps) {
-  if (S == 4)
-    k_oz_mma<4><<<grid, OZ_THREADS, oz_mma_smem(4), st>>>(probs, nprobs, sched, sched_off, exps, hL, hR, err, maps);
-  else if (S == 5)
-    k_oz_mma<5><<<grid, OZ_THREADS, oz_mma_smem(5), st>>>(probs, nprobs, sched, sched_off, exps, hL, hR, err, maps);
-  else
-    k_oz_mma<6><<<grid, OZ_THREADS, oz_mma_smem(6), st>>>(probs, nprobs, sched, sched_off, exps, hL, hR, err, maps);
+#define OZ_LAUNCH(SS, CC) \
+  k_oz_mma<SS, CC><<<grid, OZ_THREADS, oz_mma_smem(SS), st>>>(probs, nprobs, sched, sched_off, exps, hL, hR, err, maps)
+  if (S == 4) {
+    if (chunked) OZ_LAUNCH(4, true);
+    else OZ_LAUNCH(4, false);
+  } else if (S == 5) {
+    if (chunked) OZ_LAUNCH(5, true);
+    else OZ_LAUNCH(5, false);
+  } else {
+    if (chunked) OZ_LAUNCH(6, true);
+    else OZ_LAUNCH(6, false);
+  }
+#undef OZ_LAUNCH
 }
 
 // CTA schedule: longest-processing-time-first assignment of tiles to the
@@ -727,7 +781,7 @@ int autotune(imsrg_basis *b, OzPlan *pl, int hL, int hR) {
   IMSRG_CUDA_TRY(cudaEventCreate(&e1));
   auto launch_timed = [&](float *ms) -> int {
     IMSRG_CUDA_TRY(cudaEventRecord(e0, b->stream));
-    launch_mma(pl->S, pl->grid, b->stream, pl->d_probs, pl->nprobs, pl->d_sched, pl->d_sched_off, pl->d_exps, hL, hR,
+    launch_mma(pl->S, pl->chunked, pl->grid, b->stream, pl->d_probs, pl->nprobs, pl->d_sched, pl->d_sched_off, pl->d_exps, hL, hR,
                pl->d_err, pl->d_maps);
     b->launches++;
     IMSRG_CUDA_TRY(cudaEventRecord(e1, b->stream));
@@ -768,6 +822,7 @@ int ozaki_prepare(imsrg_basis *b) {
   OzPlan *pl = new OzPlan();
   b->ozaki = pl;
   pl->S = b->split_digits;
+  if (b->split_chunk_steps > 0) pl->chunk_steps = std::min(b->split_chunk_steps, kOzChunkSteps);
   if (pl->S < 4 || pl->S > 6) return IMSRG_ERR_INVALID;
   int dev = b->device, major = 0, nsm = 0;
   IMSRG_CUDA_TRY(cudaDeviceGetAttribute(&major, cudaDevAttrComputeCapabilityMajor, dev));
@@ -982,9 +1037,17 @@ int ozaki_prepare(imsrg_basis *b) {
       o.use_hl = t.use_hl;
       o.use_hr = t.use_hr;
     }
-    // exactness bound of the FP32 level accumulators
-    // (levels 2..4 are exact integers; the tail of 5..7 is rounded FP32)
-    if ((double)p.nterms * p.K * (4 + 1) * 4096.0 >= 16777216.0) return IMSRG_ERR_INVALID;
+    // exactness bound of the FP32 level accumulators (levels 2..4 are exact
+    // integers while their sums stay below 2^24; each product adds at most
+    // 5 x 2^12 per element): a chunk holds at most kOzChunkSteps steps of
+    // TK, and longer contractions run in several chunks
+    {
+      const int steps = p.nterms * p.ksteps;
+      const int lim = std::min(kOzChunkSteps, std::max(1, pl->chunk_steps));
+      p.kchunk = std::max(1, std::min(steps, lim));
+      p.nchunks = steps > 0 ? (steps + p.kchunk - 1) / p.kchunk : 0;
+      if (p.nchunks > 1) pl->chunked = true;
+    }
     p.tiles_m = (p.M + TM - 1) / TM;
     p.tiles = p.tiles_m * ((p.N + TN - 1) / TN);
     p.tile0 = tiles;
@@ -1026,12 +1089,14 @@ int ozaki_prepare(imsrg_basis *b) {
   IMSRG_CUDA_TRY(cudaMalloc((void **)&pl->d_exps, std::max(pl->ngroups, 1) * sizeof(int)));
   IMSRG_CUDA_TRY(cudaMalloc((void **)&pl->d_err, sizeof(int)));
   IMSRG_CUDA_TRY(cudaMemset(pl->d_err, 0, sizeof(int)));
-  IMSRG_CUDA_TRY(pl->S == 4   ? cudaFuncSetAttribute(k_oz_mma<4>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                                     oz_mma_smem(4))
-                 : pl->S == 5 ? cudaFuncSetAttribute(k_oz_mma<5>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                                     oz_mma_smem(5))
-                              : cudaFuncSetAttribute(k_oz_mma<6>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                                     oz_mma_smem(6)));
+  {
+    const int sm = oz_mma_smem(pl->S);
+    const void *fn[2] = {pl->S == 4 ? (const void *)k_oz_mma<4, false>
+                                    : pl->S == 5 ? (const void *)k_oz_mma<5, false> : (const void *)k_oz_mma<6, false>,
+                         pl->S == 4 ? (const void *)k_oz_mma<4, true>
+                                    : pl->S == 5 ? (const void *)k_oz_mma<5, true> : (const void *)k_oz_mma<6, true>};
+    for (const void *f : fn) IMSRG_CUDA_TRY(cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, sm));
+  }
 
   int herr = 0;
   IMSRG_CUDA_TRY(cudaMemcpy(&herr, pl->d_err, sizeof(int), cudaMemcpyDeviceToHost));
@@ -1084,7 +1149,7 @@ int ozaki_mma(imsrg_basis *b, int hL, int hR) {
     if (cs == cudaStreamCaptureStatusNone) IMSRG_TRY(autotune(b, pl, hL, hR));
   }
   ProfScope ps(b, IMSRG_KERNEL_OZAKI_MMA);
-  launch_mma(pl->S, pl->grid, b->stream, pl->d_probs, pl->nprobs, pl->d_sched, pl->d_sched_off, pl->d_exps, hL, hR,
+  launch_mma(pl->S, pl->chunked, pl->grid, b->stream, pl->d_probs, pl->nprobs, pl->d_sched, pl->d_sched_off, pl->d_exps, hL, hR,
              pl->d_err, pl->d_maps);
   b->launches++;
   return cuda_status(cudaGetLastError());
@@ -1156,6 +1221,7 @@ struct OzBatch {
   std::vector<int> exps_base;
   OzProb *d_probs = nullptr;
   int nprobs = 0, grid = 0, ngroups = 0;
+  bool chunked = false;  // some merged problem runs in more than one chunk
   int2 *d_sched = nullptr;
   int *d_sched_off = nullptr, *d_exps = nullptr, *d_err = nullptr;
   CUtensorMap *d_maps = nullptr;
@@ -1188,6 +1254,7 @@ int ozaki_batch_create(imsrg_basis *const *bases, int n, void **out) {
     OzPlan *pl = plan_of(bases[i]);
     if (!pl || !pl->ok || bases[i]->device != bases[0]->device) return fail(IMSRG_ERR_INVALID);
     bt->plans.push_back(pl);
+    bt->chunked = bt->chunked || pl->chunked;
     if (pl->S != bt->plans[0]->S) return fail(IMSRG_ERR_INVALID);  // one digit count per merged launch
     bt->exps_base.push_back(bt->ngroups);
     const int p0 = (int)probs.size(), m0 = (int)maps.size();
@@ -1246,7 +1313,7 @@ int ozaki_batch_mma(void *batch, cudaStream_t st, int hL, int hR) {
     if (bt->plans[i]->ngroups > 0)
       IMSRG_CUDA_TRY(cudaMemcpyAsync(bt->d_exps + bt->exps_base[i], bt->plans[i]->d_exps,
                                      bt->plans[i]->ngroups * sizeof(int), cudaMemcpyDeviceToDevice, st));
-  launch_mma(bt->plans[0]->S, bt->grid, st, bt->d_probs, bt->nprobs, bt->d_sched, bt->d_sched_off, bt->d_exps, hL,
+  launch_mma(bt->plans[0]->S, bt->chunked, bt->grid, st, bt->d_probs, bt->nprobs, bt->d_sched, bt->d_sched_off, bt->d_exps, hL,
              hR, bt->d_err, bt->d_maps);
   return cuda_status(cudaGetLastError());
 }

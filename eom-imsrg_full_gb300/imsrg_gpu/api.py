@@ -42,7 +42,7 @@ SYMBOLS = (
     "imsrg_gpu_batch_create", "imsrg_gpu_batch_commutator", "imsrg_gpu_batch_destroy",
     "imsrg_gpu_magnus_rules", "imsrg_gpu_magnus_decouple_checkpoint",
     "imsrg_gpu_commutator_adjoint", "imsrg_gpu_white_adjoint", "imsrg_gpu_op_dot",
-    "imsrg_gpu_magnus_decouple_adjoint",
+    "imsrg_gpu_magnus_decouple_adjoint", "imsrg_gpu_split_chunk_set",
 )
 
 KERNELS = ("cc_forward", "gemm_fp64", "assemble_2body", "assemble_1body", "ozaki_slice", "ozaki_mma",
@@ -116,6 +116,7 @@ def lib():
             "imsrg_gpu_split_schedule": [vp, ip, ip, dp, i],
             "imsrg_gpu_split_schedule_set": [vp, i],
             "imsrg_gpu_split_digits_set": [vp, i],
+            "imsrg_gpu_split_chunk_set": [vp, i],
             "imsrg_gpu_build_gs_atan": [vp, vp],
             "imsrg_gpu_build_gs_w2": [vp, vp, i],
             "imsrg_gpu_magnus_decouple_gen": [vp, vp, i, d, d, i, i, dp, ip, ip],
@@ -243,6 +244,11 @@ class Basis:
         timing (e.g. under a profiler whose serialised launches distort the
         autotuner's event timings); results do not depend on the schedule."""
         _check(lib().imsrg_gpu_split_schedule_set(self._h, int(model)), "split_schedule_set")
+
+    def set_split_chunk(self, steps: int):
+        """Cap the split engine's exact accumulator chunk at `steps` K steps
+        (0: the default, the largest exact chunk); before the first split call."""
+        _check(lib().imsrg_gpu_split_chunk_set(self.handle, int(steps)), "split_chunk_set")
 
     def set_split_digits(self, digits: int):
         """Digits per operand of the split engine on this basis: 6 (default,

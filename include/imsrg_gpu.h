@@ -338,6 +338,16 @@ int imsrg_gpu_split_schedule_set(imsrg_basis_t *b, int model);
  * K max|A| max|B|) or 4 (10 products, about 2^-28 K max|A| max|B|).  Only before the basis' first split-precision call; later
  * it accepts the current count only (IMSRG_ERR_INVALID otherwise). */
 int imsrg_gpu_split_digits_set(imsrg_basis_t *b, int digits);
+/* Contraction chunking of IMSRG_PREC_OZAKI (no reference counterpart).  A
+ * tile's digit products accumulate exactly in FP32 for at most 51 K steps of
+ * 16 (steps x 16 x 5 x 2^12 < 2^24); longer contractions (a term count times
+ * K above 816, e.g. the pppp blocks from emax = 8 on) run in chunks, each
+ * into its own accumulators, whose exact int64 level sums the epilogue adds
+ * before converting once.  steps > 0 caps the chunk at fewer steps (testing
+ * and tuning; the result stays within the same error bound), 0 restores the
+ * default.  Only before the basis' first split-precision call, like
+ * imsrg_gpu_split_digits_set. */
+int imsrg_gpu_split_chunk_set(imsrg_basis_t *b, int steps);
 
 const char *imsrg_gpu_strerror(int status);
 /* Number of library kernel launches issued so far on this basis. */
