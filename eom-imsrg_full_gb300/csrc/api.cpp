@@ -158,6 +158,7 @@ int commutator_launches(imsrg_basis *b, const double *L, int hL, const double *R
       IMSRG_CUDA_TRY(cudaEventRecord(b->ev_join3, b->side3));
     }
   }
+  const bool e0_front = (phases & kPhaseJoinE0Front) != 0;
   auto join_e0 = [&]() -> int {
     if (with_e0 && !serial) IMSRG_CUDA_TRY(cudaStreamWaitEvent(b->stream, b->ev_join3, 0));
     return IMSRG_OK;
@@ -197,6 +198,7 @@ int commutator_launches(imsrg_basis *b, const double *L, int hL, const double *R
     if (front) IMSRG_TRY(launch_cc_forward(b, L, hL, R, hR));
     if (prods) IMSRG_TRY(launch_gemm_fp64(b, L, hL, R, hR));
   }
+  if (front && e0_front) IMSRG_TRY(join_e0());
   if (!back) return IMSRG_OK;
   // one-body assembly beside the two-body assembly, after the packed (L, R)
   // pairs of the 122 gathers, which are built beside the recoupling inputs
@@ -235,7 +237,7 @@ int commutator_launches(imsrg_basis *b, const double *L, int hL, const double *R
     IMSRG_TRY(launch_asm2_range(b, L, hL, R, hR, RES, hRES, 0, b->T.n_asm2, false));
   }
   IMSRG_TRY(join(1));
-  IMSRG_TRY(join_e0());
+  if (!e0_front) IMSRG_TRY(join_e0());
   if (io) IMSRG_CUDA_TRY(cudaMemcpyAsync(io->RES, RES, bytes, cudaMemcpyDeviceToHost, b->stream));
   return IMSRG_OK;
 }
@@ -637,11 +639,14 @@ struct imsrg_batch {
     cudaGraphExec_t exec;
   };
   std::vector<Graph> graphs;  // one per argument set, least recently built dropped first
+  void *flow = nullptr;       // the lockstep flow's step graph (graph.cu), built on first use
 };
 
 namespace {
 
 void batch_release(imsrg_batch *bt) {
+  imsrg::batch_flow_free(bt->flow);
+  bt->flow = nullptr;
   for (imsrg_batch::Graph &g : bt->graphs) cudaGraphExecDestroy(g.exec);
   bt->graphs.clear();
   for (cudaEvent_t e : bt->ev_front) cudaEventDestroy(e);
@@ -721,6 +726,22 @@ int imsrg_gpu_batch_create(int n, imsrg_basis_t *const *bases, imsrg_batch_t **o
   }
   *out = bt;
   return IMSRG_OK;
+}
+
+int imsrg_gpu_batch_magnus_decouple(imsrg_batch_t *batch, imsrg_op_t *const *HS, imsrg_op_t *const *G,
+                                    double s_max, double ds, int max_steps, int precision, double *const *traces,
+                                    int *steps, int *ncomm, int *status) {
+  if (!batch || !HS || !G || ds <= 0.0 || max_steps < 0) return IMSRG_ERR_INVALID;
+  if (precision != IMSRG_PREC_FP64 && precision != IMSRG_PREC_OZAKI) return IMSRG_ERR_INVALID;
+  const int n = (int)batch->bases.size();
+  for (int i = 0; i < n; i++) {
+    IMSRG_TRY(check_op(HS[i]));
+    IMSRG_TRY(check_op(G[i]));
+    if (HS[i]->b != batch->bases[i] || G[i]->b != batch->bases[i]) return IMSRG_ERR_MISMATCH;
+    if (HS[i]->herm != 1 || HS[i] == G[i]) return IMSRG_ERR_INVALID;
+  }
+  return imsrg::batch_flow_run(batch->bases.data(), n, batch->oz, batch->st, &batch->flow, HS, G, s_max, ds,
+                               max_steps, precision, traces, steps, ncomm, status);
 }
 
 int imsrg_gpu_batch_destroy(imsrg_batch_t *batch) {

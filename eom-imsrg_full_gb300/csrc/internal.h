@@ -401,7 +401,8 @@ void ozaki_free(imsrg_basis *b);
 // ozaki_batch_mma gathers their block exponents and launches on st,
 // ozaki_batch_error reads (and clears) the bounded-wait flag.
 int ozaki_batch_create(imsrg_basis *const *bases, int n, void **out);
-int ozaki_batch_mma(void *batch, cudaStream_t st, int hL, int hR);
+// act (optional, one int per basis): only the bases with act[i] != 0 take part
+int ozaki_batch_mma(void *batch, cudaStream_t st, int hL, int hR, const int *act = nullptr);
 int ozaki_batch_error(void *batch, cudaStream_t st);
 void ozaki_batch_free(void *batch);
 
@@ -425,6 +426,14 @@ int flow_graph_set_s(imsrg_basis *b, double s);  // a flow restarted at s
 int flow_graph_launch(imsrg_basis *b);
 int flow_graph_finish(imsrg_basis *b, double *s, double *e0, double *emp2, int *nc, int *status);
 void flow_graph_free(imsrg_basis *b);
+// Lockstep batched Magnus flows of the bases of one batch (graph.cu): each
+// step one graph for all instances, the split products of all running series
+// in one masked launch per term; the graph is cached in *cache (freed by
+// batch_flow_free).
+int batch_flow_run(imsrg_basis *const *bases, int n, void *oz, cudaStream_t st, void **cache,
+                   imsrg_op *const *HS, imsrg_op *const *G, double s_max, double ds, int max_steps, int precision,
+                   double *const *traces, int *steps, int *ncomm, int *status);
+void batch_flow_free(void *cache);
 
 // Records CUDA events around the launches of one kernel class while profiling
 // is enabled (profile.cpp).
@@ -447,6 +456,9 @@ int commutator_dev(imsrg_basis *b, const double *L, int hL, const double *R, int
 // parts of the launch sequence of one commutator (device operands for any
 // part short of kPhaseAll)
 constexpr int kPhaseFront = 1, kPhaseProducts = 2, kPhaseBack = 4, kPhaseAll = 7;
+// with the phases: the E0 side stream joins at the end of the front phase (not
+// in the back phase), so front and back can be captured into separate graphs
+constexpr int kPhaseJoinE0Front = 8;
 int commutator_launches(imsrg_basis *b, const double *L, int hL, const double *R, int hR, double *RES, int hRES,
                         int precision, int with_e0, const HostIO *io, int phases);
 

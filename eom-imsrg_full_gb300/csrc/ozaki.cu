@@ -127,7 +127,8 @@ struct OzProb {
   int ldc;
   int gA, gB;
   int tiles_m, tile0, tiles;
-  int raw;  // store the exact int64 level sum v (result = v 2^k) instead of FP64: the WCC products
+  int raw;   // store the exact int64 level sum v (result = v 2^k) instead of FP64: the WCC products
+  int inst;  // instance (basis) of a merged batch plan; its tiles run only while act[inst] (0 alone)
 };
 
 // Cost models of the CTA schedule tried by the autotuner (weights of K steps,
@@ -435,7 +436,8 @@ __global__ void __launch_bounds__(OZ_THREADS, 1) k_oz_mma(const OzProb *__restri
                                                           const int2 *__restrict__ sched,
                                                           const int *__restrict__ sched_off,
                                                           const int *__restrict__ exps, int hL, int hR, int *err,
-                                                          const CUtensorMap *__restrict__ maps) {
+                                                          const CUtensorMap *__restrict__ maps,
+                                                          const int *__restrict__ act) {
   extern __shared__ __align__(1024) uint8_t smem_raw[];
   uint8_t *smem = (uint8_t *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
   constexpr int STAGE_BYTES = oz_stage_bytes(S), LMAX = S + 1;
@@ -482,7 +484,7 @@ __global__ void __launch_bounds__(OZ_THREADS, 1) k_oz_mma(const OzProb *__restri
       for (int ti = t_begin; ti < t_end && !*abort_flag; ti++) {
         const int2 slot = sched[ti];
         const OzProb &P = probs[slot.x];
-        if (P.ksteps == 0) continue;
+        if (P.ksteps == 0 || (act && !act[P.inst])) continue;
         const int lt = slot.y;
         int tm = lt % P.tiles_m, tn = lt / P.tiles_m;
         for (int it = 0; it < P.nterms; it++) {
@@ -519,7 +521,7 @@ __global__ void __launch_bounds__(OZ_THREADS, 1) k_oz_mma(const OzProb *__restri
       uint32_t phase = 0;
       for (int ti = t_begin; ti < t_end && !*abort_flag; ti++) {
         const OzProb &P = probs[sched[ti].x];
-        if (P.ksteps == 0) continue;
+        if (P.ksteps == 0 || (act && !act[P.inst])) continue;
         const uint64_t desc0 = smem_desc(smem_u32(smem), 128, 256);
         const int kchunk = CH ? P.kchunk : 0x40000000;
         int left = 0;                          // steps left in the current chunk
@@ -598,6 +600,7 @@ __global__ void __launch_bounds__(OZ_THREADS, 1) k_oz_mma(const OzProb *__restri
     for (int ti = t_begin; ti < t_end; ti++) {
       const int2 slot = sched[ti];
       const OzProb &P = probs[slot.x];
+      if (act && !act[P.inst]) continue;  // an instance whose series has stopped: its outputs stay
       const int lt = slot.y;
       // problem fields in registers: the stores below could alias the problem
       // table as far as the compiler knows, which would force a reload per column
@@ -714,9 +717,11 @@ __global__ void __launch_bounds__(OZ_THREADS, 1) k_oz_mma(const OzProb *__restri
 OzPlan *plan_of(imsrg_basis *b) { return (OzPlan *)b->ozaki; }
 
 void launch_mma(int S, bool chunked, int grid, cudaStream_t st, const OzProb *probs, int nprobs, const int2 *sched,
-                const int *sched_off, const int *exps, int hL, int hR, int *err, const CUtensorMap *maps) {
-#define OZ_LAUNCH(SS, CC) \
-  k_oz_mma<SS, CC><<<grid, OZ_THREADS, oz_mma_smem(SS), st>>>(probs, nprobs, sched, sched_off, exps, hL, hR, err, maps)
+                const int *sched_off, const int *exps, int hL, int hR, int *err, const CUtensorMap *maps,
+                const int *act = nullptr) {
+#define OZ_LAUNCH(SS, CC)                                                                                    \
+  k_oz_mma<SS, CC><<<grid, OZ_THREADS, oz_mma_smem(SS), st>>>(probs, nprobs, sched, sched_off, exps, hL, hR, err, \
+                                                              maps, act)
   if (S == 4) {
     if (chunked) OZ_LAUNCH(4, true);
     else OZ_LAUNCH(4, false);
@@ -1260,6 +1265,7 @@ int ozaki_batch_create(imsrg_basis *const *bases, int n, void **out) {
     const int p0 = (int)probs.size(), m0 = (int)maps.size();
     for (const OzProb &p : pl->probs) {
       OzProb q = p;
+      q.inst = i;
       q.gA += bt->ngroups;
       q.gB += bt->ngroups;
       for (int t = 0; t < q.nterms; t++) {
@@ -1306,15 +1312,15 @@ int ozaki_batch_create(imsrg_basis *const *bases, int n, void **out) {
   return IMSRG_OK;
 }
 
-int ozaki_batch_mma(void *batch, cudaStream_t st, int hL, int hR) {
+int ozaki_batch_mma(void *batch, cudaStream_t st, int hL, int hR, const int *act) {
   OzBatch *bt = (OzBatch *)batch;
   if (!bt) return IMSRG_ERR_INVALID;
   for (size_t i = 0; i < bt->plans.size(); i++)
     if (bt->plans[i]->ngroups > 0)
       IMSRG_CUDA_TRY(cudaMemcpyAsync(bt->d_exps + bt->exps_base[i], bt->plans[i]->d_exps,
                                      bt->plans[i]->ngroups * sizeof(int), cudaMemcpyDeviceToDevice, st));
-  launch_mma(bt->plans[0]->S, bt->chunked, bt->grid, st, bt->d_probs, bt->nprobs, bt->d_sched, bt->d_sched_off, bt->d_exps, hL,
-             hR, bt->d_err, bt->d_maps);
+  launch_mma(bt->plans[0]->S, bt->chunked, bt->grid, st, bt->d_probs, bt->nprobs, bt->d_sched, bt->d_sched_off,
+             bt->d_exps, hL, hR, bt->d_err, bt->d_maps, act);
   return cuda_status(cudaGetLastError());
 }
 

@@ -42,7 +42,7 @@ SYMBOLS = (
     "imsrg_gpu_batch_create", "imsrg_gpu_batch_commutator", "imsrg_gpu_batch_destroy",
     "imsrg_gpu_magnus_rules", "imsrg_gpu_magnus_decouple_checkpoint",
     "imsrg_gpu_commutator_adjoint", "imsrg_gpu_white_adjoint", "imsrg_gpu_op_dot",
-    "imsrg_gpu_magnus_decouple_adjoint", "imsrg_gpu_split_chunk_set",
+    "imsrg_gpu_magnus_decouple_adjoint", "imsrg_gpu_split_chunk_set", "imsrg_gpu_batch_magnus_decouple",
 )
 
 KERNELS = ("cc_forward", "gemm_fp64", "assemble_2body", "assemble_1body", "ozaki_slice", "ozaki_mma",
@@ -134,6 +134,8 @@ def lib():
             "imsrg_gpu_batch_create": [i, C.POINTER(vp), C.POINTER(vp)],
             "imsrg_gpu_batch_commutator": [vp, C.POINTER(vp), C.POINTER(vp), C.POINTER(vp), i, i],
             "imsrg_gpu_batch_destroy": [vp],
+            "imsrg_gpu_batch_magnus_decouple": [vp, C.POINTER(vp), C.POINTER(vp), d, d, i, i, C.POINTER(dp), ip, ip,
+                                                ip],
             "imsrg_gpu_magnus_rules": [vp, d, dp, ip],
             "imsrg_gpu_commutator_adjoint": [vp, vp, i, i, vp],
             "imsrg_gpu_white_adjoint": [vp, vp, vp],
@@ -612,6 +614,29 @@ class Batch:
         assert len(L) == len(R) == len(RES) == n
         arrs = [(C.c_void_p * n)(*[o.handle.value for o in ops]) for ops in (L, R, RES)]
         _check(lib().imsrg_gpu_batch_commutator(self._h, *arrs, PREC[precision], int(with_e0)), "batch_commutator")
+
+    def magnus_decouple(self, HS: list, G: list, s_max: float = 50.0, ds: float = 0.5, max_steps: int = 1000,
+                        precision: str = "ozaki"):
+        """The instances' Magnus flows in lockstep, each step one CUDA graph
+        for all of them and one merged product launch per series term
+        (imsrg_gpu_batch_magnus_decouple): a list of dicts as
+        magnus_decouple_batch returns."""
+        n = len(self.bases)
+        assert len(HS) == len(G) == n
+        traces = [np.zeros(5 * (max_steps + 1)) for _ in range(n)]
+        tp = (C.POINTER(C.c_double) * n)(*[_dp(t) for t in traces])
+        hs = (C.c_void_p * n)(*[h.handle for h in HS])
+        gs = (C.c_void_p * n)(*[g.handle for g in G])
+        steps, nc, st = (C.c_int * n)(), (C.c_int * n)(), (C.c_int * n)()
+        rc = lib().imsrg_gpu_batch_magnus_decouple(self._h, hs, gs, float(s_max), float(ds), int(max_steps),
+                                                   PREC[precision], tp, steps, nc, st)
+        out = []
+        for i in range(n):
+            k = steps[i] + 1
+            out.append(dict(steps=steps[i], ncomm=nc[i], status=st[i], trace=traces[i][:5 * k].reshape(k, 5)))
+        if rc != 0 and all(o["status"] == 0 for o in out):
+            _check(rc, "batch_magnus_decouple")
+        return out
 
     def close(self):
         if self._h:

@@ -396,6 +396,23 @@ int imsrg_gpu_batch_create(int n, imsrg_basis_t *const *bases, imsrg_batch_t **o
 int imsrg_gpu_batch_commutator(imsrg_batch_t *batch, imsrg_op_t *const *L, imsrg_op_t *const *R,
                                imsrg_op_t *const *RES, int precision, int with_e0);
 int imsrg_gpu_batch_destroy(imsrg_batch_t *batch);
+/* magnus_decouple (IMSRG_MAGNUS.f90:15-128, White generator) of the batch's
+ * n instances in lockstep: HS[i] (herm +1; in = normal-ordered H, out =
+ * H(s)) and G[i] (out = Omega(s)) on the batch's basis i.  Each Magnus step is
+ * ONE CUDA graph launch for all instances: the Magnus and BCH series loop on
+ * the device while any instance's series runs; every series term computes
+ * the split-precision products of all instances whose series still runs in
+ * ONE persistent tensor-core launch (the others' tiles are skipped; FP64:
+ * each instance's own products); instances whose series or flow has stopped
+ * are skipped by conditional graph nodes.  Each instance's results, trace and
+ * counts equal its unbatched imsrg_gpu_magnus_decouple_graph flow bit for
+ * bit.  traces, steps, ncomm, status as in imsrg_gpu_magnus_decouple_batch.
+ * The step graph is built on the first call for an (HS, G, precision, ds)
+ * set and reused.  No reference counterpart (the reference runs one flow per
+ * Hamiltonian). */
+int imsrg_gpu_batch_magnus_decouple(imsrg_batch_t *batch, imsrg_op_t *const *HS, imsrg_op_t *const *G,
+                                    double s_max, double ds, int max_steps, int precision, double *const *traces,
+                                    int *steps, int *ncomm, int *status);
 
 /* --- setup: interaction file, one-body HO part, Hartree-Fock ---------------
  * imsrg_gpu_read_interaction replaces read_interaction (interaction_IO.f90:
