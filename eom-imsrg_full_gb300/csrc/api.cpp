@@ -116,17 +116,36 @@ int commutator_launches(imsrg_basis *b, const double *L, int hL, const double *R
   // digit images and its half of the Pandya transform run on side2 while L is
   // in flight, and RES comes back by output range beside the two-body assembly.
   const bool overlap = io && io->pinned && !serial;
+  // packed host arrays (vectorize order): copied into staging buffers and
+  // unpacked on the device; RES packed before one copy back
+  const bool packed = io && io->Lst;
+  const size_t pbytes = (size_t)b->neq * sizeof(double);
   // the transform also reduces the LCC/RCC block exponents (split precision)
   int *cc_exps = nullptr, gL = 0, gR = 0;
   if (overlap) {
     if (oz) IMSRG_TRY(ozaki_cc_exponents(b, b->stream, &cc_exps, &gL, &gR));
-    IMSRG_CUDA_TRY(cudaMemcpyAsync(const_cast<double *>(R), io->R, bytes, cudaMemcpyHostToDevice, b->stream));
-    IMSRG_CUDA_TRY(cudaEventRecord(b->ev_hostR, b->stream));
-    IMSRG_CUDA_TRY(cudaMemcpyAsync(const_cast<double *>(L), io->L, bytes, cudaMemcpyHostToDevice, b->stream));
-    IMSRG_CUDA_TRY(cudaStreamWaitEvent(b->side2, b->ev_hostR, 0));
+    if (packed) {
+      IMSRG_CUDA_TRY(cudaMemcpyAsync(io->Rst, io->R, pbytes, cudaMemcpyHostToDevice, b->stream));
+      IMSRG_CUDA_TRY(cudaEventRecord(b->ev_hostR, b->stream));
+      IMSRG_CUDA_TRY(cudaMemcpyAsync(io->Lst, io->L, pbytes, cudaMemcpyHostToDevice, b->stream));
+      IMSRG_CUDA_TRY(cudaStreamWaitEvent(b->side2, b->ev_hostR, 0));
+      IMSRG_TRY(launch_unpack(b, io->Rst, hR, const_cast<double *>(R), b->side2));
+      IMSRG_TRY(launch_unpack(b, io->Lst, hL, const_cast<double *>(L), b->stream));
+    } else {
+      IMSRG_CUDA_TRY(cudaMemcpyAsync(const_cast<double *>(R), io->R, bytes, cudaMemcpyHostToDevice, b->stream));
+      IMSRG_CUDA_TRY(cudaEventRecord(b->ev_hostR, b->stream));
+      IMSRG_CUDA_TRY(cudaMemcpyAsync(const_cast<double *>(L), io->L, bytes, cudaMemcpyHostToDevice, b->stream));
+      IMSRG_CUDA_TRY(cudaStreamWaitEvent(b->side2, b->ev_hostR, 0));
+    }
     if (oz) IMSRG_TRY(ozaki_slice(b, L, R, 1, b->side2));
     IMSRG_TRY(launch_cc_forward(b, L, hL, R, hR, cc_exps, gL, gR, 2, b->side2));
     IMSRG_CUDA_TRY(cudaEventRecord(b->ev_join2, b->side2));
+  } else if (io && packed) {  // pageable packed host operands, one after the other
+    IMSRG_CUDA_TRY(cudaMemcpyAsync(io->Lst, io->L, pbytes, cudaMemcpyHostToDevice, b->stream));
+    IMSRG_TRY(launch_unpack(b, io->Lst, hL, const_cast<double *>(L), b->stream));
+    IMSRG_CUDA_TRY(cudaEventRecord(b->ev_hostL, b->stream));
+    IMSRG_CUDA_TRY(cudaMemcpyAsync(io->Rst, io->R, pbytes, cudaMemcpyHostToDevice, b->stream));
+    IMSRG_TRY(launch_unpack(b, io->Rst, hR, const_cast<double *>(R), b->stream));
   } else if (io) {  // pageable host operands: L first, so the digit images of L start while R is in flight
     IMSRG_CUDA_TRY(cudaMemcpyAsync(const_cast<double *>(L), io->L, bytes, cudaMemcpyHostToDevice, b->stream));
     IMSRG_CUDA_TRY(cudaEventRecord(b->ev_hostL, b->stream));
@@ -207,7 +226,7 @@ int commutator_launches(imsrg_basis *b, const double *L, int hL, const double *R
   IMSRG_TRY(launch_lr_pack(b, L, R, side));
   if (!serial) IMSRG_CUDA_TRY(cudaEventRecord(b->ev_lr, side));
   IMSRG_TRY(launch_assemble_1body(b, L, hL, R, hR, RES, hRES, side));
-  if (overlap) {
+  if (overlap && !packed) {
     // two-body elements by output range; each range's copy to the host runs on
     // side2 beside the assembly of the next (see imsrg_basis::asm2_el)
     IMSRG_TRY(launch_ph_inputs(b, hL, hR, precision));
@@ -238,7 +257,12 @@ int commutator_launches(imsrg_basis *b, const double *L, int hL, const double *R
   }
   IMSRG_TRY(join(1));
   if (!e0_front) IMSRG_TRY(join_e0());
-  if (io) IMSRG_CUDA_TRY(cudaMemcpyAsync(io->RES, RES, bytes, cudaMemcpyDeviceToHost, b->stream));
+  if (io && packed) {
+    IMSRG_TRY(launch_pack(b, RES, io->RESst, b->stream));
+    IMSRG_CUDA_TRY(cudaMemcpyAsync(io->RES, io->RESst, pbytes, cudaMemcpyDeviceToHost, b->stream));
+  } else if (io) {
+    IMSRG_CUDA_TRY(cudaMemcpyAsync(io->RES, RES, bytes, cudaMemcpyDeviceToHost, b->stream));
+  }
   return IMSRG_OK;
 }
 
@@ -280,7 +304,7 @@ int commutator_dev(imsrg_basis *b, const double *L, int hL, const double *R, int
   for (imsrg_basis::CommGraph &g : b->comm_graphs)
     if (g.L == L && g.R == R && g.RES == RES && g.hL == hL && g.hR == hR && g.hRES == hRES &&
         g.precision == precision && g.with_e0 == with_e0 && g.io.L == key.L && g.io.R == key.R &&
-        g.io.RES == key.RES) {
+        g.io.RES == key.RES && g.io.Lst == key.Lst) {
       g.last_use = b->comm_calls;
       b->launches += g.nlaunch;
       return cuda_status(cudaGraphLaunch(g.exec, b->stream));
@@ -619,6 +643,36 @@ int imsrg_gpu_commutator_host(imsrg_basis_t *b, const double *L, int herm_L, con
   dR->herm = herm_R;
   dRES->herm = -herm_L * herm_R;
   const imsrg::HostIO io{L, R, RES};
+  IMSRG_TRY(imsrg::commutator_dev(b, dL->d, herm_L, dR->d, herm_R, dRES->d, dRES->herm, precision, with_e0 ? 1 : 0,
+                                  &io));
+  IMSRG_CUDA_TRY(cudaStreamSynchronize(b->stream));
+  return imsrg::ozaki_check_error(b);
+}
+
+int imsrg_gpu_commutator_host_packed(imsrg_basis_t *b, const double *L, int herm_L, const double *R, int herm_R,
+                                     double *RES, int precision, int with_e0) {
+  if (!b || !L || !R || !RES) return IMSRG_ERR_INVALID;
+  if ((herm_L != 1 && herm_L != -1) || (herm_R != 1 && herm_R != -1)) return IMSRG_ERR_INVALID;
+  const size_t bytes = (size_t)b->neq * sizeof(double);
+  auto overlap = [&](const void *x, const void *y) {
+    const char *p = (const char *)x, *q = (const char *)y;
+    return p < q + bytes && q < p + bytes;
+  };
+  if (overlap(RES, L) || overlap(RES, R)) return IMSRG_ERR_INVALID;
+  imsrg_op *dL, *dR, *dRES, *sL, *sR, *sRES;  // device operands (17-19) and packed staging (23-25)
+  IMSRG_TRY(tmp_op(b, 17, &dL));
+  IMSRG_TRY(tmp_op(b, 18, &dR));
+  IMSRG_TRY(tmp_op(b, 19, &dRES));
+  IMSRG_TRY(tmp_op(b, 23, &sL));
+  IMSRG_TRY(tmp_op(b, 24, &sR));
+  IMSRG_TRY(tmp_op(b, 25, &sRES));
+  dL->herm = herm_L;
+  dR->herm = herm_R;
+  dRES->herm = -herm_L * herm_R;
+  imsrg::HostIO io{L, R, RES};
+  io.Lst = sL->d;
+  io.Rst = sR->d;
+  io.RESst = sRES->d;
   IMSRG_TRY(imsrg::commutator_dev(b, dL->d, herm_L, dR->d, herm_R, dRES->d, dRES->herm, precision, with_e0 ? 1 : 0,
                                   &io));
   IMSRG_CUDA_TRY(cudaStreamSynchronize(b->stream));

@@ -182,6 +182,10 @@ struct HostIO {
   const double *L, *R;
   double *RES;
   bool pinned = false;
+  // packed (vectorize-order, neq doubles) host arrays when set: device staging
+  // buffers the copies land in, unpacked into L and R on the device; RES is
+  // packed into RESst before its one copy back
+  double *Lst = nullptr, *Rst = nullptr, *RESst = nullptr;
 };
 // The two-body part of RES is assembled, and copied back to a page-locked host
 // result, in this many address ranges, so that each range's copy runs beside
@@ -356,8 +360,8 @@ int launch_generator(imsrg_basis *b, const double *Hden, int hH, const double *H
 int launch_white_tangent(imsrg_basis *b, const double *H, const double *dH, int hH, double *dETA);
 // Hb += (d White / d H)^T ETAb (reverse mode; monob: norb x norb scratch)
 int launch_white_adjoint(imsrg_basis *b, const double *H, int hH, const double *ETAb, double *Hb, double *monob);
-int launch_pack(imsrg_basis *b, const double *flat, double *packed);
-int launch_unpack(imsrg_basis *b, const double *packed, int herm, double *flat);
+int launch_pack(imsrg_basis *b, const double *flat, double *packed, cudaStream_t st = nullptr);
+int launch_unpack(imsrg_basis *b, const double *packed, int herm, double *flat, cudaStream_t st = nullptr);
 int launch_check_finite(imsrg_basis *b, const double *op, int *d_flag);
 int launch_normal_order(imsrg_basis *b, const double *Tin, int herm, double *H);
 

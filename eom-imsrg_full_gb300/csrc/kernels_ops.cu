@@ -445,15 +445,17 @@ int launch_white_adjoint(imsrg_basis *b, const double *H, int hH, const double *
   return cuda_status(cudaGetLastError());
 }
 
-int launch_pack(imsrg_basis *b, const double *flat, double *packed) {
-  k_pack<<<(unsigned)((b->neq + 255) / 256), 256, 0, b->stream>>>(flat, b->d_pack_src, packed, b->neq);
+int launch_pack(imsrg_basis *b, const double *flat, double *packed, cudaStream_t st) {
+  if (!st) st = b->stream;
+  k_pack<<<(unsigned)((b->neq + 255) / 256), 256, 0, st>>>(flat, b->d_pack_src, packed, b->neq);
   b->launches++;
   return cuda_status(cudaGetLastError());
 }
 
-int launch_unpack(imsrg_basis *b, const double *packed, int herm, double *flat) {
-  k_unpack<<<(unsigned)((b->neq + 255) / 256), 256, 0, b->stream>>>(packed, b->d_pack_src, b->d_pack_mirror, herm,
-                                                                      flat, b->neq);
+int launch_unpack(imsrg_basis *b, const double *packed, int herm, double *flat, cudaStream_t st) {
+  if (!st) st = b->stream;
+  k_unpack<<<(unsigned)((b->neq + 255) / 256), 256, 0, st>>>(packed, b->d_pack_src, b->d_pack_mirror, herm, flat,
+                                                              b->neq);
   b->launches++;
   return cuda_status(cudaGetLastError());
 }

@@ -43,6 +43,7 @@ SYMBOLS = (
     "imsrg_gpu_magnus_rules", "imsrg_gpu_magnus_decouple_checkpoint",
     "imsrg_gpu_commutator_adjoint", "imsrg_gpu_white_adjoint", "imsrg_gpu_op_dot",
     "imsrg_gpu_magnus_decouple_adjoint", "imsrg_gpu_split_chunk_set", "imsrg_gpu_batch_magnus_decouple",
+    "imsrg_gpu_commutator_host_packed",
 )
 
 KERNELS = ("cc_forward", "gemm_fp64", "assemble_2body", "assemble_1body", "ozaki_slice", "ozaki_mma",
@@ -97,6 +98,7 @@ def lib():
             "imsrg_gpu_op_get_e0": [vp, dp],
             "imsrg_gpu_commutator": [vp, vp, vp, i, i],
             "imsrg_gpu_commutator_host": [vp, vp, i, vp, i, vp, i, i],
+            "imsrg_gpu_commutator_host_packed": [vp, vp, i, vp, i, vp, i, i],
             "imsrg_gpu_build_gs_white": [vp, vp],
             "imsrg_gpu_magnus_expand": [vp, vp, i, ip],
             "imsrg_gpu_bch_expand": [vp, vp, vp, i, ip],
@@ -411,6 +413,18 @@ def commutator_host(basis: Basis, L: np.ndarray, herm_L: int, R: np.ndarray, her
             raise ValueError(f"commutator_host: operands must be C-contiguous float64 arrays of {n} elements")
     _check(lib().imsrg_gpu_commutator_host(basis.handle, _addr(L), int(herm_L), _addr(R), int(herm_R), _addr(RES),
                                            PREC[precision], int(with_e0)), "commutator_host")
+
+
+def commutator_host_packed(basis: Basis, L: np.ndarray, herm_L: int, R: np.ndarray, herm_R: int, RES: np.ndarray,
+                           precision: str = "fp64", with_e0: bool = True):
+    """[L, R] on host operands in the packed (vectorize) layout, neq doubles
+    each: copies in, device unpacking, commutator, device packing, copy out."""
+    n = basis.neq
+    for a in (L, R, RES):
+        if a.dtype != _F64 or not a.flags.c_contiguous or a.size != n:
+            raise ValueError(f"commutator_host_packed: operands must be C-contiguous float64 arrays of {n} elements")
+    _check(lib().imsrg_gpu_commutator_host_packed(basis.handle, _addr(L), int(herm_L), _addr(R), int(herm_R),
+                                                  _addr(RES), PREC[precision], int(with_e0)), "commutator_host_packed")
 
 
 def commutator_noalloc(basis: Basis, d_L: int, herm_L: int, d_R: int, herm_R: int, d_RES: int,

@@ -165,6 +165,17 @@ int imsrg_gpu_commutator(const imsrg_op_t *L, const imsrg_op_t *R, imsrg_op_t *R
  * replays as one CUDA graph.  RES must not overlap L or R. */
 int imsrg_gpu_commutator_host(imsrg_basis_t *b, const double *L, int herm_L, const double *R, int herm_R,
                               double *RES, int precision, int with_e0);
+/* The same on host operands in the packed (vectorize) layout of
+ * basic_IMSRG.f90:3794-3918 (neq doubles each: only the independent
+ * elements, ~57 % of the flat layout at emax = 6), the form the reference's
+ * ODE solver and checkpoints hold operators in: L and R are copied in and
+ * unpacked on the device (R first, its unpacking and its half of the work
+ * beside L's copy), RES is packed on the device and copied back.  Square
+ * arrays' lower triangles come from herm x the upper ones (repackage).  RES
+ * must not overlap L or R.  From page-locked buffers the sequence replays as
+ * one CUDA graph. */
+int imsrg_gpu_commutator_host_packed(imsrg_basis_t *b, const double *L, int herm_L, const double *R, int herm_R,
+                                     double *RES, int precision, int with_e0);
 
 /* build_gs_white (generators.f90:4-106): ETA (herm -1) from H.  ETA E0 is
  * left unchanged, as in the reference. */

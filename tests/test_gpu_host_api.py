@@ -71,3 +71,39 @@ def test_host_commutator_rejects_aliased_result(gpu_lib):
     for bad in (a[:-1], a.astype(np.float32), np.zeros(2 * lay.nfull)[::2]):
         with pytest.raises(ValueError):
             gpu_lib.commutator_host(B, bad, -1, a, 1, np.zeros(lay.nfull))
+
+
+@pytest.mark.parametrize("precision", ["fp64", "ozaki"])
+@pytest.mark.parametrize("pinned", [True, False])
+@pytest.mark.parametrize("emax", [4, 6])
+def test_packed_host_commutator_equals_device_commutator(gpu_lib, precision, pinned, emax):
+    """imsrg_gpu_commutator_host_packed (operands in the vectorize layout of
+    basic_IMSRG.f90:3794-3918): its result is the packed form of the
+    device-operand commutator bit for bit, call after call, interleaved with
+    the flat host call on the same basis."""
+    from imsrg_gpu.synth import synth_hamiltonian, synth_omega
+    bas, lay = make_case(emax)
+    B = gpu_lib.Basis.from_dict(bas)
+    B.set_split_digits(5)
+    keep = []
+    for seed in (5, 6):
+        Hh, Oh = synth_hamiltonian(lay, seed), synth_omega(lay, seed)
+        O, H, R = gpu_lib.Operator(B, -1, Oh), gpu_lib.Operator(B, 1, Hh), gpu_lib.Operator(B, 1)
+        gpu_lib.commutator(O, H, R, precision=precision)
+        ref = R.download_packed()
+        Op, Hp = O.download_packed(), H.download_packed()
+        if pinned:
+            (ho, to), (hh, th), (hr, tr) = _pinned(Op), _pinned(Hp), _pinned(np.zeros(B.neq))
+            (fo, t1), (fh, t2), (fr, t3) = _pinned(Oh), _pinned(Hh), _pinned(np.zeros(lay.nfull))
+            keep += [to, th, tr, t1, t2, t3]
+        else:
+            ho, hh, hr = Op.copy(), Hp.copy(), np.zeros(B.neq)
+            fo, fh, fr = Oh.copy(), Hh.copy(), np.zeros(lay.nfull)
+        for _ in range(3):  # first call builds, later calls replay
+            hr[:] = np.nan
+            gpu_lib.commutator_host_packed(B, ho, -1, hh, 1, hr, precision=precision)
+            assert np.array_equal(hr, ref)
+            gpu_lib.commutator_host(B, fo, -1, fh, 1, fr, precision=precision)
+            assert np.array_equal(fr, R.download())
+    with pytest.raises(ValueError):
+        gpu_lib.commutator_host_packed(B, np.zeros(lay.nfull), -1, hh, 1, hr)
