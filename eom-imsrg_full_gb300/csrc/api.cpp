@@ -694,6 +694,13 @@ struct imsrg_batch {
   };
   std::vector<Graph> graphs;  // one per argument set, least recently built dropped first
   void *flow = nullptr;       // the lockstep flow's step graph (graph.cu), built on first use
+  // merged FP64 product lists, one per operand set (graphs replay them)
+  struct Fp64List {
+    std::vector<const void *> key;
+    imsrg::GemmProb *d_probs;
+    int nprobs, ntiles;
+  };
+  std::vector<Fp64List> fp64;
 };
 
 namespace {
@@ -701,6 +708,8 @@ namespace {
 void batch_release(imsrg_batch *bt) {
   imsrg::batch_flow_free(bt->flow);
   bt->flow = nullptr;
+  for (imsrg_batch::Fp64List &l : bt->fp64) cudaFree(l.d_probs);
+  bt->fp64.clear();
   for (imsrg_batch::Graph &g : bt->graphs) cudaGraphExecDestroy(g.exec);
   bt->graphs.clear();
   for (cudaEvent_t e : bt->ev_front) cudaEventDestroy(e);
@@ -712,26 +721,56 @@ void batch_release(imsrg_batch *bt) {
   delete bt;
 }
 
+// The merged FP64 product list of the operand set (built on first use).
+int batch_fp64_list(imsrg_batch *bt, imsrg_op_t *const *L, imsrg_op_t *const *R, imsrg_batch::Fp64List **out) {
+  const int n = (int)bt->bases.size();
+  std::vector<const void *> key;
+  std::vector<const double *> dl(n), dr(n);
+  for (int i = 0; i < n; i++) {
+    key.push_back(L[i]->d);
+    key.push_back(R[i]->d);
+    dl[i] = L[i]->d;
+    dr[i] = R[i]->d;
+  }
+  for (imsrg_batch::Fp64List &l : bt->fp64)
+    if (l.key == key) {
+      *out = &l;
+      return IMSRG_OK;
+    }
+  imsrg_batch::Fp64List l{key, nullptr, 0, 0};
+  IMSRG_TRY(imsrg::gemm_fp64_merged(bt->bases.data(), n, dl.data(), dr.data(), &l.d_probs, &l.nprobs, &l.ntiles));
+  bt->fp64.push_back(l);
+  *out = &bt->fp64.back();
+  return IMSRG_OK;
+}
+
 // One step of the batch on the batch stream: every basis's part before the
-// products on its own streams, the products of all bases in one launch (split
-// precision; FP64 runs each basis's own sequence), every basis's part after
-// them, joined back into the batch stream.
+// products on its own streams, the products of all bases in one launch (the
+// split engine's merged plan, or the merged FP64 list), every basis's part
+// after them, joined back into the batch stream.
 int batch_sequence(imsrg_batch *bt, imsrg_op_t *const *L, imsrg_op_t *const *R, imsrg_op_t *const *RES,
                    int precision, int with_e0) {
   const int n = (int)bt->bases.size();
   const bool oz = precision == IMSRG_PREC_OZAKI;
+  imsrg_batch::Fp64List *fl = nullptr;
+  // (built, with an allocation, outside any capture: imsrg_gpu_batch_commutator
+  // asks for it before it captures a new operand set)
+  if (!oz) IMSRG_TRY(batch_fp64_list(bt, L, R, &fl));
   IMSRG_CUDA_TRY(cudaEventRecord(bt->ev_start, bt->st));
   for (int i = 0; i < n; i++) {
     imsrg_basis *b = bt->bases[i];
     IMSRG_CUDA_TRY(cudaStreamWaitEvent(b->stream, bt->ev_start, 0));
     IMSRG_TRY(imsrg::commutator_launches(b, L[i]->d, L[i]->herm, R[i]->d, R[i]->herm, RES[i]->d, RES[i]->herm,
-                                         precision, with_e0, nullptr,
-                                         oz ? imsrg::kPhaseFront : imsrg::kPhaseAll));
+                                         precision, with_e0, nullptr, imsrg::kPhaseFront));
     IMSRG_CUDA_TRY(cudaEventRecord(bt->ev_front[i], b->stream));
     IMSRG_CUDA_TRY(cudaStreamWaitEvent(bt->st, bt->ev_front[i], 0));
   }
-  if (!oz) return IMSRG_OK;
-  IMSRG_TRY(imsrg::ozaki_batch_mma(bt->oz, bt->st, L[0]->herm, R[0]->herm));
+  if (oz) {
+    IMSRG_TRY(imsrg::ozaki_batch_mma(bt->oz, bt->st, L[0]->herm, R[0]->herm));
+  } else {
+    IMSRG_TRY(imsrg::launch_gemm_fp64_merged(fl->d_probs, fl->nprobs, fl->ntiles, L[0]->herm, R[0]->herm, nullptr,
+                                             bt->st));
+  }
   for (imsrg_basis *b : bt->bases) b->launches++;
   IMSRG_CUDA_TRY(cudaEventRecord(bt->ev_mma, bt->st));
   for (int i = 0; i < n; i++) {
@@ -836,6 +875,10 @@ int imsrg_gpu_batch_commutator(imsrg_batch_t *batch, imsrg_op_t *const *L, imsrg
     for (const imsrg_batch::Graph &g : batch->graphs)
       if (g.key == key) exec = g.exec;
     if (!exec) {
+      if (precision == IMSRG_PREC_FP64) {  // allocate the merged FP64 list before capturing
+        imsrg_batch::Fp64List *fl = nullptr;
+        IMSRG_TRY(batch_fp64_list(batch, L, R, &fl));
+      }
       IMSRG_CUDA_TRY(cudaStreamBeginCapture(batch->st, cudaStreamCaptureModeThreadLocal));
       const int s = batch_sequence(batch, L, R, RES, precision, with_e0 ? 1 : 0);
       cudaGraph_t graph = nullptr;

@@ -348,8 +348,9 @@ int flow_graph_finish(imsrg_basis *b, double *s, double *e0, double *emp2, int *
 // and BCH series are WHILE loops that run while any instance's series
 // continues; in each iteration every instance's commutator is split into its
 // part before the products (an IF node: the instance's series still runs),
-// ONE persistent tensor-core launch over the tiles of all instances whose
-// series runs (the others' tiles are skipped), and its part after the products
+// ONE launch of the products of all instances whose series runs (the split
+// engine's persistent tensor-core kernel over the merged tile list, or the
+// merged FP64 list; the others' tiles are skipped), and its part after the products
 // (an IF node).  The set-up of the Magnus series, the Euler step with the BCH
 // set-up, and the generator with the stop criterion are IF nodes too (the
 // instance still flows).  Every instance runs the kernels of its unbatched
@@ -433,6 +434,8 @@ struct BatchFlowGraph {
   FlowDev *d_state = nullptr, *h_state = nullptr;
   int *d_go = nullptr, *d_flow = nullptr, *d_act = nullptr, *h_flow = nullptr;
   cudaGraphConditionalHandle *d_h = nullptr;  // IF handles: 3n of the step, 2n per series body
+  GemmProb *d_fp64 = nullptr;                 // FP64: the merged product list of [G_i, X0_i]
+  int fp64_nprobs = 0, fp64_ntiles = 0;
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t exec = nullptr;
 };
@@ -447,6 +450,7 @@ void batch_flow_free(void *p) {
   cudaFree(f->d_flow);
   cudaFree(f->d_act);
   cudaFree(f->d_h);
+  cudaFree(f->d_fp64);
   if (f->h_state) cudaFreeHost(f->h_state);
   if (f->h_flow) cudaFreeHost(f->h_flow);
   delete f;
@@ -462,6 +466,14 @@ int build_batch_graph(BatchFlowGraph *f, imsrg_basis *const *bases, void *oz, cu
   const bool ozp = precision == IMSRG_PREC_OZAKI;
   std::vector<imsrg_op *> H0(n), DG(n), X0(n), X1(n);
   for (int i = 0; i < n; i++) IMSRG_TRY(flow_tmp_ops(bases[i], &H0[i], &DG[i], &X0[i], &X1[i]));
+  if (!ozp) {  // every series term is [G_i, X0_i]: one merged FP64 product list
+    std::vector<const double *> Lp(n), Rp(n);
+    for (int i = 0; i < n; i++) {
+      Lp[i] = G[i]->d;
+      Rp[i] = X0[i]->d;
+    }
+    IMSRG_TRY(gemm_fp64_merged(bases, n, Lp.data(), Rp.data(), &f->d_fp64, &f->fp64_nprobs, &f->fp64_ntiles));
+  }
   cudaGraph_t g = nullptr;
   IMSRG_CUDA_TRY(cudaGraphCreate(&g, 0));
   f->graph = g;
@@ -515,7 +527,7 @@ int build_batch_graph(BatchFlowGraph *f, imsrg_basis *const *bases, void *oz, cu
       return cuda_status(cudaGetLastError());
     }, &bfr));
     const int hX = magnus ? -1 : 1, hRES = magnus ? -1 : 1, with_e0 = magnus ? 0 : 1;
-    const int fphase = kPhaseFront | kPhaseJoinE0Front | (ozp ? 0 : kPhaseProducts);
+    const int fphase = kPhaseFront | kPhaseJoinE0Front;
     for (int i = 0; i < n; i++) {
       imsrg_basis *b = bases[i];
       cudaGraphNode_t node;
@@ -527,10 +539,11 @@ int build_batch_graph(BatchFlowGraph *f, imsrg_basis *const *bases, void *oz, cu
       }, nullptr));
       fronts.push_back(node);
     }
-    std::vector<cudaGraphNode_t> mfr = fronts;
-    if (ozp)
-      IMSRG_TRY(capture_st(st, body, fronts, [&]() -> int { return ozaki_batch_mma(oz, st, -1, hX, f->d_act); },
-                           &mfr));
+    std::vector<cudaGraphNode_t> mfr;
+    IMSRG_TRY(capture_st(st, body, fronts, [&]() -> int {
+      if (ozp) return ozaki_batch_mma(oz, st, -1, hX, f->d_act);
+      return launch_gemm_fp64_merged(f->d_fp64, f->fp64_nprobs, f->fp64_ntiles, -1, hX, f->d_act, st);
+    }, &mfr));
     for (int i = 0; i < n; i++) {
       imsrg_basis *b = bases[i];
       FlowDev *F = f->d_state + i;

@@ -143,6 +143,7 @@ struct GemmTerm {
   int lda, ldb;
   double coef;
   int use_hl, use_hr;  // multiply coef by herm(L) / herm(R)
+  const double *a_abs, *b_abs;  // merged lists of several bases: the operands themselves
 };
 
 struct GemmProb {
@@ -155,6 +156,8 @@ struct GemmProb {
   int tiles_m;  // tiles along M
   int tiles;    // tiles of this problem
   int shape;    // FP64 tile: 0 = 64 x 64, 1 = 256 x 8 (problems with N <= 8)
+  double *c_abs;  // merged lists of several bases: the output itself
+  int inst;       // merged lists: the basis the problem belongs to
 };
 
 struct Operands {
@@ -339,6 +342,14 @@ inline int asm2_ctas(const imsrg_basis *b) { return (b->T.n_asm2 + ASM2_THREADS 
 int launch_cc_forward(imsrg_basis *b, const double *L, int hL, const double *R, int hR, int *exps = nullptr,
                       int gL = 0, int gR = 0, int sides = 3, cudaStream_t st = nullptr);
 int launch_gemm_fp64(imsrg_basis *b, const double *L, int hL, const double *R, int hR);
+// The FP64 products of several bases (operators L[i], R[i] of bases[i]) as one
+// problem list with absolute pointers, uploaded to *d_probs (cudaFree it).
+int gemm_fp64_merged(imsrg_basis *const *bases, int n, const double *const *L, const double *const *R,
+                     GemmProb **d_probs, int *nprobs, int *ntiles);
+// one launch of a merged list; act (optional, one int per basis): only the
+// bases with act[i] != 0 take part
+int launch_gemm_fp64_merged(const GemmProb *d_probs, int nprobs, int ntiles, int hL, int hR, const int *act,
+                            cudaStream_t st);
 // the two-body assembly: the recoupling inputs of 222_ph, then the elements
 // [w0, w1) of the signature work order or of the order by output range
 // (which read b->lr, see launch_lr_pack)

@@ -88,6 +88,7 @@ __global__ void __launch_bounds__(256) k_cc_forward(DevTables T, const double *_
 constexpr int BM = 64, BN = 64, BK = 16;
 constexpr int TBM = 256, TBN = 8, TBK = 8;
 
+template <bool ABS>
 __device__ __forceinline__ void gemm_thin_tile(const GemmProb &P, int lt, const Operands &ops, int hL, int hR) {
   __shared__ double As[TBK][TBM];
   __shared__ double Bs[TBK][TBN];
@@ -99,8 +100,8 @@ __device__ __forceinline__ void gemm_thin_tile(const GemmProb &P, int lt, const 
   for (int j = 0; j < TBN; j++) acc[j] = 0.0;
   for (int it = 0; it < P.nterms; it++) {
     const GemmTerm &Tm = P.t[it];
-    const double *A = ops.src[Tm.a_src] + Tm.a_off;
-    const double *B = ops.src[Tm.b_src] + Tm.b_off;
+    const double *A = ABS ? Tm.a_abs : ops.src[Tm.a_src] + Tm.a_off;
+    const double *B = ABS ? Tm.b_abs : ops.src[Tm.b_src] + Tm.b_off;
     const double alpha = Tm.coef * (Tm.use_hl ? hL : 1) * (Tm.use_hr ? hR : 1);
     double part[TBN];
 #pragma unroll
@@ -145,14 +146,17 @@ __device__ __forceinline__ void gemm_thin_tile(const GemmProb &P, int lt, const 
   }
   const int gm = m0 + tid;
   if (gm >= P.M) return;
-  double *Cp = ops.dst[P.c_dst] + P.c_off;
+  double *Cp = ABS ? P.c_abs : ops.dst[P.c_dst] + P.c_off;
 #pragma unroll
   for (int j = 0; j < TBN; j++)
     if (j < P.N) Cp[gm + (long)j * P.ldc] = acc[j];
 }
 
+// ABS: a merged list of several bases (absolute pointers, tiles of bases
+// with act[inst] == 0 skipped)
+template <bool ABS>
 __global__ void __launch_bounds__(256) k_gemm_fp64(const GemmProb *__restrict__ probs, int nprobs, Operands ops,
-                                                   int hL, int hR) {
+                                                   int hL, int hR, const int *__restrict__ act) {
   __shared__ double As[BK][BM + 1];
   __shared__ double Bs[BK][BN + 1];
   int tile = blockIdx.x;
@@ -164,9 +168,10 @@ __global__ void __launch_bounds__(256) k_gemm_fp64(const GemmProb *__restrict__ 
     else hi = mid;
   }
   const GemmProb &P = probs[lo - 1];
+  if (ABS && act && !act[P.inst]) return;  // block-uniform
   int lt = tile - P.tile0;
   if (P.shape == 1) {  // block-uniform
-    gemm_thin_tile(P, lt, ops, hL, hR);
+    gemm_thin_tile<ABS>(P, lt, ops, hL, hR);
     return;
   }
   int m0 = (lt % P.tiles_m) * BM, n0 = (lt / P.tiles_m) * BN;
@@ -179,8 +184,8 @@ __global__ void __launch_bounds__(256) k_gemm_fp64(const GemmProb *__restrict__ 
     for (int j = 0; j < 4; j++) acc[i][j] = 0.0;
   for (int it = 0; it < P.nterms; it++) {
     const GemmTerm &Tm = P.t[it];
-    const double *A = ops.src[Tm.a_src] + Tm.a_off;
-    const double *B = ops.src[Tm.b_src] + Tm.b_off;
+    const double *A = ABS ? Tm.a_abs : ops.src[Tm.a_src] + Tm.a_off;
+    const double *B = ABS ? Tm.b_abs : ops.src[Tm.b_src] + Tm.b_off;
     double alpha = Tm.coef * (Tm.use_hl ? hL : 1) * (Tm.use_hr ? hR : 1);
     double part[4][4];
 #pragma unroll
@@ -233,7 +238,7 @@ __global__ void __launch_bounds__(256) k_gemm_fp64(const GemmProb *__restrict__ 
 #pragma unroll
       for (int j = 0; j < 4; j++) acc[i][j] += alpha * part[i][j];
   }
-  double *Cp = ops.dst[P.c_dst] + P.c_off;
+  double *Cp = ABS ? P.c_abs : ops.dst[P.c_dst] + P.c_off;
 #pragma unroll
   for (int j = 0; j < 4; j++) {
     int gn = n0 + 4 * ty + j;
@@ -691,8 +696,45 @@ int launch_gemm_fp64(imsrg_basis *b, const double *L, int hL, const double *R, i
   ops.dst[SRC_W2] = b->w2;
   ops.dst[SRC_WCC] = b->wcc;
   ProfScope ps(b, IMSRG_KERNEL_GEMM_FP64);
-  k_gemm_fp64<<<b->ntiles, 256, 0, b->stream>>>(b->d_probs, b->nprobs, ops, hL, hR);
+  k_gemm_fp64<false><<<b->ntiles, 256, 0, b->stream>>>(b->d_probs, b->nprobs, ops, hL, hR, nullptr);
   b->launches++;
+  return cuda_status(cudaGetLastError());
+}
+
+int gemm_fp64_merged(imsrg_basis *const *bases, int n, const double *const *L, const double *const *R,
+                     GemmProb **d_probs, int *nprobs, int *ntiles) {
+  std::vector<GemmProb> all;
+  int tiles = 0;
+  for (int i = 0; i < n; i++) {
+    imsrg_basis *b = bases[i];
+    const double *src[7] = {L[i], R[i], b->w1, b->w2, b->lcc, b->rcc, b->wcc};
+    double *dst[7] = {nullptr, nullptr, b->w1, b->w2, nullptr, nullptr, b->wcc};
+    for (GemmProb p : b->probs) {
+      for (int t = 0; t < p.nterms; t++) {
+        p.t[t].a_abs = src[p.t[t].a_src] + p.t[t].a_off;
+        p.t[t].b_abs = src[p.t[t].b_src] + p.t[t].b_off;
+      }
+      p.c_abs = dst[p.c_dst] + p.c_off;
+      p.inst = i;
+      p.tile0 = tiles;
+      tiles += p.tiles;
+      all.push_back(p);
+    }
+  }
+  *d_probs = nullptr;
+  *nprobs = (int)all.size();
+  *ntiles = tiles;
+  if (all.empty()) return IMSRG_OK;
+  IMSRG_CUDA_TRY(cudaMalloc((void **)d_probs, all.size() * sizeof(GemmProb)));
+  IMSRG_CUDA_TRY(cudaMemcpy(*d_probs, all.data(), all.size() * sizeof(GemmProb), cudaMemcpyHostToDevice));
+  return IMSRG_OK;
+}
+
+int launch_gemm_fp64_merged(const GemmProb *d_probs, int nprobs, int ntiles, int hL, int hR, const int *act,
+                            cudaStream_t st) {
+  if (ntiles == 0) return IMSRG_OK;
+  Operands ops{};
+  k_gemm_fp64<true><<<ntiles, 256, 0, st>>>(d_probs, nprobs, ops, hL, hR, act);
   return cuda_status(cudaGetLastError());
 }
 
@@ -772,7 +814,7 @@ int launch_commutator_fp64_ws(imsrg_basis *b, const Workspace &ws, const double 
     ops.dst[SRC_W1] = ws.w1;
     ops.dst[SRC_W2] = ws.w2;
     ops.dst[SRC_WCC] = ws.wcc;
-    k_gemm_fp64<<<b->ntiles, 256, 0, st>>>(b->d_probs, b->nprobs, ops, hL, hR);
+    k_gemm_fp64<false><<<b->ntiles, 256, 0, st>>>(b->d_probs, b->nprobs, ops, hL, hR, nullptr);
     b->launches++;
   }
   if (b->T.n_ph > 0) {
@@ -802,7 +844,7 @@ int launch_commutator_fp64_ws(imsrg_basis *b, const Workspace &ws, const double 
 
 int preload_commutator_fp64_ws() {
   cudaFuncAttributes a;
-  const void *fns[] = {(const void *)k_cc_forward<3>, (const void *)k_gemm_fp64, (const void *)k_ph_inputs,
+  const void *fns[] = {(const void *)k_cc_forward<3>, (const void *)k_gemm_fp64<false>, (const void *)k_ph_inputs,
                        (const void *)k_assemble_2body<false>, (const void *)k_assemble_1body, (const void *)k_energy};
   for (const void *f : fns) {
     cudaError_t e = cudaFuncGetAttributes(&a, f);

@@ -398,8 +398,9 @@ int imsrg_gpu_profile_reset(imsrg_basis_t *b);
  * workspace; they must outlive the batch) and prepares the merged plan.
  * imsrg_gpu_batch_commutator computes RES_i = [L_i, R_i] for every i (each
  * operator of basis i; one herm_L and one herm_R for the whole batch;
- * RES_i herm = -herm_L herm_R) in either precision (FP64: each basis's own
- * sequence, side by side), results identical to imsrg_gpu_commutator, and
+ * RES_i herm = -herm_L herm_R) in either precision (FP64: the products of
+ * all bases as one grouped FP64 launch), results identical to
+ * imsrg_gpu_commutator, and
  * returns when all are done.  Each step is one cached CUDA graph per argument
  * set. */
 typedef struct imsrg_batch imsrg_batch_t;
@@ -413,8 +414,8 @@ int imsrg_gpu_batch_destroy(imsrg_batch_t *batch);
  * ONE CUDA graph launch for all instances: the Magnus and BCH series loop on
  * the device while any instance's series runs; every series term computes
  * the split-precision products of all instances whose series still runs in
- * ONE persistent tensor-core launch (the others' tiles are skipped; FP64:
- * each instance's own products); instances whose series or flow has stopped
+ * ONE persistent tensor-core launch (FP64: one grouped FP64 launch; the
+ * others' tiles are skipped); instances whose series or flow has stopped
  * are skipped by conditional graph nodes.  Each instance's results, trace and
  * counts equal its unbatched imsrg_gpu_magnus_decouple_graph flow bit for
  * bit.  traces, steps, ncomm, status as in imsrg_gpu_magnus_decouple_batch.
