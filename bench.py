@@ -626,7 +626,8 @@ def batched_commutators(api, n=64, reps=20):
     """n independent Hamiltonians (hbar*omega ~ U[12,28] MeV, two-body scale
     ~ U[0.5,2] MeV, emax cycling 2, 4, 6): [Omega_i, H_i] for all of them per
     step, (a) as one batch (the split-precision products of every instance in
-    one persistent launch, one graph per step) and (b) as n single commutators
+    one persistent launch, or in FP64 one grouped FP64 launch; one graph per
+    step) and (b) as n single commutators
     issued back to back on the instances' own streams (each its own graph),
     then a synchronisation.  Same results (bit for bit); wall time per step."""
     import numpy as np
@@ -651,26 +652,35 @@ def batched_commutators(api, n=64, reps=20):
     batch = api.Batch(bases)
     out = {"instances": n, "emax_counts": {e: emaxes.count(e) for e in (2, 4, 6)}, "setup_s": setup_s,
            "precision": "ozaki", "reps": reps}
-    for _ in range(3):  # graphs, autotuning of each instance's own schedule
-        batch.commutator(L, R, RES)
-        for i in range(n):
-            api.commutator(L[i], R[i], RES[i], precision="ozaki")
-        for B in bases:
-            B.synchronize()
-    t0 = time.perf_counter()
-    for _ in range(reps):
-        batch.commutator(L, R, RES)
-    tb = (time.perf_counter() - t0) / reps
-    t0 = time.perf_counter()
-    for _ in range(reps):
-        for i in range(n):
-            api.commutator(L[i], R[i], RES[i], precision="ozaki")
-        for B in bases:
-            B.synchronize()
-    ts = (time.perf_counter() - t0) / reps
-    batch.close()
+
+    def timed(prec):
+        for _ in range(3):  # graphs, autotuning of each instance's own schedule
+            batch.commutator(L, R, RES, precision=prec)
+            for i in range(n):
+                api.commutator(L[i], R[i], RES[i], precision=prec)
+            for B in bases:
+                B.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(reps):
+            batch.commutator(L, R, RES, precision=prec)
+        tb = (time.perf_counter() - t0) / reps
+        t0 = time.perf_counter()
+        for _ in range(reps):
+            for i in range(n):
+                api.commutator(L[i], R[i], RES[i], precision=prec)
+            for B in bases:
+                B.synchronize()
+        ts = (time.perf_counter() - t0) / reps
+        return tb, ts
+
+    tb, ts = timed("ozaki")
     out.update({"batch_ms_per_step": tb * 1e3, "batch_commutators_per_s": n / tb,
                 "single_calls_ms_per_step": ts * 1e3, "single_calls_commutators_per_s": n / ts})
+    # FP64: the products of every instance in one grouped FP64 launch
+    tb, ts = timed("fp64")
+    out["fp64"] = {"batch_ms_per_step": tb * 1e3, "batch_commutators_per_s": n / tb,
+                   "single_calls_ms_per_step": ts * 1e3, "single_calls_commutators_per_s": n / ts}
+    batch.close()
     return out
 
 
