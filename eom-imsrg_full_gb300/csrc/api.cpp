@@ -130,6 +130,7 @@ int commutator_launches(imsrg_basis *b, const double *L, int hL, const double *R
       IMSRG_CUDA_TRY(cudaMemcpyAsync(io->Lst, io->L, pbytes, cudaMemcpyHostToDevice, b->stream));
       IMSRG_CUDA_TRY(cudaStreamWaitEvent(b->side2, b->ev_hostR, 0));
       IMSRG_TRY(launch_unpack(b, io->Rst, hR, const_cast<double *>(R), b->side2));
+      IMSRG_CUDA_TRY(cudaEventRecord(b->ev_rdev, b->side2));  // R is on the device
       IMSRG_TRY(launch_unpack(b, io->Lst, hL, const_cast<double *>(L), b->stream));
     } else {
       IMSRG_CUDA_TRY(cudaMemcpyAsync(const_cast<double *>(R), io->R, bytes, cudaMemcpyHostToDevice, b->stream));
@@ -163,23 +164,40 @@ int commutator_launches(imsrg_basis *b, const double *L, int hL, const double *R
     IMSRG_CUDA_TRY(cudaStreamWaitEvent(b->stream, b->ev_join[k], 0));
     return IMSRG_OK;
   };
-  // E0 needs only L and R: its single CTA runs on side3 from here, beside the
-  // Pandya transform and the slicing, and is joined at the end (after the
-  // one-body assembly, where it ran before, it finished last: the one-body
-  // kernel runs slowly beside the 3,769 CTAs of the two-body assembly)
-  if (with_e0 && front) {
+  // E0 and the commutator_122 part of the two-body assembly need only L and
+  // R: E0's single CTA runs on side3 and the 122 sums (with the packed (L, R)
+  // pairs they read) on side4 from here, beside the Pandya transform, the
+  // slicing and the products.  E0 is joined at the end (after the one-body
+  // assembly, where it ran before, it finished last: the one-body kernel runs
+  // slowly beside the 3,769 CTAs of the two-body assembly), the 122 sums
+  // before the rest of the two-body assembly.
+  if (front) {
     if (serial) {
-      IMSRG_TRY(launch_e0(b, L, hL, R, hR, RES, b->stream));
+      if (with_e0) IMSRG_TRY(launch_e0(b, L, hL, R, hR, RES, b->stream));
+      IMSRG_TRY(launch_lr_pack(b, L, R, b->stream));
+      IMSRG_TRY(launch_asm2_122(b, L, hL, R, hR, RES, hRES, true, b->stream));
     } else {
       IMSRG_CUDA_TRY(cudaEventRecord(b->ev_fork[0], b->stream));
-      IMSRG_CUDA_TRY(cudaStreamWaitEvent(b->side3, b->ev_fork[0], 0));
-      IMSRG_TRY(launch_e0(b, L, hL, R, hR, RES, b->side3));
-      IMSRG_CUDA_TRY(cudaEventRecord(b->ev_join3, b->side3));
+      for (cudaStream_t s : {b->side3, b->side4}) {
+        IMSRG_CUDA_TRY(cudaStreamWaitEvent(s, b->ev_fork[0], 0));
+        if (overlap && packed) IMSRG_CUDA_TRY(cudaStreamWaitEvent(s, b->ev_rdev, 0));
+      }
+      if (with_e0) {
+        IMSRG_TRY(launch_e0(b, L, hL, R, hR, RES, b->side3));
+        IMSRG_CUDA_TRY(cudaEventRecord(b->ev_join3, b->side3));
+      }
+      IMSRG_TRY(launch_lr_pack(b, L, R, b->side4));
+      IMSRG_TRY(launch_asm2_122(b, L, hL, R, hR, RES, hRES, true, b->side4));
+      IMSRG_CUDA_TRY(cudaEventRecord(b->ev_pre, b->side4));
     }
   }
   const bool e0_front = (phases & kPhaseJoinE0Front) != 0;
   auto join_e0 = [&]() -> int {
     if (with_e0 && !serial) IMSRG_CUDA_TRY(cudaStreamWaitEvent(b->stream, b->ev_join3, 0));
+    return IMSRG_OK;
+  };
+  auto join_pre = [&]() -> int {
+    if (!serial) IMSRG_CUDA_TRY(cudaStreamWaitEvent(b->stream, b->ev_pre, 0));
     return IMSRG_OK;
   };
   if (overlap) {  // R's half is under way on side2; L's half once L is in
@@ -217,20 +235,19 @@ int commutator_launches(imsrg_basis *b, const double *L, int hL, const double *R
     if (front) IMSRG_TRY(launch_cc_forward(b, L, hL, R, hR));
     if (prods) IMSRG_TRY(launch_gemm_fp64(b, L, hL, R, hR));
   }
-  if (front && e0_front) IMSRG_TRY(join_e0());
+  if (front && e0_front) {  // phases in separate graphs: join what the front forked
+    IMSRG_TRY(join_e0());
+    IMSRG_TRY(join_pre());
+  }
   if (!back) return IMSRG_OK;
-  // one-body assembly beside the two-body assembly, after the packed (L, R)
-  // pairs of the 122 gathers, which are built beside the recoupling inputs
-  // (earlier, beside the Pandya transform, they slowed it)
+  // one-body assembly beside the two-body assembly
   IMSRG_TRY(fork(1));
-  IMSRG_TRY(launch_lr_pack(b, L, R, side));
-  if (!serial) IMSRG_CUDA_TRY(cudaEventRecord(b->ev_lr, side));
   IMSRG_TRY(launch_assemble_1body(b, L, hL, R, hR, RES, hRES, side));
   if (overlap && !packed) {
     // two-body elements by output range; each range's copy to the host runs on
     // side2 beside the assembly of the next (see imsrg_basis::asm2_el)
     IMSRG_TRY(launch_ph_inputs(b, hL, hR, precision));
-    IMSRG_CUDA_TRY(cudaStreamWaitEvent(b->stream, b->ev_lr, 0));
+    if (!e0_front) IMSRG_TRY(join_pre());
     for (int c = 0; c < kOutChunks; c++) {
       IMSRG_TRY(launch_asm2_range(b, L, hL, R, hR, RES, hRES, b->asm2_el[c], b->asm2_el[c + 1], true));
       IMSRG_CUDA_TRY(cudaEventRecord(b->ev_out[c], b->stream));
@@ -252,7 +269,7 @@ int commutator_launches(imsrg_basis *b, const double *L, int hL, const double *R
   {
     ProfScope ps(b, IMSRG_KERNEL_ASSEMBLE_2BODY);
     IMSRG_TRY(launch_ph_inputs(b, hL, hR, precision));
-    if (!serial) IMSRG_CUDA_TRY(cudaStreamWaitEvent(b->stream, b->ev_lr, 0));
+    if (!e0_front) IMSRG_TRY(join_pre());
     IMSRG_TRY(launch_asm2_range(b, L, hL, R, hR, RES, hRES, 0, b->T.n_asm2, false));
   }
   IMSRG_TRY(join(1));

@@ -408,7 +408,10 @@ int build_basis(imsrg_basis *b) {
   IMSRG_CUDA_TRY(cudaStreamCreateWithFlags(&b->side, cudaStreamNonBlocking));
   IMSRG_CUDA_TRY(cudaStreamCreateWithFlags(&b->side2, cudaStreamNonBlocking));
   IMSRG_CUDA_TRY(cudaStreamCreateWithFlags(&b->side3, cudaStreamNonBlocking));
+  IMSRG_CUDA_TRY(cudaStreamCreateWithFlags(&b->side4, cudaStreamNonBlocking));
   IMSRG_CUDA_TRY(cudaEventCreateWithFlags(&b->ev_join3, cudaEventDisableTiming));
+  IMSRG_CUDA_TRY(cudaEventCreateWithFlags(&b->ev_pre, cudaEventDisableTiming));
+  IMSRG_CUDA_TRY(cudaEventCreateWithFlags(&b->ev_rdev, cudaEventDisableTiming));
   IMSRG_CUDA_TRY(cudaEventCreateWithFlags(&b->ev_join2, cudaEventDisableTiming));
   IMSRG_CUDA_TRY(cudaEventCreateWithFlags(&b->ev_hostL, cudaEventDisableTiming));
   for (int k = 0; k < 2; k++) {
@@ -416,7 +419,6 @@ int build_basis(imsrg_basis *b) {
     IMSRG_CUDA_TRY(cudaEventCreateWithFlags(&b->ev_join[k], cudaEventDisableTiming));
   }
   IMSRG_CUDA_TRY(cudaEventCreateWithFlags(&b->ev_hostR, cudaEventDisableTiming));
-  IMSRG_CUDA_TRY(cudaEventCreateWithFlags(&b->ev_lr, cudaEventDisableTiming));
   IMSRG_CUDA_TRY(cudaEventCreateWithFlags(&b->ev_outj, cudaEventDisableTiming));
   for (cudaEvent_t &ev : b->ev_out) IMSRG_CUDA_TRY(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
   DevTables &T = b->T;
@@ -661,6 +663,33 @@ int build_basis(imsrg_basis *b) {
                       items_out.begin();
     T.n_asm2 = (int)ordered.size();
     T.n_ph = (int)zt.size();
+    {  // the commutator_122 sums by term count, 32 elements to a warp (see DevTables::pre_warp)
+      std::vector<std::vector<int>> by_n(32);
+      for (size_t h = 0; h < heads.size(); h++) by_n[heads[h].meta & 31].push_back((int)h);
+      std::vector<Asm2PreWarp> pw;
+      std::vector<unsigned> pe;
+      std::vector<unsigned long long> pt;
+      for (int n = 0; n < 32; n++)
+        for (size_t g0 = 0; g0 < by_n[n].size(); g0 += 32) {
+          Asm2PreWarp w{(long long)pt.size(), n, 0};
+          pw.push_back(w);
+          pt.resize(pt.size() + (size_t)32 * n, 0ull);
+          for (int l = 0; l < 32; l++) {
+            if (g0 + l >= by_n[n].size()) {
+              pe.push_back(0xFFFFFFFFu);
+              continue;
+            }
+            const Asm2Head &h = heads[by_n[n][g0 + l]];
+            const unsigned nd = (h.meta >> 18) & 3, diag = (h.meta >> 20) & 1;
+            pe.push_back((unsigned)h.e | nd << 28 | diag << 30);
+            for (int k = 0; k < n; k++) pt[(size_t)w.base + (size_t)32 * k + l] = terms[(size_t)h.start + k];
+          }
+        }
+      T.n_pre_warps = (int)pw.size();
+      IMSRG_TRY(dev_upload(b, pw, &T.pre_warp));
+      IMSRG_TRY(dev_upload(b, pe, &T.pre_el));
+      IMSRG_TRY(dev_upload(b, pt, &T.pre_terms));
+    }
     IMSRG_TRY(dev_upload(b, ordered, &T.asm2_head));
     IMSRG_TRY(dev_upload(b, ordered_out, &T.asm2_head_out));
     IMSRG_TRY(dev_upload(b, terms, &T.asm2_terms));
@@ -910,15 +939,17 @@ void free_basis_device(imsrg_basis *b) {
   if (b->side) cudaStreamDestroy(b->side);
   if (b->side2) cudaStreamDestroy(b->side2);
   if (b->side3) cudaStreamDestroy(b->side3);
-  b->side = b->side2 = b->side3 = nullptr;
+  if (b->side4) cudaStreamDestroy(b->side4);
+  b->side = b->side2 = b->side3 = b->side4 = nullptr;
   if (b->ev_join3) cudaEventDestroy(b->ev_join3);
-  b->ev_join3 = nullptr;
+  if (b->ev_pre) cudaEventDestroy(b->ev_pre);
+  if (b->ev_rdev) cudaEventDestroy(b->ev_rdev);
+  b->ev_join3 = b->ev_pre = b->ev_rdev = nullptr;
   if (b->ev_join2) cudaEventDestroy(b->ev_join2);
   if (b->ev_hostL) cudaEventDestroy(b->ev_hostL);
   if (b->ev_hostR) cudaEventDestroy(b->ev_hostR);
-  if (b->ev_lr) cudaEventDestroy(b->ev_lr);
   if (b->ev_outj) cudaEventDestroy(b->ev_outj);
-  b->ev_join2 = b->ev_hostL = b->ev_hostR = b->ev_lr = b->ev_outj = nullptr;
+  b->ev_join2 = b->ev_hostL = b->ev_hostR = b->ev_outj = nullptr;
   for (cudaEvent_t &ev : b->ev_out) {
     if (ev) cudaEventDestroy(ev);
     ev = nullptr;

@@ -65,6 +65,16 @@ struct DevTables {
   int n_asm2;
   const struct PhTerm *ph_terms;
   int n_ph;
+  // The commutator_122 sums again, for the kernel that runs them ahead of the
+  // products (k_asm2_122): warp g takes elements pre_el[32 g .. 32 g + 32),
+  // all with pre_warp[g].n122 terms; term k of its lane l is
+  // pre_terms[pre_warp[g].base + 32 k + l] (one coalesced load per term).
+  // pre_el: bits 0-27 flat index, 28-29 identical orbit pairs, 30 diagonal;
+  // 0xFFFFFFFF pads a warp.
+  const struct Asm2PreWarp *pre_warp;
+  const unsigned *pre_el;
+  const unsigned long long *pre_terms;
+  int n_pre_warps;
   const int *ccf_order;    // cross-coupled elements (bits 0-23), with their block in bits 24-30 if ccf_packed
   int n_ccf;
   int ccf_packed;
@@ -96,6 +106,14 @@ struct OneBodyTerm {
   int idx;
   int meta;     // bits 0-1 kind, bit 2 trans, bit 3 W2 (else W1), bits 8.. ph
   double coef;  // (2J+1) x phase x sqrt(2)^n
+};
+
+// One warp of the commutator_122 sums run ahead of the products (see
+// DevTables::pre_warp).
+struct __align__(16) Asm2PreWarp {
+  long long base;  // first term of lane 0
+  int n122;
+  int pad;
 };
 
 // One J'-term of the inverse Pandya recoupling of commutator_222_ph
@@ -241,13 +259,16 @@ struct imsrg_basis {
   cudaStream_t own_stream = nullptr;  // the library's own stream
   // Library streams for independent launches inside one commutator, forked
   // from and joined back into `stream` with events.
-  // side3 runs E0 (one CTA) from the first fork to the end.
-  cudaStream_t side = nullptr, side2 = nullptr, side3 = nullptr;
+  // side3 runs E0 (one CTA) from the first fork to the end; side4 the
+  // commutator_122 sums, which need only L and R, beside the Pandya transform,
+  // the digit images and the products.
+  cudaStream_t side = nullptr, side2 = nullptr, side3 = nullptr, side4 = nullptr;
+  cudaEvent_t ev_pre = nullptr;    // the commutator_122 sums are in RES
+  cudaEvent_t ev_rdev = nullptr;   // a packed host operand R is unpacked on the device
   cudaEvent_t ev_fork[2] = {nullptr, nullptr}, ev_join[2] = {nullptr, nullptr}, ev_join2 = nullptr;
   cudaEvent_t ev_join3 = nullptr;
   cudaEvent_t ev_hostL = nullptr;  // a host operand L has arrived (commutator_host)
   cudaEvent_t ev_hostR = nullptr;  // a host operand R has arrived
-  cudaEvent_t ev_lr = nullptr;     // the packed (L, R) pairs are built
   cudaEvent_t ev_out[imsrg::kOutChunks] = {}, ev_outj = nullptr;  // chunked copy of RES to the host
   // Two-body work order by output range: elements asm2_el[c] .. asm2_el[c+1]
   // write only RES[asm2_addr[c] ..) (the mirror of a square-array element
@@ -356,6 +377,10 @@ int launch_gemm_fp64_merged(const GemmProb *d_probs, int nprobs, int ntiles, int
 int launch_ph_inputs(imsrg_basis *b, int hL, int hR, int precision);
 // b->lr from L and R on stream st (before the two-body assembly)
 int launch_lr_pack(imsrg_basis *b, const double *L, const double *R, cudaStream_t st);
+// commutator_122 part of every two-body element into RES (the assembly after
+// the products adds the rest); packed: from b->lr (launch_lr_pack first)
+int launch_asm2_122(imsrg_basis *b, const double *L, int hL, const double *R, int hR, double *RES, int hRES,
+                    bool packed, cudaStream_t st);
 int launch_asm2_range(imsrg_basis *b, const double *L, int hL, const double *R, int hR, double *RES, int hRES,
                       long w0, long w1, bool by_range);
 int launch_assemble_1body(imsrg_basis *b, const double *L, int hL, const double *R, int hR, double *RES, int hRES,

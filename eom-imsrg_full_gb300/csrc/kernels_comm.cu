@@ -353,12 +353,13 @@ __device__ void energy_block(const DevTables &T, const double *L, int hL, const 
 }
 
 // commutator_122 (commutators.f90:283-396) of one element: f_L V_R - f_R V_L
-// over its leg terms
+// over its leg terms (term k at tm[k * STRIDE])
+template <int STRIDE>
 __device__ __forceinline__ double sum122(const unsigned long long *tm, int n122, const double *L, int nL,
-                                              const double *R, int nR) {
+                                         const double *R, int nR) {
   double t = 0.0;
   for (int k = 0; k < n122; k++) {
-    const unsigned long long u = tm[k];
+    const unsigned long long u = tm[k * STRIDE];
     const long vi = (long)(u & 0xFFFFFFFull), fi = (long)((u >> 28) & 0xFFFFFull);
     const int sg = (int)(u >> 48) & 1, nsq = (int)(u >> 49) & 3, tr = (int)(u >> 51) & 1, ftr = (int)(u >> 52) & 1;
     double vR = dflip(R[vi], tr & nR), vL = dflip(L[vi], tr & nL);
@@ -377,11 +378,12 @@ __device__ __forceinline__ double sum122(const unsigned long long *tm, int n122,
 // The same sum from the packed (c L, c R) pairs of b->lr: one 16-byte gather
 // and no multiplications per term.  c x rounds exactly as above, and a sign
 // flip commutes with it, so the sum is bit-identical.
+template <int STRIDE>
 __device__ __forceinline__ double sum122_lr(const unsigned long long *tm, int n122, const double *L, int nL,
                                             const double *R, int nR, const double2 *__restrict__ LR) {
   double t = 0.0;
   for (int k = 0; k < n122; k++) {
-    const unsigned long long u = tm[k];
+    const unsigned long long u = tm[k * STRIDE];
     const long vi = (long)(u & 0xFFFFFFFull), fi = (long)((u >> 28) & 0xFFFFFull);
     const int sg = (int)(u >> 48) & 1, tr = (int)(u >> 51) & 1, ftr = (int)(u >> 52) & 1;
     const double2 v = LR[vi];
@@ -410,14 +412,39 @@ __global__ void __launch_bounds__(256) k_lr_pack(DevTables T, const double *__re
   LR[i] = make_double2(x, y);
 }
 
+// The commutator_122 part of every two-body element (upper triangles), with
+// the element's 1/sqrt(1 + delta) factors and the diagonal's sign, into RES:
+// it needs only L and R, so it runs ahead of the products, and the assembly
+// after them (k_assemble_2body<., true>) starts from it.  One warp per 32
+// elements of equal term count; term k of every lane is one coalesced load.
+// The arithmetic is the assembly's own, so RES is bit-identical either way.
+template <bool PACKED>
+__global__ void __launch_bounds__(ASM2_THREADS) k_asm2_122(DevTables T, const double *__restrict__ L, int hL,
+                                                           const double *__restrict__ R, int hR, int hRES,
+                                                           const double2 *__restrict__ LR, double *RES) {
+  const int g = (int)(((long)blockIdx.x * blockDim.x + threadIdx.x) >> 5), lane = threadIdx.x & 31;
+  if (g >= T.n_pre_warps) return;
+  const unsigned pe = T.pre_el[(long)g * 32 + lane];
+  if (pe >> 31) return;  // padding
+  const Asm2PreWarp W = T.pre_warp[g];
+  const unsigned long long *tm = T.pre_terms + W.base + lane;
+  const int nL = hL < 0, nR = hR < 0;
+  double t = PACKED ? sum122_lr<32>(tm, W.n122, L, nL, R, nR, LR) : sum122<32>(tm, W.n122, L, nL, R, nR);
+  const int nd = (pe >> 28) & 3;
+  if (nd) t = t * (nd == 1 ? 0.7071067811865476 : 0.5);
+  if ((pe >> 30) & 1) t = dflip(t, hRES < 0);
+  RES[pe & 0x0FFFFFFFu] = t;
+}
+
 // Every two-body element of RES once (upper triangles of square arrays, the
 // mirror written alongside): the one-body insertions of commutator_122, the
 // antisymmetrised ladder epilogue of 222_pp_hh (:658-764) and the 222_ph
 // recoupling sum over J' of {6j} Z(J').  Thread t takes element w0 + t of the
 // work order `heads` while below w1.  LR != nullptr: the 122 sums read the
-// packed pairs (k_lr_pack).  has220 (the allocation-free path, w0 = 0): each
-// CTA leaves its commutator_220 partial in e0p for k_energy.
-template <bool PACKED>
+// packed pairs (k_lr_pack).  PRE: the 122 part is already in RES
+// (k_asm2_122).  has220 (the allocation-free path, w0 = 0): each CTA leaves
+// its commutator_220 partial in e0p for k_energy.
+template <bool PACKED, bool PRE>
 __global__ void __launch_bounds__(ASM2_THREADS) k_assemble_2body(DevTables T, const double *__restrict__ L, int hL,
                                                                  const double *__restrict__ R, int hR,
                                                                  const double *__restrict__ W1,
@@ -434,13 +461,18 @@ __global__ void __launch_bounds__(ASM2_THREADS) k_assemble_2body(DevTables T, co
     const unsigned long long *tm = T.asm2_terms + h.start;
     const unsigned meta = h.meta;
     const int nL = hL < 0, nR = hR < 0, nres = hRES < 0, npm = (hL * hR) < 0;
-    double t = PACKED ? sum122_lr(tm, meta & 31, L, nL, R, nR, LR) : sum122(tm, meta & 31, L, nL, R, nR);
-    // / sqrt(1 + delta_ab) / sqrt(1 + delta_cd)
     const int nd = (meta >> 18) & 3;
-    if (nd) t = t * (nd == 1 ? 0.7071067811865476 : 0.5);
     const bool diag = (meta >> 20) & 1, square = (meta >> 21) & 1;
     const long e = h.e, em = h.em;
-    if (diag) t = dflip(t, nres);
+    double t;
+    if (PRE) {
+      t = RES[e];
+    } else {
+      t = PACKED ? sum122_lr<1>(tm, meta & 31, L, nL, R, nR, LR) : sum122<1>(tm, meta & 31, L, nL, R, nR);
+      // / sqrt(1 + delta_ab) / sqrt(1 + delta_cd)
+      if (nd) t = t * (nd == 1 ? 0.7071067811865476 : 0.5);
+      if (diag) t = dflip(t, nres);
+    }
     t = t + W1[e];
     t = t - W2[e];
     if (square) t = t - dflip(W1[em] - W2[em], npm);
@@ -755,11 +787,24 @@ int launch_asm2_range(imsrg_basis *b, const double *L, int hL, const double *R, 
                       long w0, long w1, bool by_range) {
   const long n = w1 - w0;
   if (n > 0) {
-    k_assemble_2body<true><<<(unsigned)((n + ASM2_THREADS - 1) / ASM2_THREADS), ASM2_THREADS, 0, b->stream>>>(
+    k_assemble_2body<true, true><<<(unsigned)((n + ASM2_THREADS - 1) / ASM2_THREADS), ASM2_THREADS, 0, b->stream>>>(
         b->T, L, hL, R, hR, b->w1, b->w2, b->zph, RES, hRES, by_range ? b->T.asm2_head_out : b->T.asm2_head, w0,
         w1, b->lr, 0, nullptr);
     b->launches++;
   }
+  return cuda_status(cudaGetLastError());
+}
+
+int launch_asm2_122(imsrg_basis *b, const double *L, int hL, const double *R, int hR, double *RES, int hRES,
+                    bool packed, cudaStream_t st) {
+  if (b->T.n_pre_warps == 0) return IMSRG_OK;
+  ProfScope ps(b, IMSRG_KERNEL_ASSEMBLE_2BODY, st);
+  const unsigned grid = (unsigned)(((long)b->T.n_pre_warps * 32 + ASM2_THREADS - 1) / ASM2_THREADS);
+  if (packed)
+    k_asm2_122<true><<<grid, ASM2_THREADS, 0, st>>>(b->T, L, hL, R, hR, hRES, b->lr, RES);
+  else
+    k_asm2_122<false><<<grid, ASM2_THREADS, 0, st>>>(b->T, L, hL, R, hR, hRES, nullptr, RES);
+  b->launches++;
   return cuda_status(cudaGetLastError());
 }
 
@@ -825,7 +870,7 @@ int launch_commutator_fp64_ws(imsrg_basis *b, const Workspace &ws, const double 
   const long n2 = b->T.n_asm2;
   if (n2 > 0) {
     const int has220 = with_e0 && hL * hR == -1;
-    k_assemble_2body<false><<<(unsigned)((n2 + ASM2_THREADS - 1) / ASM2_THREADS), ASM2_THREADS, 0, st>>>(
+    k_assemble_2body<false, false><<<(unsigned)((n2 + ASM2_THREADS - 1) / ASM2_THREADS), ASM2_THREADS, 0, st>>>(
         b->T, L, hL, R, hR, ws.w1, ws.w2, ws.zph, RES, hRES, b->T.asm2_head, 0, n2, nullptr, has220, ws.e0p);
     b->launches++;
   }
@@ -845,7 +890,7 @@ int launch_commutator_fp64_ws(imsrg_basis *b, const Workspace &ws, const double 
 int preload_commutator_fp64_ws() {
   cudaFuncAttributes a;
   const void *fns[] = {(const void *)k_cc_forward<3>, (const void *)k_gemm_fp64<false>, (const void *)k_ph_inputs,
-                       (const void *)k_assemble_2body<false>, (const void *)k_assemble_1body, (const void *)k_energy};
+                       (const void *)k_assemble_2body<false, false>, (const void *)k_assemble_1body, (const void *)k_energy};
   for (const void *f : fns) {
     cudaError_t e = cudaFuncGetAttributes(&a, f);
     if (e != cudaSuccess) return cuda_status(e);
