@@ -120,11 +120,20 @@ int commutator_launches(imsrg_basis *b, const double *L, int hL, const double *R
   // unpacked on the device; RES packed before one copy back
   const bool packed = io && io->Lst;
   const size_t pbytes = (size_t)b->neq * sizeof(double);
+  // packed page-locked operands the device addresses: no staging copies
+  const bool direct = overlap && packed && io->Ldev && io->Rdev && io->RESdev;
   // the transform also reduces the LCC/RCC block exponents (split precision)
   int *cc_exps = nullptr, gL = 0, gR = 0;
   if (overlap) {
     if (oz) IMSRG_TRY(ozaki_cc_exponents(b, b->stream, &cc_exps, &gL, &gR));
-    if (packed) {
+    if (direct) {
+      // the unpack kernels of R (side2) and L read the host arrays at once
+      IMSRG_CUDA_TRY(cudaEventRecord(b->ev_hostR, b->stream));
+      IMSRG_CUDA_TRY(cudaStreamWaitEvent(b->side2, b->ev_hostR, 0));
+      IMSRG_TRY(launch_unpack(b, io->Rdev, hR, const_cast<double *>(R), b->side2));
+      IMSRG_CUDA_TRY(cudaEventRecord(b->ev_rdev, b->side2));  // R is on the device
+      IMSRG_TRY(launch_unpack(b, io->Ldev, hL, const_cast<double *>(L), b->stream));
+    } else if (packed) {
       IMSRG_CUDA_TRY(cudaMemcpyAsync(io->Rst, io->R, pbytes, cudaMemcpyHostToDevice, b->stream));
       IMSRG_CUDA_TRY(cudaEventRecord(b->ev_hostR, b->stream));
       IMSRG_CUDA_TRY(cudaMemcpyAsync(io->Lst, io->L, pbytes, cudaMemcpyHostToDevice, b->stream));
@@ -274,7 +283,9 @@ int commutator_launches(imsrg_basis *b, const double *L, int hL, const double *R
   }
   IMSRG_TRY(join(1));
   if (!e0_front) IMSRG_TRY(join_e0());
-  if (io && packed) {
+  if (direct) {
+    IMSRG_TRY(launch_pack(b, RES, io->RESdev, b->stream, true));
+  } else if (io && packed) {
     IMSRG_TRY(launch_pack(b, RES, io->RESst, b->stream));
     IMSRG_CUDA_TRY(cudaMemcpyAsync(io->RES, io->RESst, pbytes, cudaMemcpyDeviceToHost, b->stream));
   } else if (io) {
@@ -298,18 +309,28 @@ int commutator_dev(imsrg_basis *b, const double *L, int hL, const double *R, int
   cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
   IMSRG_CUDA_TRY(cudaStreamIsCapturing(b->stream, &cs));
   bool pinned = true;  // host copies enter a graph only from page-locked memory
-  if (io)
-    for (const void *p : {(const void *)io->L, (const void *)io->R, (const void *)io->RES}) {
+  void *dev[3] = {nullptr, nullptr, nullptr};  // their device addresses, when mapped
+  if (io) {
+    const void *hp[3] = {io->L, io->R, io->RES};
+    for (int k = 0; k < 3; k++) {
       cudaPointerAttributes a{};
-      if (cudaPointerGetAttributes(&a, p) != cudaSuccess || a.type != cudaMemoryTypeHost) {
+      if (cudaPointerGetAttributes(&a, hp[k]) != cudaSuccess || a.type != cudaMemoryTypeHost) {
         cudaGetLastError();
         pinned = false;
+      } else {
+        dev[k] = a.devicePointer;
       }
     }
+  }
   HostIO hio{};
   if (io) {
     hio = *io;
     hio.pinned = pinned;
+    if (pinned && hio.Lst) {
+      hio.Ldev = (const double *)dev[0];
+      hio.Rdev = (const double *)dev[1];
+      hio.RESdev = (double *)dev[2];
+    }
     io = &hio;
   }
   const bool graphable = !b->prof.on && cs == cudaStreamCaptureStatusNone && pinned &&
@@ -450,8 +471,7 @@ int imsrg_gpu_block_dims(const imsrg_basis_t *b, int q, int *npp, int *nph, int 
 
 int imsrg_gpu_synchronize(imsrg_basis_t *b) {
   if (!b) return IMSRG_ERR_INVALID;
-  IMSRG_CUDA_TRY(cudaStreamSynchronize(b->stream));
-  return imsrg::ozaki_check_error(b);
+  return imsrg::synchronize_checked(b);
 }
 
 int imsrg_gpu_launch_count(const imsrg_basis_t *b, long *count) {
@@ -662,8 +682,7 @@ int imsrg_gpu_commutator_host(imsrg_basis_t *b, const double *L, int herm_L, con
   const imsrg::HostIO io{L, R, RES};
   IMSRG_TRY(imsrg::commutator_dev(b, dL->d, herm_L, dR->d, herm_R, dRES->d, dRES->herm, precision, with_e0 ? 1 : 0,
                                   &io));
-  IMSRG_CUDA_TRY(cudaStreamSynchronize(b->stream));
-  return imsrg::ozaki_check_error(b);
+  return imsrg::synchronize_checked(b);
 }
 
 int imsrg_gpu_commutator_host_packed(imsrg_basis_t *b, const double *L, int herm_L, const double *R, int herm_R,
@@ -692,8 +711,7 @@ int imsrg_gpu_commutator_host_packed(imsrg_basis_t *b, const double *L, int herm
   io.RESst = sRES->d;
   IMSRG_TRY(imsrg::commutator_dev(b, dL->d, herm_L, dR->d, herm_R, dRES->d, dRES->herm, precision, with_e0 ? 1 : 0,
                                   &io));
-  IMSRG_CUDA_TRY(cudaStreamSynchronize(b->stream));
-  return imsrg::ozaki_check_error(b);
+  return imsrg::synchronize_checked(b);
 }
 
 }  // extern "C"

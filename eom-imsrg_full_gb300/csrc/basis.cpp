@@ -403,6 +403,7 @@ int build_basis(imsrg_basis *b) {
   // --- device copies
   cudaError_t ce = cudaGetDevice(&b->device);
   if (ce != cudaSuccess) return cuda_status(ce);
+  IMSRG_CUDA_TRY(cudaDeviceGetAttribute(&b->num_sms, cudaDevAttrMultiProcessorCount, b->device));
   IMSRG_CUDA_TRY(cudaStreamCreateWithFlags(&b->own_stream, cudaStreamNonBlocking));
   b->stream = b->own_stream;
   IMSRG_CUDA_TRY(cudaStreamCreateWithFlags(&b->side, cudaStreamNonBlocking));

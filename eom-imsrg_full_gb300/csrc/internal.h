@@ -207,6 +207,11 @@ struct HostIO {
   // buffers the copies land in, unpacked into L and R on the device; RES is
   // packed into RESst before its one copy back
   double *Lst = nullptr, *Rst = nullptr, *RESst = nullptr;
+  // packed page-locked host arrays the device can address (set by
+  // commutator_dev): the unpack kernels read L and R, and the pack kernel
+  // writes RES, over the host link directly, with no staging copies
+  const double *Ldev = nullptr, *Rdev = nullptr;
+  double *RESdev = nullptr;
 };
 // The two-body part of RES is assembled, and copied back to a page-locked host
 // result, in this many address ranges, so that each range's copy runs beside
@@ -277,6 +282,7 @@ struct imsrg_basis {
   // to c is assembled.
   long asm2_el[imsrg::kOutChunks + 1] = {}, asm2_addr[imsrg::kOutChunks + 1] = {};
   int device = 0;
+  int num_sms = 1;  // multiprocessors of the device
   imsrg::Profiler prof;
   // commutator workspace
   double *w1 = nullptr, *w2 = nullptr, *lcc = nullptr, *rcc = nullptr, *wcc = nullptr;
@@ -396,7 +402,10 @@ int launch_generator(imsrg_basis *b, const double *Hden, int hH, const double *H
 int launch_white_tangent(imsrg_basis *b, const double *H, const double *dH, int hH, double *dETA);
 // Hb += (d White / d H)^T ETAb (reverse mode; monob: norb x norb scratch)
 int launch_white_adjoint(imsrg_basis *b, const double *H, int hH, const double *ETAb, double *Hb, double *monob);
-int launch_pack(imsrg_basis *b, const double *flat, double *packed, cudaStream_t st = nullptr);
+// (un)pack between the flat layout and vectorize order; `packed` may be
+// device-addressable page-locked host memory (to_host: a grid sized for
+// writes over the host link)
+int launch_pack(imsrg_basis *b, const double *flat, double *packed, cudaStream_t st = nullptr, bool to_host = false);
 int launch_unpack(imsrg_basis *b, const double *packed, int herm, double *flat, cudaStream_t st = nullptr);
 int launch_check_finite(imsrg_basis *b, const double *op, int *d_flag);
 int launch_normal_order(imsrg_basis *b, const double *Tin, int herm, double *H);
@@ -427,6 +436,9 @@ int ozaki_slice(imsrg_basis *b, const double *L, const double *R, int part, cuda
 int ozaki_cc_exponents(imsrg_basis *b, cudaStream_t st, int **exps, int *gL, int *gR);
 int ozaki_mma(imsrg_basis *b, int hL, int hR);
 int ozaki_check_error(imsrg_basis *b);  // IMSRG_ERR_TIMEOUT if a bounded device wait gave up
+// synchronise the basis stream and then check as ozaki_check_error, with one
+// synchronisation (the flag is read back behind the work)
+int synchronize_checked(imsrg_basis *b);
 bool ozaki_tuned(imsrg_basis *b);       // the CTA schedule has been autotuned
 // After a split-precision product WCC holds exact int64 level sums v with
 // WCC = v 2^k, k = (exps[g.x] - 1022) + (exps[g.y] - 1022) - kshift for the

@@ -277,6 +277,14 @@ __device__ __forceinline__ void tmem_ld16(uint32_t taddr, uint32_t *r) {
 
 __device__ __forceinline__ void tmem_ld_wait() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
 
+// The tail accumulator rounded to an integer.  Below 2^31 in magnitude (always
+// at five digits or fewer) the 32-bit conversion rounds exactly as the 64-bit
+// one, and it runs on the conversion pipe rather than the FP64 pipe, which the
+// 64-bit conversion of every output kept busy for a third of the kernel.
+__device__ __forceinline__ long long tail_to_ll(float x) {
+  return fabsf(x) < 2147483648.0f ? (long long)__float2int_rn(x) : __float2ll_rn(x);
+}
+
 // ---------------------------------------------------------------------------
 // 1. block exponents: max biased exponent of each group (integer atomicMax,
 //    order-independent, so the result is deterministic)
@@ -654,7 +662,7 @@ __global__ void __launch_bounds__(OZ_THREADS, 1) k_oz_mma(const OzProb *__restri
   (((long long)__float2int_rn(__uint_as_float(acc[0][c])) << (7 * (LMAX - 2))) +         \
    ((long long)__float2int_rn(__uint_as_float(acc[1][c])) << (7 * (LMAX - 3))) +         \
    ((long long)__float2int_rn(__uint_as_float(acc[2][c])) << (7 * (LMAX - 4))) +         \
-   __float2ll_rn(__uint_as_float(acc[3][c])))
+   tail_to_ll(__uint_as_float(acc[3][c])))
         if (nch == 1 && !raw) {
           const int k = (exps[gA] - 1022) + (exps[gB] - 1022) - 7 * LMAX;  // result = v * 2^k
 #pragma unroll
@@ -1163,10 +1171,19 @@ int ozaki_mma(imsrg_basis *b, int hL, int hR) {
 int ozaki_check_error(imsrg_basis *b) {
   OzPlan *pl = plan_of(b);
   if (!pl || !pl->d_err) return IMSRG_OK;
-  int h = 0;
-  IMSRG_CUDA_TRY(cudaMemcpyAsync(&h, pl->d_err, sizeof(int), cudaMemcpyDeviceToHost, b->stream));
+  return synchronize_checked(b);
+}
+
+// The engine's error flag comes back into a page-locked slot queued behind
+// the work, so one stream synchronisation serves both.
+int synchronize_checked(imsrg_basis *b) {
+  OzPlan *pl = plan_of(b);
+  int *slot = reinterpret_cast<int *>(b->h_scal + 63);
+  *slot = 0;
+  if (pl && pl->d_err)
+    IMSRG_CUDA_TRY(cudaMemcpyAsync(slot, pl->d_err, sizeof(int), cudaMemcpyDeviceToHost, b->stream));
   IMSRG_CUDA_TRY(cudaStreamSynchronize(b->stream));
-  if (h) {
+  if (*slot) {
     cudaMemsetAsync(pl->d_err, 0, sizeof(int), b->stream);
     return IMSRG_ERR_TIMEOUT;
   }
