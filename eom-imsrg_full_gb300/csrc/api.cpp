@@ -174,17 +174,15 @@ int commutator_launches(imsrg_basis *b, const double *L, int hL, const double *R
     return IMSRG_OK;
   };
   // E0 and the commutator_122 part of the two-body assembly need only L and
-  // R: E0's single CTA runs on side3 and the 122 sums (with the packed (L, R)
-  // pairs they read) on side4 from here, beside the Pandya transform, the
-  // slicing and the products.  E0 is joined at the end (after the one-body
+  // R: E0's single CTA runs on side3 and the 122 sums on side4 from here,
+  // beside the Pandya transform, the slicing and the products.  E0 is joined at the end (after the one-body
   // assembly, where it ran before, it finished last: the one-body kernel runs
   // slowly beside the 3,769 CTAs of the two-body assembly), the 122 sums
   // before the rest of the two-body assembly.
   if (front) {
     if (serial) {
       if (with_e0) IMSRG_TRY(launch_e0(b, L, hL, R, hR, RES, b->stream));
-      IMSRG_TRY(launch_lr_pack(b, L, R, b->stream));
-      IMSRG_TRY(launch_asm2_122(b, L, hL, R, hR, RES, hRES, true, b->stream));
+      IMSRG_TRY(launch_asm2_122(b, L, hL, R, hR, RES, hRES, b->stream));
     } else {
       IMSRG_CUDA_TRY(cudaEventRecord(b->ev_fork[0], b->stream));
       for (cudaStream_t s : {b->side3, b->side4}) {
@@ -195,8 +193,7 @@ int commutator_launches(imsrg_basis *b, const double *L, int hL, const double *R
         IMSRG_TRY(launch_e0(b, L, hL, R, hR, RES, b->side3));
         IMSRG_CUDA_TRY(cudaEventRecord(b->ev_join3, b->side3));
       }
-      IMSRG_TRY(launch_lr_pack(b, L, R, b->side4));
-      IMSRG_TRY(launch_asm2_122(b, L, hL, R, hR, RES, hRES, true, b->side4));
+      IMSRG_TRY(launch_asm2_122(b, L, hL, R, hR, RES, hRES, b->side4));
       IMSRG_CUDA_TRY(cudaEventRecord(b->ev_pre, b->side4));
     }
   }

@@ -905,8 +905,6 @@ int build_basis(imsrg_basis *b) {
   b->wcc = (double *)p;
   IMSRG_TRY(dev_alloc(b, (size_t)T.n_ph * sizeof(double), &p));
   b->zph = (double *)p;
-  IMSRG_TRY(dev_alloc(b, b->nfull * sizeof(double2), &p));
-  b->lr = (double2 *)p;
   IMSRG_TRY(dev_alloc(b, (size_t)2 * N * N * sizeof(double), &p));  // monopoles of H and of a tangent dH
   b->mono = (double *)p;
   IMSRG_TRY(dev_alloc(b, 64 * sizeof(double), &p));

@@ -287,10 +287,6 @@ struct imsrg_basis {
   // commutator workspace
   double *w1 = nullptr, *w2 = nullptr, *lcc = nullptr, *rcc = nullptr, *wcc = nullptr;
   double *zph = nullptr;        // 222_ph recoupling inputs (T.n_ph)
-  // [flat index] (c L, c R) of the commutator's operands with c the element's
-  // sqrt(2)^vsq factor as v_elem applies it: one 16-byte gather per
-  // commutator_122 term instead of two (two-body indices only)
-  double2 *lr = nullptr;
   long off_2b = 0;              // first two-body index of the flat layout
   double *mono = nullptr;       // 2 x norb x norb monopole tables of the White generator (H, tangent dH)
   double *scal = nullptr;       // small device scratch for reductions (E0, norms)
@@ -378,15 +374,13 @@ int gemm_fp64_merged(imsrg_basis *const *bases, int n, const double *const *L, c
 int launch_gemm_fp64_merged(const GemmProb *d_probs, int nprobs, int ntiles, int hL, int hR, const int *act,
                             cudaStream_t st);
 // the two-body assembly: the recoupling inputs of 222_ph, then the elements
-// [w0, w1) of the signature work order or of the order by output range
-// (which read b->lr, see launch_lr_pack)
+// [w0, w1) of the signature work order or of the order by output range, on
+// top of launch_asm2_122's part in RES
 int launch_ph_inputs(imsrg_basis *b, int hL, int hR, int precision);
-// b->lr from L and R on stream st (before the two-body assembly)
-int launch_lr_pack(imsrg_basis *b, const double *L, const double *R, cudaStream_t st);
-// commutator_122 part of every two-body element into RES (the assembly after
-// the products adds the rest); packed: from b->lr (launch_lr_pack first)
+// commutator_122 part of every two-body element into RES on stream st (the
+// assembly after the products adds the rest)
 int launch_asm2_122(imsrg_basis *b, const double *L, int hL, const double *R, int hR, double *RES, int hRES,
-                    bool packed, cudaStream_t st);
+                    cudaStream_t st);
 int launch_asm2_range(imsrg_basis *b, const double *L, int hL, const double *R, int hR, double *RES, int hRES,
                       long w0, long w1, bool by_range);
 int launch_assemble_1body(imsrg_basis *b, const double *L, int hL, const double *R, int hR, double *RES, int hRES,

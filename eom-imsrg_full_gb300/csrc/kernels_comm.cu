@@ -1,9 +1,8 @@
 // kernels_comm.cu -- FP64 kernels of one scalar-scalar commutator [L, R].
 //
 // One commutator is these launches on the basis stream (4 on a side stream
-// beside 3, after lr_pack, which packs the (sqrt(2)-normalised) pairs (L, R)
-// of every two-body element for the commutator_122 gathers of 3 beside its
-// recoupling inputs; 5 on a third stream from the start, beside 1 and 2):
+// beside 3; 5 and the commutator_122 sums of 3 (k_asm2_122) on streams of
+// their own from the start, beside 1 and 2):
 //   1. cc_forward      Pandya transform of L and R into LCC, RCC
 //                      (calculate_cross_coupled, cross_coupled.f90:1190-1300)
 //   2. gemm_fp64       every dense contraction as one grouped GEMM: the 12
@@ -375,53 +374,18 @@ __device__ __forceinline__ double sum122(const unsigned long long *tm, int n122,
   return t;
 }
 
-// The same sum from the packed (c L, c R) pairs of b->lr: one 16-byte gather
-// and no multiplications per term.  c x rounds exactly as above, and a sign
-// flip commutes with it, so the sum is bit-identical.
-template <int STRIDE>
-__device__ __forceinline__ double sum122_lr(const unsigned long long *tm, int n122, const double *L, int nL,
-                                            const double *R, int nR, const double2 *__restrict__ LR) {
-  double t = 0.0;
-  for (int k = 0; k < n122; k++) {
-    const unsigned long long u = tm[k * STRIDE];
-    const long vi = (long)(u & 0xFFFFFFFull), fi = (long)((u >> 28) & 0xFFFFFull);
-    const int sg = (int)(u >> 48) & 1, tr = (int)(u >> 51) & 1, ftr = (int)(u >> 52) & 1;
-    const double2 v = LR[vi];
-    const double vL = dflip(v.x, tr & nL), vR = dflip(v.y, tr & nR);
-    const double fL = dflip(L[fi], (ftr & nL) ^ sg), fR = dflip(R[fi], (ftr & nR) ^ sg ^ 1);
-    t = fma(fL, vR, t);
-    t = fma(fR, vL, t);
-  }
-  return t;
-}
-
-// (c L, c R) of every two-body element, c = sqrt(2)^vsq as v_elem applies it
-// (device.cuh, the same constants).
-__global__ void __launch_bounds__(256) k_lr_pack(DevTables T, const double *__restrict__ L,
-                                                 const double *__restrict__ R, double2 *__restrict__ LR, long i0,
-                                                 long n) {
-  const long i = i0 + (long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n) return;
-  double x = L[i], y = R[i];
-  const int s = T.vsq[i];
-  if (s) {
-    const double c = s == 1 ? IMSRG_SQRT2 : 2.0000000000000004;
-    x = x * c;
-    y = y * c;
-  }
-  LR[i] = make_double2(x, y);
-}
-
 // The commutator_122 part of every two-body element (upper triangles), with
 // the element's 1/sqrt(1 + delta) factors and the diagonal's sign, into RES:
 // it needs only L and R, so it runs ahead of the products, and the assembly
-// after them (k_assemble_2body<., true>) starts from it.  One warp per 32
+// after them (k_assemble_2body<true>) starts from it.  One warp per 32
 // elements of equal term count; term k of every lane is one coalesced load.
 // The arithmetic is the assembly's own, so RES is bit-identical either way.
-template <bool PACKED>
+// (Packing the sqrt(2)-scaled (L, R) pairs first, for one 16-byte gather per
+// term, measured slower here: the pack kernel took more of the shared front
+// than it saved.)
 __global__ void __launch_bounds__(ASM2_THREADS) k_asm2_122(DevTables T, const double *__restrict__ L, int hL,
                                                            const double *__restrict__ R, int hR, int hRES,
-                                                           const double2 *__restrict__ LR, double *RES) {
+                                                           double *RES) {
   const int g = (int)(((long)blockIdx.x * blockDim.x + threadIdx.x) >> 5), lane = threadIdx.x & 31;
   if (g >= T.n_pre_warps) return;
   const unsigned pe = T.pre_el[(long)g * 32 + lane];
@@ -429,7 +393,7 @@ __global__ void __launch_bounds__(ASM2_THREADS) k_asm2_122(DevTables T, const do
   const Asm2PreWarp W = T.pre_warp[g];
   const unsigned long long *tm = T.pre_terms + W.base + lane;
   const int nL = hL < 0, nR = hR < 0;
-  double t = PACKED ? sum122_lr<32>(tm, W.n122, L, nL, R, nR, LR) : sum122<32>(tm, W.n122, L, nL, R, nR);
+  double t = sum122<32>(tm, W.n122, L, nL, R, nR);
   const int nd = (pe >> 28) & 3;
   if (nd) t = t * (nd == 1 ? 0.7071067811865476 : 0.5);
   if ((pe >> 30) & 1) t = dflip(t, hRES < 0);
@@ -440,19 +404,17 @@ __global__ void __launch_bounds__(ASM2_THREADS) k_asm2_122(DevTables T, const do
 // mirror written alongside): the one-body insertions of commutator_122, the
 // antisymmetrised ladder epilogue of 222_pp_hh (:658-764) and the 222_ph
 // recoupling sum over J' of {6j} Z(J').  Thread t takes element w0 + t of the
-// work order `heads` while below w1.  LR != nullptr: the 122 sums read the
-// packed pairs (k_lr_pack).  PRE: the 122 part is already in RES
+// work order `heads` while below w1.  PRE: the 122 part is already in RES
 // (k_asm2_122).  has220 (the allocation-free path, w0 = 0): each CTA leaves
 // its commutator_220 partial in e0p for k_energy.
-template <bool PACKED, bool PRE>
+template <bool PRE>
 __global__ void __launch_bounds__(ASM2_THREADS) k_assemble_2body(DevTables T, const double *__restrict__ L, int hL,
                                                                  const double *__restrict__ R, int hR,
                                                                  const double *__restrict__ W1,
                                                                  const double *__restrict__ W2,
                                                                  const double *__restrict__ Z, double *RES, int hRES,
                                                                  const Asm2Head *__restrict__ heads, long w0, long w1,
-                                                                 const double2 *__restrict__ LR, int has220,
-                                                                 double *e0p) {
+                                                                 int has220, double *e0p) {
   __shared__ double sh220[ASM2_THREADS / 32];
   const long w = w0 + (long)blockIdx.x * blockDim.x + threadIdx.x;
   double e220 = 0.0;  // this element's commutator_220 term (pphh arrays only)
@@ -468,7 +430,7 @@ __global__ void __launch_bounds__(ASM2_THREADS) k_assemble_2body(DevTables T, co
     if (PRE) {
       t = RES[e];
     } else {
-      t = PACKED ? sum122_lr<1>(tm, meta & 31, L, nL, R, nR, LR) : sum122<1>(tm, meta & 31, L, nL, R, nR);
+      t = sum122<1>(tm, meta & 31, L, nL, R, nR);
       // / sqrt(1 + delta_ab) / sqrt(1 + delta_cd)
       if (nd) t = t * (nd == 1 ? 0.7071067811865476 : 0.5);
       if (diag) t = dflip(t, nres);
@@ -787,36 +749,23 @@ int launch_asm2_range(imsrg_basis *b, const double *L, int hL, const double *R, 
                       long w0, long w1, bool by_range) {
   const long n = w1 - w0;
   if (n > 0) {
-    k_assemble_2body<true, true><<<(unsigned)((n + ASM2_THREADS - 1) / ASM2_THREADS), ASM2_THREADS, 0, b->stream>>>(
+    k_assemble_2body<true><<<(unsigned)((n + ASM2_THREADS - 1) / ASM2_THREADS), ASM2_THREADS, 0, b->stream>>>(
         b->T, L, hL, R, hR, b->w1, b->w2, b->zph, RES, hRES, by_range ? b->T.asm2_head_out : b->T.asm2_head, w0,
-        w1, b->lr, 0, nullptr);
+        w1, 0, nullptr);
     b->launches++;
   }
   return cuda_status(cudaGetLastError());
 }
 
 int launch_asm2_122(imsrg_basis *b, const double *L, int hL, const double *R, int hR, double *RES, int hRES,
-                    bool packed, cudaStream_t st) {
+                    cudaStream_t st) {
   if (b->T.n_pre_warps == 0) return IMSRG_OK;
   ProfScope ps(b, IMSRG_KERNEL_ASSEMBLE_2BODY, st);
   const unsigned grid = (unsigned)(((long)b->T.n_pre_warps * 32 + ASM2_THREADS - 1) / ASM2_THREADS);
-  if (packed)
-    k_asm2_122<true><<<grid, ASM2_THREADS, 0, st>>>(b->T, L, hL, R, hR, hRES, b->lr, RES);
-  else
-    k_asm2_122<false><<<grid, ASM2_THREADS, 0, st>>>(b->T, L, hL, R, hR, hRES, nullptr, RES);
+  k_asm2_122<<<grid, ASM2_THREADS, 0, st>>>(b->T, L, hL, R, hR, hRES, RES);
   b->launches++;
   return cuda_status(cudaGetLastError());
 }
-
-int launch_lr_pack(imsrg_basis *b, const double *L, const double *R, cudaStream_t st) {
-  const long n = b->nfull - b->off_2b;
-  if (n <= 0) return IMSRG_OK;
-  ProfScope ps(b, IMSRG_KERNEL_ASSEMBLE_2BODY, st);
-  k_lr_pack<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(b->T, L, R, b->lr, b->off_2b, b->nfull);
-  b->launches++;
-  return cuda_status(cudaGetLastError());
-}
-
 
 int launch_e0(imsrg_basis *b, const double *L, int hL, const double *R, int hR, double *RES, cudaStream_t st) {
   ProfScope ps(b, IMSRG_KERNEL_ASSEMBLE_1BODY, st);
@@ -870,8 +819,8 @@ int launch_commutator_fp64_ws(imsrg_basis *b, const Workspace &ws, const double 
   const long n2 = b->T.n_asm2;
   if (n2 > 0) {
     const int has220 = with_e0 && hL * hR == -1;
-    k_assemble_2body<false, false><<<(unsigned)((n2 + ASM2_THREADS - 1) / ASM2_THREADS), ASM2_THREADS, 0, st>>>(
-        b->T, L, hL, R, hR, ws.w1, ws.w2, ws.zph, RES, hRES, b->T.asm2_head, 0, n2, nullptr, has220, ws.e0p);
+    k_assemble_2body<false><<<(unsigned)((n2 + ASM2_THREADS - 1) / ASM2_THREADS), ASM2_THREADS, 0, st>>>(
+        b->T, L, hL, R, hR, ws.w1, ws.w2, ws.zph, RES, hRES, b->T.asm2_head, 0, n2, has220, ws.e0p);
     b->launches++;
   }
   const int grid1 = b->T.n_asm1_heavy + (b->T.n_asm1_light + 3) / 4;
@@ -890,7 +839,7 @@ int launch_commutator_fp64_ws(imsrg_basis *b, const Workspace &ws, const double 
 int preload_commutator_fp64_ws() {
   cudaFuncAttributes a;
   const void *fns[] = {(const void *)k_cc_forward<3>, (const void *)k_gemm_fp64<false>, (const void *)k_ph_inputs,
-                       (const void *)k_assemble_2body<false, false>, (const void *)k_assemble_1body, (const void *)k_energy};
+                       (const void *)k_assemble_2body<false>, (const void *)k_assemble_1body, (const void *)k_energy};
   for (const void *f : fns) {
     cudaError_t e = cudaFuncGetAttributes(&a, f);
     if (e != cudaSuccess) return cuda_status(e);
