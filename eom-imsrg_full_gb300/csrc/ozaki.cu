@@ -16,31 +16,29 @@
 //      tcgen05 K-major canonical layout (8 x 16-byte core matrices, no
 //      swizzle), once with the second index contiguous (R image) and once with
 //      the first (C image), so every transposition of every use is K-major.
-//   3. k_oz_mma: persistent kernel, one 128 x 64 output tile at a time.  A
-//      producer thread streams the six A digit planes and fifteen B planes
-//      (d_1..d_6, 2^7 d_1..d_5, 2^14 d_1..d_4) of each K = 16 step into
-//      shared memory with two TMA tensor loads (3-D boxes: 256-byte core
-//      matrix rows x row groups x planes, one per operand; one request per
-//      plane measured 4.8 us slower per commutator at 12 instead of 21
-//      requests, whatever the bytes); one thread issues the 21
-//      tcgen05.mma products d_s x d_t with s + t <= 7 (negating A for terms
-//      with coefficient -1) into four FP32 accumulators in TMEM: one per
-//      level l = s + t = 2, 3, 4 and one "tail" that sums levels 5, 6, 7 in
-//      units of level 7 (the pre-scaled B planes supply 128^(7 - l)).  The
-//      accumulators are double-buffered (2 x 4 x 64 = 512 columns) so the
-//      sixteen epilogue warps read one tile (tcgen05.ld), combine it in int64
-//      and write FP64 while the next tile's products run.  Each CTA takes a
-//      host-built list of (problem, tile) slots, longest first under a cost
-//      model that an autotuner picks by timing the kernel when the plan is
-//      built.
+//   3. k_oz_mma: persistent kernel, one 128 x TN output tile at a time.  A
+//      producer thread streams the S A digit planes and S B planes of each
+//      K = 16 step into shared memory with two TMA tensor loads (3-D boxes:
+//      256-byte core matrix rows x row groups x planes, one per operand; one
+//      request per plane measured 4.8 us slower per commutator at 12 instead
+//      of 21 requests, whatever the bytes); one thread issues, per A plane
+//      s, ONE tcgen05.mma of d_s against the B planes d_1 .. d_(S+1-s) side
+//      by side (negating A for terms with coefficient -1) into the FP32
+//      accumulators of levels l = s + t = s + 1 .. S + 1, side by side in
+//      TMEM: S MMAs per K step.  The accumulators are double-buffered (two
+//      sets of S x TN columns) so the epilogue warps read one tile
+//      (tcgen05.ld), combine its levels in int64 and write FP64 while the
+//      next tile's products run.  Each CTA takes a host-built list of
+//      (problem, tile) slots, longest first under a cost model that an
+//      autotuner picks by timing the kernel when the plan is built.
 //
 // Exactness: the level sums of levels 2..4 are bounded by 5 * 2^12 per
 // product and term, so those accumulators hold exact integers below 2^24
-// while nterms K 5 2^12 < 2^24 (checked per problem when the plan is built).
-// The tail is rounded to FP32 (relative 2^-24 of a quantity 2^-14 below the
-// leading level).  The result differs from the exact product by the dropped
-// levels (s + t >= 8), the digit rounding and the tail rounding: about
-// 2^-42 K max|A| max|B|.
+// while nterms K 5 2^12 < 2^24 (a longer contraction runs in chunks whose
+// int64 sums the epilogue adds).  The lower levels may round in FP32 there
+// (relative 2^-24 of a quantity 2^-14 below the leading level).  The result
+// differs from the exact product by the dropped levels (s + t > S + 1) and
+// the digit rounding: about 2^-(7S) K max|A| max|B|.
 //
 // Every mbarrier wait is bounded (about 2 s of %globaltimer); a timeout sets
 // an error flag that the host reports as IMSRG_ERR_TIMEOUT.
@@ -57,34 +55,42 @@ namespace imsrg {
 
 namespace {
 
-// S digits (slices) per operand, S = 6 (default), 5 or 4.  Levels l = s + t
-// up to S + 1 are kept; levels 2, 3, 4 have exact accumulators and the levels
-// 5..S+1 share an FP32 tail accumulator in units of level S + 1, with B planes
-// pre-scaled by 2^(7 j), j = S + 1 - l: d_1..d_S (j = 0), 2^7 d_1..d_{S-1}
-// (j = 1, S >= 5) and 2^14 d_1..d_4 (j = 2, S = 6).
+// S digits (slices) per operand, S = 6, 5 or 4.  Levels l = s + t up to
+// S + 1 are kept, each in its own FP32 accumulator: a tile's S accumulators
+// lie side by side in TMEM (level l at column (l - 2) x TN), as do the S B
+// planes of a stage in shared memory, so the products of A plane s with B
+// planes 1 .. S + 1 - s are ONE tcgen05.mma of width (S + 1 - s) x TN into
+// the accumulators of levels s + 1 .. S + 1: S MMAs per K step.  (Fewer,
+// wider MMAs: the tensor pipe pays a large fixed cost per instruction at
+// these shapes.)  The tile width TN(S) keeps S x TN <= 256 (the widest MMA)
+// with every level's block on a 32-column boundary: 64 for four digits, 32
+// for five and six.
 constexpr int OZ_SMAX = 6;
-constexpr int OZ_NACC = 4;                   // accumulators: levels 2, 3, 4 exact + FP32 tail
-__host__ __device__ constexpr int oz_bplanes(int S) { return S == 6 ? 15 : S == 5 ? 9 : 4; }
-__host__ __device__ constexpr int oz_plane_off(int S, int j) { return j == 0 ? 0 : j == 1 ? S : 2 * S - 1; }
-constexpr int TM = 128, TN = 64, TK = 16;
-// Largest chunk of a tile's K steps whose FP32 level sums stay exact:
-// steps x TK x 5 x 2^12 < 2^24.
+constexpr int TM = 128, TK = 16;
+__host__ __device__ constexpr int oz_tn(int S) { return S <= 4 ? 64 : 32; }
+// Largest chunk of a tile's K steps whose FP32 level sums stay exact for
+// levels 2..4 (at most 5 x 2^12 per product term and K): steps x TK x 5 x
+// 2^12 < 2^24; the lower levels may round there, below the truncation.
 constexpr int kOzChunkSteps = (16777216 - 1) / (TK * 5 * 4096);
 static_assert(kOzChunkSteps * TK * 5 * 4096 < 16777216, "chunk bound");
-constexpr int STAGES = 4;
+constexpr int STAGES = 6;
 // Lines (8 elements each) per slicing CTA: small CTAs spread the ~100,000
 // lines of a part evenly over the SMs (emax=6: with 256, the SMs were busy
 // for 47% of the L slicing; 128 took the commutator from 159.6 to 156.5 us,
 // 64 gave 159.5).
 constexpr int SLICE_THREADS = 128;
 constexpr int A_SLICE_BYTES = TM * TK * 2;   // 4096
-constexpr int B_SLICE_BYTES = TN * TK * 2;   // 2048
-__host__ __device__ constexpr int oz_stage_bytes(int S) { return S * A_SLICE_BYTES + oz_bplanes(S) * B_SLICE_BYTES; }
+__host__ __device__ constexpr int oz_b_slice_bytes(int S) { return oz_tn(S) * TK * 2; }
+__host__ __device__ constexpr int oz_stage_bytes(int S) { return S * (A_SLICE_BYTES + oz_b_slice_bytes(S)); }
 __host__ __device__ constexpr int oz_mma_smem(int S) { return STAGES * oz_stage_bytes(S) + 1024 + 256; }
 constexpr int TMEM_COLS = 512;
-constexpr int EPI_WARPS = 16;                // one per (TMEM lane quadrant, 16-column chunk)
-constexpr int OZ_THREADS = 32 * (2 + EPI_WARPS);  // warp 0 producer, 1 MMA, 2-17 epilogue
-constexpr int ACC_BUF_COLS = OZ_NACC * TN;   // two accumulator sets fill the 512 columns
+constexpr int ACC_BUF_COLS = 256;  // accumulator set b (double-buffered) starts at column 256 b
+// epilogue warps: one per (TMEM lane quadrant, 16-column chunk of the tile)
+__host__ __device__ constexpr int oz_epi_warps(int S) { return 4 * (oz_tn(S) / 16); }
+// warp 0 producer, 1 MMA issuer, then the epilogue warps
+__host__ __device__ constexpr int oz_threads(int S) { return 32 * (2 + oz_epi_warps(S)); }
+static_assert(OZ_SMAX * 32 <= ACC_BUF_COLS && 4 * 64 <= ACC_BUF_COLS, "level accumulators of a set");
+static_assert(oz_mma_smem(OZ_SMAX) <= 227 * 1024, "stages");
 constexpr unsigned long long WAIT_NS = 2000000000ull;
 
 struct OzMatrix {
@@ -96,7 +102,7 @@ struct OzMatrix {
   long img_c;      // byte offset of the C image (rows n2, K = n1), -1 when no problem reads it
   int rg_r, rg_c;  // row groups (of 8 rows) of each image
   long plane_r, plane_c;  // bytes per digit plane
-  int np_r, np_c;         // digit planes stored: S (A role only) or oz_bplanes(S) (B role: with the scaled tail planes)
+  int np_r, np_c;         // digit planes stored (S)
   int line_r0, line_c0;   // first line of this matrix in the R / C slicing grids
 };
 
@@ -277,12 +283,15 @@ __device__ __forceinline__ void tmem_ld16(uint32_t taddr, uint32_t *r) {
 
 __device__ __forceinline__ void tmem_ld_wait() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
 
-// The tail accumulator rounded to an integer.  Below 2^31 in magnitude (always
-// at five digits or fewer) the 32-bit conversion rounds exactly as the 64-bit
-// one, and it runs on the conversion pipe rather than the FP64 pipe, which the
-// 64-bit conversion of every output kept busy for a third of the kernel.
-__device__ __forceinline__ long long tail_to_ll(float x) {
-  return fabsf(x) < 2147483648.0f ? (long long)__float2int_rn(x) : __float2ll_rn(x);
+// A tile element's level sums (integer-valued FP32 accumulators, below 2^31)
+// combined exactly in int64, in units of level S + 1 (32-bit conversions: the
+// conversion pipe, where a 64-bit one would take the FP64 pipe).
+template <int S>
+__device__ __forceinline__ long long oz_level_sum(const uint32_t (&acc)[S][16], int c) {
+  long long v = 0;
+#pragma unroll
+  for (int l = 0; l < S; l++) v += (long long)__float2int_rn(__uint_as_float(acc[l][c])) << (7 * (S - 1 - l));
+  return v;
 }
 
 // ---------------------------------------------------------------------------
@@ -405,7 +414,6 @@ __global__ void __launch_bounds__(SLICE_THREADS) k_oz_slice(const OzMatrix *__re
     off = m.img_r + ((long)((cg >> 1) * m.rg_r + (r >> 3)) * 2 + (cg & 1)) * 128 + (r & 7) * 16;
     plane = m.plane_r;
   }
-  const int nplanes = cimg ? m.np_c : m.np_r;
   uint32_t h[8][S];  // BF16 bits of each digit
 #pragma unroll
   for (int i = 0; i < 8; i++) {
@@ -414,21 +422,12 @@ __global__ void __launch_bounds__(SLICE_THREADS) k_oz_slice(const OzMatrix *__re
 #pragma unroll
     for (int s = 0; s < S; s++) h[i][s] = tab[d[s] + 128];
   }
-  // plane k: digit s = k (k < S), 2^7 d_{k-S} (S <= k < 2S - 1), 2^14
-  // d_{k-2S+1} (k >= 2S - 1): the scaled planes add 7 or 14 to the BF16
-  // exponent of every non-zero digit, all exact
-  constexpr int P1 = oz_plane_off(S, 1), P2 = oz_plane_off(S, 2);
+  // plane s: digit s of the 8 elements (16 bytes)
 #pragma unroll
-  for (int k = 0; k < oz_bplanes(S); k++) {
-    if (k >= nplanes) break;
-    const int s = k < P1 ? k : k < P2 ? k - P1 : k - P2;
-    const uint32_t add = k < P1 ? 0u : k < P2 ? (7u << 7) : (14u << 7);
+  for (int k = 0; k < S; k++) {
     uint32_t w4[4];
 #pragma unroll
-    for (int i = 0; i < 8; i += 2) {
-      const uint32_t a0 = h[i][s], a1 = h[i + 1][s];
-      w4[i >> 1] = (a0 ? a0 + add : 0u) | ((a1 ? a1 + add : 0u) << 16);
-    }
+    for (int i = 0; i < 8; i += 2) w4[i >> 1] = h[i][k] | (h[i + 1][k] << 16);
     *reinterpret_cast<uint4 *>(img + off + k * plane) = make_uint4(w4[0], w4[1], w4[2], w4[3]);
   }
 }
@@ -440,7 +439,7 @@ __global__ void __launch_bounds__(SLICE_THREADS) k_oz_slice(const OzMatrix *__re
 // CH: the plan has contractions in several chunks (see OzProb); without any,
 // the chunk bookkeeping folds away at compile time.
 template <int S, bool CH>
-__global__ void __launch_bounds__(OZ_THREADS, 1) k_oz_mma(const OzProb *__restrict__ probs, int nprobs,
+__global__ void __launch_bounds__(oz_threads(S), 1) k_oz_mma(const OzProb *__restrict__ probs, int nprobs,
                                                           const int2 *__restrict__ sched,
                                                           const int *__restrict__ sched_off,
                                                           const int *__restrict__ exps, int hL, int hR, int *err,
@@ -448,7 +447,7 @@ __global__ void __launch_bounds__(OZ_THREADS, 1) k_oz_mma(const OzProb *__restri
                                                           const int *__restrict__ act) {
   extern __shared__ __align__(1024) uint8_t smem_raw[];
   uint8_t *smem = (uint8_t *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
-  constexpr int STAGE_BYTES = oz_stage_bytes(S), LMAX = S + 1;
+  constexpr int STAGE_BYTES = oz_stage_bytes(S), LMAX = S + 1, TN = oz_tn(S);
   uint64_t *full = (uint64_t *)(smem + STAGES * STAGE_BYTES);
   uint64_t *empty = full + STAGES;
   uint64_t *acc_full = empty + STAGES;   // [2]
@@ -466,7 +465,7 @@ __global__ void __launch_bounds__(OZ_THREADS, 1) k_oz_mma(const OzProb *__restri
     }
     for (int b = 0; b < 2; b++) {
       mbar_init(&acc_full[b], 1);
-      mbar_init(&acc_empty[b], EPI_WARPS);
+      mbar_init(&acc_empty[b], oz_epi_warps(S));
     }
     *abort_flag = 0;
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
@@ -539,8 +538,9 @@ __global__ void __launch_bounds__(OZ_THREADS, 1) k_oz_mma(const OzProb *__restri
         for (int it = 0; it < P.nterms && !*abort_flag; it++) {
           const OzTerm &T = P.t[it];
           int neg = T.neg ^ (T.use_hl & (hL < 0)) ^ (T.use_hr & (hR < 0));
-          const uint32_t idesc = idesc_bf16(TM, TN, neg);
-          const uint32_t idesc2 = idesc_bf16(TM, 2 * TN, neg), idesc3 = idesc_bf16(TM, 3 * TN, neg);
+          uint32_t idesc[S];  // A plane s: width (S - s) TN
+#pragma unroll
+          for (int s = 0; s < S; s++) idesc[s] = idesc_bf16(TM, (S - s) * TN, neg);
           for (int kk = 0; kk < P.ksteps; kk++) {
             if (left == 0) {  // a chunk starts: take the next accumulator set
               const int buf = nt & 1;
@@ -565,26 +565,14 @@ __global__ void __launch_bounds__(OZ_THREADS, 1) k_oz_mma(const OzProb *__restri
             // descriptor start-address fields advance in 16-byte units
             const uint64_t da = desc0 + (uint64_t)((stage * STAGE_BYTES) >> 4);
             const uint64_t db = da + (uint64_t)((S * A_SLICE_BYTES) >> 4);
+            // A plane s (0-based) times B planes 0 .. S - 1 - s (side by side
+            // in the stage) is one MMA into the accumulators of levels s + 2
+            // .. S + 1 (side by side in TMEM).  The first K step of a chunk
+            // overwrites: plane 0's MMA covers every accumulator.
 #pragma unroll
-            for (int s = 0; s < S; s++) {
-              // level l = s + u + 2 (digits are 1-based).  Levels 2..4 have
-              // their own accumulators, side by side in TMEM, and B planes
-              // u = 0, 1, 2 lie side by side in the stage: the exact products
-              // of A plane s are one MMA of width (3 - s) x 64 into
-              // accumulators s..2 (s <= 2).  Levels 5..7 share the tail
-              // accumulator, with B pre-scaled by 2^(7 (S + 1 - l)).  The first
-              // product into every accumulator of a tile overwrites it.
-              if (s <= 2)
-                mma_bf16(dbase + (uint32_t)(s * TN), da + (uint64_t)(s * (A_SLICE_BYTES >> 4)), db,
-                         s == 0 ? idesc3 : s == 1 ? idesc2 : idesc, (first && s == 0) ? 0 : 1);
-#pragma unroll
-              for (int u = s <= 2 ? 3 - s : 0; u < S - s; u++) {
-                const int lvl = s + u + 2;
-                const int bp = oz_plane_off(S, LMAX - lvl) + u;
-                mma_bf16(dbase + (uint32_t)(3 * TN), da + (uint64_t)(s * (A_SLICE_BYTES >> 4)),
-                         db + (uint64_t)(bp * (B_SLICE_BYTES >> 4)), idesc, (first && s == 0 && u == 3) ? 0 : 1);
-              }
-            }
+            for (int s = 0; s < S; s++)
+              mma_bf16(dbase + (uint32_t)(s * TN), da + (uint64_t)(s * (A_SLICE_BYTES >> 4)), db, idesc[s],
+                       (first && s == 0) ? 0 : 1);
             first = false;
             mma_commit(&empty[stage]);
             if (++stage == STAGES) {
@@ -600,7 +588,7 @@ __global__ void __launch_bounds__(OZ_THREADS, 1) k_oz_mma(const OzProb *__restri
       }
     }
   } else {
-    // epilogue warps 2..17: TMEM lane quadrant = warp % 4 (the lanes a warp
+    // epilogue warps 2..: TMEM lane quadrant = warp % 4 (the lanes a warp
     // may read), 16-column chunk = (warp - 2) / 4
     const int quad = warp & 3, chunk = (warp - 2) >> 2;
     const int row = quad * 32 + lane;
@@ -642,10 +630,10 @@ __global__ void __launch_bounds__(OZ_THREADS, 1) k_oz_mma(const OzProb *__restri
           break;
         }
         tc_fence_after();
-        uint32_t acc[OZ_NACC][16];
+        uint32_t acc[S][16];
         if (live) {
 #pragma unroll
-          for (int l = 0; l < OZ_NACC; l++)
+          for (int l = 0; l < S; l++)
             tmem_ld16(tmem + ((uint32_t)(quad * 32) << 16) + (uint32_t)(buf * ACC_BUF_COLS + l * TN + 16 * chunk),
                       acc[l]);
         }
@@ -655,14 +643,10 @@ __global__ void __launch_bounds__(OZ_THREADS, 1) k_oz_mma(const OzProb *__restri
         __syncwarp();
         if (lane == 0) mbar_arrive(&acc_empty[buf]);
         if (!live) continue;
-        // exact integer levels 2..4 and the rounded tail, in units of level
-        // S + 1 (hardware conversions: measured faster here than assembling
-        // the double from integer bit operations)
-#define OZ_LEVEL_SUM(c)                                                                   \
-  (((long long)__float2int_rn(__uint_as_float(acc[0][c])) << (7 * (LMAX - 2))) +         \
-   ((long long)__float2int_rn(__uint_as_float(acc[1][c])) << (7 * (LMAX - 3))) +         \
-   ((long long)__float2int_rn(__uint_as_float(acc[2][c])) << (7 * (LMAX - 4))) +         \
-   tail_to_ll(__uint_as_float(acc[3][c])))
+        // the level sums in units of level S + 1 (hardware conversions:
+        // measured faster here than assembling the double from integer bit
+        // operations)
+#define OZ_LEVEL_SUM(c) oz_level_sum<S>(acc, c)
         if (nch == 1 && !raw) {
           const int k = (exps[gA] - 1022) + (exps[gB] - 1022) - 7 * LMAX;  // result = v * 2^k
 #pragma unroll
@@ -728,7 +712,7 @@ void launch_mma(int S, bool chunked, int grid, cudaStream_t st, const OzProb *pr
                 const int *sched_off, const int *exps, int hL, int hR, int *err, const CUtensorMap *maps,
                 const int *act = nullptr) {
 #define OZ_LAUNCH(SS, CC)                                                                                    \
-  k_oz_mma<SS, CC><<<grid, OZ_THREADS, oz_mma_smem(SS), st>>>(probs, nprobs, sched, sched_off, exps, hL, hR, err, \
+  k_oz_mma<SS, CC><<<grid, oz_threads(SS), oz_mma_smem(SS), st>>>(probs, nprobs, sched, sched_off, exps, hL, hR, err, \
                                                               maps, act)
   if (S == 4) {
     if (chunked) OZ_LAUNCH(4, true);
@@ -917,7 +901,7 @@ int ozaki_prepare(imsrg_basis *b) {
     if (role_r[i]) {
       m.rg_r = (m.n1 + 7) / 8;
       m.plane_r = (long)m.rg_r * ((m.n2 + 15) / 16) * 256;
-      m.np_r = b_role_r[i] ? oz_bplanes(pl->S) : pl->S;
+      m.np_r = pl->S;
       m.img_r = imgb[m.src];
       imgb[m.src] += m.np_r * m.plane_r;
       lines_r += ((m.n2 + 7) / 8) * m.n1;
@@ -925,7 +909,7 @@ int ozaki_prepare(imsrg_basis *b) {
     if (role_c[i]) {
       m.rg_c = (m.n2 + 7) / 8;
       m.plane_c = (long)m.rg_c * ((m.n1 + 15) / 16) * 256;
-      m.np_c = b_role_c[i] ? oz_bplanes(pl->S) : pl->S;
+      m.np_c = pl->S;
       m.img_c = imgb[m.src];
       imgb[m.src] += m.np_c * m.plane_c;
       lines_c += ((m.n1 + 7) / 8) * m.n2;
@@ -995,12 +979,12 @@ int ozaki_prepare(imsrg_basis *b) {
       *idx = it->second;
       return IMSRG_OK;
     }
-    const cuuint32_t box_planes = brole ? oz_bplanes(pl->S) : pl->S;
+    const cuuint32_t box_planes = pl->S;
     if (plane <= 0 || plane % 256 || (long)np < (long)box_planes) return IMSRG_ERR_INVALID;
     CUtensorMap m;
     const cuuint64_t gdim[3] = {32, (cuuint64_t)(plane / 256), (cuuint64_t)np};
     const cuuint64_t gstride[2] = {256, (cuuint64_t)plane};
-    const cuuint32_t box[3] = {32, (cuuint32_t)(brole ? TN / 8 : TM / 8), box_planes};
+    const cuuint32_t box[3] = {32, (cuuint32_t)(brole ? oz_tn(pl->S) / 8 : TM / 8), box_planes};
     const cuuint32_t estride[3] = {1, 1, 1};
     if (encode(&m, CU_TENSOR_MAP_DATA_TYPE_UINT64, 3, (void *)img, gdim, gstride, box, estride,
                CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
@@ -1051,8 +1035,8 @@ int ozaki_prepare(imsrg_basis *b) {
       o.use_hr = t.use_hr;
     }
     // exactness bound of the FP32 level accumulators (levels 2..4 are exact
-    // integers while their sums stay below 2^24; each product adds at most
-    // 5 x 2^12 per element): a chunk holds at most kOzChunkSteps steps of
+    // integers while their sums stay below 2^24; each of their products adds
+    // at most 5 x 2^12 per element): a chunk holds at most kOzChunkSteps steps of
     // TK, and longer contractions run in several chunks
     {
       const int steps = p.nterms * p.ksteps;
@@ -1061,6 +1045,7 @@ int ozaki_prepare(imsrg_basis *b) {
       p.nchunks = steps > 0 ? (steps + p.kchunk - 1) / p.kchunk : 0;
       if (p.nchunks > 1) pl->chunked = true;
     }
+    const int TN = oz_tn(pl->S);
     p.tiles_m = (p.M + TM - 1) / TM;
     p.tiles = p.tiles_m * ((p.N + TN - 1) / TN);
     p.tile0 = tiles;
