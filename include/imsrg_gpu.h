@@ -168,12 +168,16 @@ int imsrg_gpu_commutator_host(imsrg_basis_t *b, const double *L, int herm_L, con
 /* The same on host operands in the packed (vectorize) layout of
  * basic_IMSRG.f90:3794-3918 (neq doubles each: only the independent
  * elements, ~57 % of the flat layout at emax = 6), the form the reference's
- * ODE solver and checkpoints hold operators in: L and R are copied in and
- * unpacked on the device (R first, its unpacking and its half of the work
- * beside L's copy), RES is packed on the device and copied back.  Square
- * arrays' lower triangles come from herm x the upper ones (repackage).  RES
- * must not overlap L or R.  From page-locked buffers the sequence replays as
- * one CUDA graph. */
+ * ODE solver and checkpoints hold operators in.  Page-locked arrays the
+ * device can address (cudaHostAlloc, or cudaHostRegister with mapping) are
+ * read by the device's unpack kernels and the result is written by its pack
+ * kernel in place, over the host link, with no staging copies (R's
+ * unpacking and its half of the work run beside L's); other arrays are
+ * copied in, unpacked, packed and copied back.  Square arrays' lower
+ * triangles come from herm x the upper ones (repackage).  RES must not
+ * overlap L or R, and none of the three may be touched by the caller until
+ * the call returns.  From page-locked buffers the sequence replays as one
+ * CUDA graph. */
 int imsrg_gpu_commutator_host_packed(imsrg_basis_t *b, const double *L, int herm_L, const double *R, int herm_R,
                                      double *RES, int precision, int with_e0);
 
