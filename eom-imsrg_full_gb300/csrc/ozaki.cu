@@ -138,12 +138,17 @@ struct OzProb {
 };
 
 // Cost models of the CTA schedule tried by the autotuner (weights of K steps,
-// of the epilogue's live outputs, and a per-tile constant).
+// of the epilogue's live outputs in 64ths of a tile, and a per-tile
+// constant).  Model 1 balances K steps alone; the others charge a full
+// tile's epilogue and each tile's fixed cost between a quarter and four K
+// steps (with the per-level kernel a tile's epilogue costs about one to two
+// K steps of products; weights of 10-40 per 64th, tried before, were 25-50 %
+// slower).
 struct SchedModel {
   int kw, ew, base;
 };
 constexpr int kNumSchedModels = 5;
-constexpr SchedModel kSchedModels[kNumSchedModels] = {{4, 20, 4}, {4, 0, 1}, {4, 10, 2}, {4, 40, 4}, {1, 40, 8}};
+constexpr SchedModel kSchedModels[kNumSchedModels] = {{16, 1, 16}, {4, 0, 1}, {32, 1, 16}, {8, 0, 8}, {64, 1, 16}};
 
 struct OzPlan {
   int S = OZ_SMAX;  // digits per operand
