@@ -1391,7 +1391,7 @@ int imsrg_gpu_split_schedule(imsrg_basis_t *b, int *choice, int *ncand, double *
 }
 
 int imsrg_gpu_split_digits_set(imsrg_basis_t *b, int digits) {
-  if (!b || digits < 4 || digits > 6) return IMSRG_ERR_INVALID;
+  if (!b || digits < 4 || digits > 8) return IMSRG_ERR_INVALID;
   if (b->ozaki) return digits == b->split_digits ? IMSRG_OK : IMSRG_ERR_INVALID;  // plan already built
   b->split_digits = digits;
   return IMSRG_OK;

@@ -310,7 +310,7 @@ struct imsrg_basis {
   long launches = 0;
   // Ozaki split-precision engine state (allocated on first use)
   void *ozaki = nullptr;
-  int split_digits = 6;  // digits per operand of the split engine (4, 5 or 6), fixed once its plan exists
+  int split_digits = 6;  // digits per operand of the split engine (4 to 8), fixed once its plan exists
   int split_chunk_steps = 0;  // K steps per exact accumulator chunk (0: the largest exact one)
   // Reverse-mode (adjoint) workspace (adjoint.cu), allocated on first use
   void *adjoint = nullptr;

@@ -65,14 +65,22 @@ namespace {
 // these shapes.)  The tile width TN(S) keeps S x TN <= 256 (the widest MMA)
 // with every level's block on a 32-column boundary: 64 for four digits, 32
 // for five and six.
-constexpr int OZ_SMAX = 6;
+constexpr int OZ_SMAX = 8;
 constexpr int TM = 128, TK = 16;
 __host__ __device__ constexpr int oz_tn(int S) { return S <= 4 ? 64 : 32; }
+// Seven and eight digits are the FP64-class settings: every level stays an
+// exact integer (chunks of at most (2^24 - 1) / (TK (S + 2) 2^12) K steps:
+// a level sums at most S products of 2^12 plus two of 2^13 with the leading
+// digit), the level sums are combined in two int64 halves (7 (S - 1) + 24
+// bits do not fit one) and converted once, and the WCC products are stored as
+// FP64 like every other output.
+__host__ __device__ constexpr bool oz_fp64_class(int S) { return S >= 7; }
 // Largest chunk of a tile's K steps whose FP32 level sums stay exact for
 // levels 2..4 (at most 5 x 2^12 per product term and K): steps x TK x 5 x
 // 2^12 < 2^24; the lower levels may round there, below the truncation.
 constexpr int kOzChunkSteps = (16777216 - 1) / (TK * 5 * 4096);
 static_assert(kOzChunkSteps * TK * 5 * 4096 < 16777216, "chunk bound");
+// pipeline stages: six, five where six would not fit (eight digits; oz_stages)
 constexpr int STAGES = 6;
 // Lines (8 elements each) per slicing CTA: small CTAs spread the ~100,000
 // lines of a part evenly over the SMs (emax=6: with 256, the SMs were busy
@@ -82,7 +90,12 @@ constexpr int SLICE_THREADS = 128;
 constexpr int A_SLICE_BYTES = TM * TK * 2;   // 4096
 __host__ __device__ constexpr int oz_b_slice_bytes(int S) { return oz_tn(S) * TK * 2; }
 __host__ __device__ constexpr int oz_stage_bytes(int S) { return S * (A_SLICE_BYTES + oz_b_slice_bytes(S)); }
-__host__ __device__ constexpr int oz_mma_smem(int S) { return STAGES * oz_stage_bytes(S) + 1024 + 256; }
+__host__ __device__ constexpr int oz_stages(int S) { return S >= 8 ? 5 : STAGES; }
+__host__ __device__ constexpr int oz_mma_smem(int S) { return oz_stages(S) * oz_stage_bytes(S) + 1024 + 256; }
+// K steps per accumulator chunk (see kOzChunkSteps and oz_fp64_class)
+__host__ __device__ constexpr int oz_chunk_steps(int S) {
+  return oz_fp64_class(S) ? (16777216 - 1) / (TK * (S + 2) * 4096) : kOzChunkSteps;
+}
 constexpr int TMEM_COLS = 512;
 constexpr int ACC_BUF_COLS = 256;  // accumulator set b (double-buffered) starts at column 256 b
 // epilogue warps: one per (TMEM lane quadrant, 16-column chunk of the tile)
@@ -90,7 +103,8 @@ __host__ __device__ constexpr int oz_epi_warps(int S) { return 4 * (oz_tn(S) / 1
 // warp 0 producer, 1 MMA issuer, then the epilogue warps
 __host__ __device__ constexpr int oz_threads(int S) { return 32 * (2 + oz_epi_warps(S)); }
 static_assert(OZ_SMAX * 32 <= ACC_BUF_COLS && 4 * 64 <= ACC_BUF_COLS, "level accumulators of a set");
-static_assert(oz_mma_smem(OZ_SMAX) <= 227 * 1024, "stages");
+static_assert(oz_mma_smem(6) <= 227 * 1024 && oz_mma_smem(7) <= 227 * 1024 && oz_mma_smem(8) <= 227 * 1024,
+              "stages");
 constexpr unsigned long long WAIT_NS = 2000000000ull;
 
 struct OzMatrix {
@@ -299,6 +313,39 @@ __device__ __forceinline__ long long oz_level_sum(const uint32_t (&acc)[S][16], 
   return v;
 }
 
+// The same as one FP64 value, in units of level S + 1: one conversion of the
+// exact int64 sum, or for seven and eight digits the sum's two halves (the
+// levels at least 2^28 apart and the rest, each exact in int64 and below
+// 2^53) converted exactly and added with one rounding.
+template <int S>
+__device__ __forceinline__ double oz_level_value(const uint32_t (&acc)[S][16], int c) {
+  if constexpr (S <= 6) {
+    return (double)oz_level_sum<S>(acc, c);
+  } else {
+    long long hi = 0, lo = 0;
+#pragma unroll
+    for (int l = 0; l < S; l++) {
+      const long long a = (long long)__float2int_rn(__uint_as_float(acc[l][c]));
+      const int sh = 7 * (S - 1 - l);
+      if (sh >= 28) hi += a << (sh - 28);
+      else lo += a << sh;
+    }
+    return fma((double)hi, 268435456.0, (double)lo);
+  }
+}
+
+// d 2^k: k added to the exponent field on the integer pipe while the result
+// stays normal (exactly ldexp's value), else ldexp
+__device__ __forceinline__ double oz_scale(double d, int k) {
+  unsigned long long bits = (unsigned long long)__double_as_longlong(d);
+  const int E = (int)((bits >> 52) & 0x7FF);
+  if (E != 0 && E + k > 0 && E + k < 2047) {
+    bits += (unsigned long long)(long long)k << 52;
+    return __longlong_as_double((long long)bits);
+  }
+  return E != 0 ? ldexp(d, k) : d;
+}
+
 // ---------------------------------------------------------------------------
 // 1. block exponents: max biased exponent of each group (integer atomicMax,
 //    order-independent, so the result is deterministic)
@@ -330,7 +377,8 @@ __global__ void __launch_bounds__(256) k_oz_exponents(const OzChunk *chunks, con
 // ---------------------------------------------------------------------------
 // Digits of x with |x| < 2^e: x = 2^(e-7S) sum_{s} d_s 128^(S-1-s), d_0 first.
 // One 64-bit shift rounds |x| to the 7S-bit integer V; the balanced base-128
-// digits then come from its low 21 bits and the rest on the 32-bit integer pipe.
+// digits then come from its low 21 bits and the rest on the 32-bit integer
+// pipe (S <= 6), or all on the 64-bit one (S = 7, 8: V has up to 56 bits).
 template <int S>
 __device__ __forceinline__ void digits(double x, int e, int *d) {
   const unsigned long long bits = (unsigned long long)__double_as_longlong(x);
@@ -339,8 +387,28 @@ __device__ __forceinline__ void digits(double x, int e, int *d) {
   unsigned long long V = 0;
   if (E != 0) {
     const unsigned long long mant = (bits & ((1ull << 52) - 1)) | (1ull << 52);
-    const int rs = e + 1075 - 7 * S - E;  // V = round(|x| 2^(7S - e)), rs >= 11
-    if (rs <= 63) V = (mant + (1ull << (rs - 1))) >> rs;
+    // V = round(|x| 2^(7S - e)): rs >= 53 - 7S (>= 11 for S <= 6, >= -3 for S = 8)
+    const int rs = e + 1075 - 7 * S - E;
+    if constexpr (S >= 8) {
+      if (rs <= 0) V = mant << (-rs);  // exact: the 53-bit significand fits in 56 bits
+      else if (rs <= 63) V = (mant + (1ull << (rs - 1))) >> rs;
+    } else {
+      if (rs <= 63) V = (mant + (1ull << (rs - 1))) >> rs;
+    }
+  }
+  if constexpr (S >= 7) {
+#pragma unroll
+    for (int s = S - 1; s >= 1; s--) {
+      int u = (int)(V & 127u);
+      V >>= 7;
+      if (u >= 64) {
+        u -= 128;
+        V += 1;
+      }
+      d[s] = neg ? -u : u;
+    }
+    d[0] = neg ? -(int)V : (int)V;
+    return;
   }
   unsigned lo = (unsigned)(V & 0x1FFFFFu), hi = (unsigned)(V >> 21);
 #pragma unroll
@@ -452,7 +520,7 @@ __global__ void __launch_bounds__(oz_threads(S), 1) k_oz_mma(const OzProb *__res
                                                           const int *__restrict__ act) {
   extern __shared__ __align__(1024) uint8_t smem_raw[];
   uint8_t *smem = (uint8_t *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
-  constexpr int STAGE_BYTES = oz_stage_bytes(S), LMAX = S + 1, TN = oz_tn(S);
+  constexpr int STAGE_BYTES = oz_stage_bytes(S), LMAX = S + 1, TN = oz_tn(S), STAGES = oz_stages(S);
   uint64_t *full = (uint64_t *)(smem + STAGES * STAGE_BYTES);
   uint64_t *empty = full + STAGES;
   uint64_t *acc_full = empty + STAGES;   // [2]
@@ -656,19 +724,27 @@ __global__ void __launch_bounds__(oz_threads(S), 1) k_oz_mma(const OzProb *__res
           const int k = (exps[gA] - 1022) + (exps[gB] - 1022) - 7 * LMAX;  // result = v * 2^k
 #pragma unroll
           for (int c = 0; c < 16; c++) {
-            double d = (double)OZ_LEVEL_SUM(c);
-            // scale by 2^k: add k to the exponent field on the integer pipe
-            unsigned long long bits = (unsigned long long)__double_as_longlong(d);
-            const int E = (int)((bits >> 52) & 0x7FF);
-            if (E != 0 && E + k > 0 && E + k < 2047) {
-              bits += (unsigned long long)(long long)k << 52;
-              d = __longlong_as_double((long long)bits);
-            } else if (E != 0) {
-              d = ldexp(d, k);
-            }
+            const double d = oz_scale(oz_level_value<S>(acc, c), k);
             const int n = n0 + c;
             if (row_ok && n < Np) crow[(long)n * ldc] = d;
           }
+          continue;
+        }
+        if constexpr (oz_fp64_class(S)) {
+          // a long contraction at seven or eight digits adds its chunks in
+          // FP64 in the output's own slots, then scales once
+#pragma unroll
+          for (int c = 0; c < 16; c++) {
+            double v = oz_level_value<S>(acc, c);
+            const int n = n0 + c;
+            if (row_ok && n < Np) {
+              if (ch > 0) v += crow[(long)n * ldc];
+              crow[(long)n * ldc] = v;
+            }
+          }
+          if (ch < nch - 1 || !row_ok) continue;
+          const int k = (exps[gA] - 1022) + (exps[gB] - 1022) - 7 * LMAX;
+          for (int c = 0; c < 16 && n0 + c < Np; c++) crow[(long)(n0 + c) * ldc] = oz_scale(crow[(long)(n0 + c) * ldc], k);
           continue;
         }
         // WCC keeps the exact level sum as an integer (the 222_ph recoupling
@@ -686,18 +762,8 @@ __global__ void __launch_bounds__(oz_threads(S), 1) k_oz_mma(const OzProb *__res
         if (raw || ch < nch - 1 || !row_ok) continue;
         // the last chunk of a long FP64 contraction: convert the summed integers
         const int k = (exps[gA] - 1022) + (exps[gB] - 1022) - 7 * LMAX;
-        for (int c = 0; c < 16 && n0 + c < Np; c++) {
-          double d = (double)irow[(long)(n0 + c) * ldc];
-          unsigned long long bits = (unsigned long long)__double_as_longlong(d);
-          const int E = (int)((bits >> 52) & 0x7FF);
-          if (E != 0 && E + k > 0 && E + k < 2047) {
-            bits += (unsigned long long)(long long)k << 52;
-            d = __longlong_as_double((long long)bits);
-          } else if (E != 0) {
-            d = ldexp(d, k);
-          }
-          crow[(long)(n0 + c) * ldc] = d;
-        }
+        for (int c = 0; c < 16 && n0 + c < Np; c++)
+          crow[(long)(n0 + c) * ldc] = oz_scale((double)irow[(long)(n0 + c) * ldc], k);
 #undef OZ_LEVEL_SUM
       }
       if (*abort_flag) break;
@@ -719,15 +785,12 @@ void launch_mma(int S, bool chunked, int grid, cudaStream_t st, const OzProb *pr
 #define OZ_LAUNCH(SS, CC)                                                                                    \
   k_oz_mma<SS, CC><<<grid, oz_threads(SS), oz_mma_smem(SS), st>>>(probs, nprobs, sched, sched_off, exps, hL, hR, err, \
                                                               maps, act)
-  if (S == 4) {
-    if (chunked) OZ_LAUNCH(4, true);
-    else OZ_LAUNCH(4, false);
-  } else if (S == 5) {
-    if (chunked) OZ_LAUNCH(5, true);
-    else OZ_LAUNCH(5, false);
-  } else {
-    if (chunked) OZ_LAUNCH(6, true);
-    else OZ_LAUNCH(6, false);
+  switch (S) {
+    case 4: if (chunked) OZ_LAUNCH(4, true); else OZ_LAUNCH(4, false); break;
+    case 5: if (chunked) OZ_LAUNCH(5, true); else OZ_LAUNCH(5, false); break;
+    case 6: if (chunked) OZ_LAUNCH(6, true); else OZ_LAUNCH(6, false); break;
+    case 7: if (chunked) OZ_LAUNCH(7, true); else OZ_LAUNCH(7, false); break;
+    default: if (chunked) OZ_LAUNCH(8, true); else OZ_LAUNCH(8, false); break;
   }
 #undef OZ_LAUNCH
 }
@@ -824,8 +887,9 @@ int ozaki_prepare(imsrg_basis *b) {
   OzPlan *pl = new OzPlan();
   b->ozaki = pl;
   pl->S = b->split_digits;
-  if (b->split_chunk_steps > 0) pl->chunk_steps = std::min(b->split_chunk_steps, kOzChunkSteps);
-  if (pl->S < 4 || pl->S > 6) return IMSRG_ERR_INVALID;
+  if (pl->S < 4 || pl->S > OZ_SMAX) return IMSRG_ERR_INVALID;
+  pl->chunk_steps = oz_chunk_steps(pl->S);
+  if (b->split_chunk_steps > 0) pl->chunk_steps = std::min(b->split_chunk_steps, oz_chunk_steps(pl->S));
   int dev = b->device, major = 0, nsm = 0;
   IMSRG_CUDA_TRY(cudaDeviceGetAttribute(&major, cudaDevAttrComputeCapabilityMajor, dev));
   IMSRG_CUDA_TRY(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
@@ -1014,7 +1078,7 @@ int ozaki_prepare(imsrg_basis *b) {
     p.nterms = gp.nterms;
     double *dst = gp.c_dst == SRC_W1 ? b->w1 : gp.c_dst == SRC_W2 ? b->w2 : b->wcc;
     p.C = dst + gp.c_off;
-    p.raw = gp.c_dst == SRC_WCC;
+    p.raw = gp.c_dst == SRC_WCC && !oz_fp64_class(pl->S);
     p.ldc = gp.ldc;
     for (int it = 0; it < gp.nterms; it++) {
       const GemmTerm &t = gp.t[it];
@@ -1045,7 +1109,7 @@ int ozaki_prepare(imsrg_basis *b) {
     // TK, and longer contractions run in several chunks
     {
       const int steps = p.nterms * p.ksteps;
-      const int lim = std::min(kOzChunkSteps, std::max(1, pl->chunk_steps));
+      const int lim = std::min(oz_chunk_steps(pl->S), std::max(1, pl->chunk_steps));
       p.kchunk = std::max(1, std::min(steps, lim));
       p.nchunks = steps > 0 ? (steps + p.kchunk - 1) / p.kchunk : 0;
       if (p.nchunks > 1) pl->chunked = true;
@@ -1094,11 +1158,13 @@ int ozaki_prepare(imsrg_basis *b) {
   IMSRG_CUDA_TRY(cudaMemset(pl->d_err, 0, sizeof(int)));
   {
     const int sm = oz_mma_smem(pl->S);
-    const void *fn[2] = {pl->S == 4 ? (const void *)k_oz_mma<4, false>
-                                    : pl->S == 5 ? (const void *)k_oz_mma<5, false> : (const void *)k_oz_mma<6, false>,
-                         pl->S == 4 ? (const void *)k_oz_mma<4, true>
-                                    : pl->S == 5 ? (const void *)k_oz_mma<5, true> : (const void *)k_oz_mma<6, true>};
-    for (const void *f : fn) IMSRG_CUDA_TRY(cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, sm));
+    const void *by_s[5][2] = {{(const void *)k_oz_mma<4, false>, (const void *)k_oz_mma<4, true>},
+                              {(const void *)k_oz_mma<5, false>, (const void *)k_oz_mma<5, true>},
+                              {(const void *)k_oz_mma<6, false>, (const void *)k_oz_mma<6, true>},
+                              {(const void *)k_oz_mma<7, false>, (const void *)k_oz_mma<7, true>},
+                              {(const void *)k_oz_mma<8, false>, (const void *)k_oz_mma<8, true>}};
+    const void *const *fn = by_s[pl->S - 4];
+    for (int v = 0; v < 2; v++) IMSRG_CUDA_TRY(cudaFuncSetAttribute(fn[v], cudaFuncAttributeMaxDynamicSharedMemorySize, sm));
   }
 
   int herr = 0;
@@ -1134,7 +1200,7 @@ int ozaki_slice(imsrg_basis *b, const double *L, const double *R, int part, cuda
   }
   const int nblk = pl->cblocks[part] + pl->rblocks[part];
   if (nblk) {
-    (pl->S == 4 ? k_oz_slice<4> : pl->S == 5 ? k_oz_slice<5> : k_oz_slice<6>)<<<nblk, SLICE_THREADS, 0, st>>>(pl->d_mats, pl->nmats, pl->d_blk_mat + pl->blk_off[part], pl->cblocks[part],
+    (pl->S == 4 ? k_oz_slice<4> : pl->S == 5 ? k_oz_slice<5> : pl->S == 6 ? k_oz_slice<6> : pl->S == 7 ? k_oz_slice<7> : k_oz_slice<8>)<<<nblk, SLICE_THREADS, 0, st>>>(pl->d_mats, pl->nmats, pl->d_blk_mat + pl->blk_off[part], pl->cblocks[part],
                                      pl->linec_lo[part], pl->linec_lo[part + 1], pl->liner_lo[part],
                                      pl->liner_lo[part + 1], L, R, b->lcc, b->rcc, pl->d_exps, pl->img[0],
                                      pl->img[1], pl->img[2], pl->img[3]);
@@ -1183,7 +1249,8 @@ int synchronize_checked(imsrg_basis *b) {
 int ozaki_wcc_scale(imsrg_basis *b, const int **exps, const int2 **ccgroups, int *kshift) {
   OzPlan *pl = plan_of(b);
   if (!pl || !pl->ok) return IMSRG_ERR_INVALID;
-  *exps = pl->d_exps;
+  // FP64-class digit counts store WCC as FP64: the recoupling inputs read it so
+  *exps = oz_fp64_class(pl->S) ? nullptr : pl->d_exps;
   *ccgroups = pl->d_ccgroups;
   *kshift = 7 * (pl->S + 1);
   return IMSRG_OK;

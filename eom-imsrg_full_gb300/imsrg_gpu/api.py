@@ -256,9 +256,10 @@ class Basis:
 
     def set_split_digits(self, digits: int):
         """Digits per operand of the split engine on this basis: 6 (default,
-        21 BF16 products), 5 (15 products) or 4 (10 products); each digit
-        fewer multiplies the truncation bound by 128.  Only before the basis'
-        first split-precision call."""
+        21 BF16 products), 5 (15 products), 4 (10 products), or the
+        FP64-class 7 and 8 (28 and 36 products, every level exact); each
+        digit fewer multiplies the truncation bound by 128.  Only before the
+        basis' first split-precision call."""
         _check(lib().imsrg_gpu_split_digits_set(self._h, int(digits)), "split_digits_set")
 
     def block_dims(self, q):

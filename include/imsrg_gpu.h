@@ -350,15 +350,20 @@ int imsrg_gpu_split_schedule_set(imsrg_basis_t *b, int model);
 /* Digits per operand of IMSRG_PREC_OZAKI on this basis (no reference
  * counterpart): 6 (the default; 21 BF16 products per term, about 2^-42
  * K max|A| max|B| from the exact product), 5 (15 products, about 2^-35
- * K max|A| max|B|) or 4 (10 products, about 2^-28 K max|A| max|B|).  Only before the basis' first split-precision call; later
+ * K max|A| max|B|), 4 (10 products, about 2^-28 K max|A| max|B|), or the
+ * FP64-class counts 7 and 8 (28 and 36 products, about 2^-49 and 2^-56
+ * K max|A| max|B|, every digit level summed exactly, FP64 rounding of the
+ * final sum).  Only before the basis' first split-precision call; later
  * it accepts the current count only (IMSRG_ERR_INVALID otherwise). */
 int imsrg_gpu_split_digits_set(imsrg_basis_t *b, int digits);
 /* Contraction chunking of IMSRG_PREC_OZAKI (no reference counterpart).  A
  * tile's digit products accumulate exactly in FP32 for at most 51 K steps of
- * 16 (steps x 16 x 5 x 2^12 < 2^24); longer contractions (a term count times
- * K above 816, e.g. the pppp blocks from emax = 8 on) run in chunks, each
- * into its own accumulators, whose exact int64 level sums the epilogue adds
- * before converting once.  steps > 0 caps the chunk at fewer steps (testing
+ * 16 (steps x 16 x 5 x 2^12 < 2^24; 28 and 25 steps at seven and eight
+ * digits, where every level stays exact); longer contractions (a term count
+ * times K above 816, e.g. the pppp blocks from emax = 8 on) run in chunks,
+ * each into its own accumulators, whose exact int64 level sums the epilogue
+ * adds before converting once (at seven and eight digits each chunk's FP64
+ * value).  steps > 0 caps the chunk at fewer steps (testing
  * and tuning; the result stays within the same error bound), 0 restores the
  * default.  Only before the basis' first split-precision call, like
  * imsrg_gpu_split_digits_set. */

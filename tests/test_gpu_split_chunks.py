@@ -12,12 +12,14 @@ from conftest import make_case, rel_err
 pytestmark = pytest.mark.gpu
 
 
-@pytest.mark.parametrize("emax,steps", [(4, 2), (6, 5)])
-def test_forced_chunks_match_fp64(gpu_lib, emax, steps):
+@pytest.mark.parametrize("emax,steps,digits", [(4, 2, 5), (6, 5, 5), (4, 2, 8), (6, 3, 7)])
+def test_forced_chunks_match_fp64(gpu_lib, emax, steps, digits):
+    """At seven and eight digits the chunks add in FP64 instead (every
+    level exact within a chunk): the same bound holds, far inside it."""
     from imsrg_gpu.synth import synth_hamiltonian, synth_omega
     bas, lay = make_case(emax)
     B = gpu_lib.Basis.from_dict(bas)
-    B.set_split_digits(5)
+    B.set_split_digits(digits)
     B.set_split_chunk(steps)
     O, H = gpu_lib.Operator(B, -1, synth_omega(lay, 8)), gpu_lib.Operator(B, 1, synth_hamiltonian(lay, 8))
     R64, Roz, Roz2 = gpu_lib.Operator(B, 1), gpu_lib.Operator(B, 1), gpu_lib.Operator(B, 1)
@@ -25,7 +27,7 @@ def test_forced_chunks_match_fp64(gpu_lib, emax, steps):
     gpu_lib.commutator(O, H, Roz, precision="ozaki")
     gpu_lib.commutator(O, H, Roz2, precision="ozaki")
     a, b = Roz.download(), R64.download()
-    assert rel_err(a, b) <= 1e-7
+    assert rel_err(a, b) <= (1e-7 if digits < 7 else 1e-12)
     assert abs(a[0] - b[0]) <= 1e-6
     assert np.array_equal(a, Roz2.download())
 
