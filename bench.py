@@ -452,6 +452,7 @@ def run_gpu(args, world, rank, local):
         line.update(extra)
         if not args.no_flows:
             line["flow"] = flow_emax6(api, orb, lay, args.split_digits)
+            line["fp64_class"] = fp64_class_extra(api, orb, lay, flush)
             line["ode"] = ode_emax6(api, orb, lay)
             line["hartree_fock"] = hf_emax6(api, orb, lay)
             line["batch"] = batch_flows(api, args.batch)
@@ -467,6 +468,47 @@ def run_gpu(args, world, rank, local):
         torch.distributed.barrier()
         torch.distributed.destroy_process_group()
     return 0
+
+
+def fp64_class_extra(api, orb, lay, flush, steps=100):
+    """Eight-digit split precision (every digit level exact: FP64-class
+    accuracy) beside the FP64 path on the benchmark's commutator: each path's
+    commutators/s (CUDA events on the library's stream, the L2 flushed between
+    steps), the eight-digit result's largest element difference from the FP64
+    path, and the emax = 6 flow to s = 50 at eight digits against the FP64
+    oracle flow (flow_emax6)."""
+    import numpy as np
+    import torch
+    from imsrg_gpu.synth import synth_hamiltonian, synth_omega
+    B = api.Basis.from_dict(orb)
+    B.set_split_digits(8)
+    O, H = api.Operator(B, -1, synth_omega(lay, 1)), api.Operator(B, 1, synth_hamiltonian(lay, 1))
+    res = {p: api.Operator(B, 1) for p in ("ozaki", "fp64")}
+    stream = torch.cuda.ExternalStream(B.stream())
+    out = {"split_digits": 8, "steps": steps, "l2": "flushed between timed steps"}
+    for prec in ("ozaki", "fp64"):
+        for _ in range(5):
+            api.commutator(O, H, res[prec], precision=prec)
+        B.synchronize()
+        total = 0.0
+        for _ in range(steps):
+            flush.fill_(1.0)
+            torch.cuda.synchronize()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            api.commutator(O, H, res[prec], precision=prec)
+            e1.record(stream)
+            e1.synchronize()
+            total += e0.elapsed_time(e1) / 1e3
+        out[prec + "_commutators_per_s"] = steps / total
+    a, b = res["ozaki"].download(), res["fp64"].download()
+    out["max_rel_elem_vs_fp64"] = float(np.max(np.abs(a - b)) / np.max(np.abs(b)))
+    out["abs_dE0_vs_fp64_MeV"] = abs(float(a[0] - b[0]))
+    out["speedup_vs_fp64"] = out["ozaki_commutators_per_s"] / out["fp64_commutators_per_s"]
+    f = flow_emax6(api, orb, lay, 8)
+    out["flow"] = {k: f["ozaki"][k] for k in ("steps", "commutators", "seconds", "commutators_per_s",
+                                             "max_abs_dE0_vs_oracle_MeV", "omega_norm_rel_err_vs_oracle")}
+    return out
 
 
 def flow_emax6(api, orb, lay, digits=5):
