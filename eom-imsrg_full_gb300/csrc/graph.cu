@@ -207,9 +207,7 @@ int build_step_graph(imsrg_basis *b, FlowGraph *fg, imsrg_op *HS, imsrg_op *G, i
   // one Magnus term: X1 = [G, X0]; DG += cof X1; |X1|; X0 = X1
   IMSRG_TRY(capture(b, body, {}, [&]() -> int {
     IMSRG_TRY(commutator_dev(b, G->d, G->herm, X0->d, -1, X1->d, -G->herm * -1, precision, 0));
-    IMSRG_TRY(launch_axpby_dev(b, DG->d, 1.0, X1->d, &F->cof, DG->d));
-    IMSRG_TRY(launch_norm(b, X1->d, &F->nrm));
-    IMSRG_CUDA_TRY(cudaMemcpyAsync(X0->d, X1->d, nb, cudaMemcpyDeviceToDevice, b->stream));
+    IMSRG_TRY(launch_series_update(b, DG->d, X1->d, &F->cof, X0->d, &F->nrm));
     k_magnus_next<<<1, 1, 0, b->stream>>>(F, hM);
     return cuda_status(cudaGetLastError());
   }, nullptr));
@@ -225,9 +223,7 @@ int build_step_graph(imsrg_basis *b, FlowGraph *fg, imsrg_op *HS, imsrg_op *G, i
   // one BCH term: X1 = [G, X0] (with E0); HS += X1 / n!; |X1|; X0 = X1
   IMSRG_TRY(capture(b, body, {}, [&]() -> int {
     IMSRG_TRY(commutator_dev(b, G->d, G->herm, X0->d, H0->herm, X1->d, -G->herm * H0->herm, precision, 1));
-    IMSRG_TRY(launch_axpby_dev(b, HS->d, 1.0, X1->d, &F->coef, HS->d));
-    IMSRG_TRY(launch_norm(b, X1->d, &F->nrm));
-    IMSRG_CUDA_TRY(cudaMemcpyAsync(X0->d, X1->d, nb, cudaMemcpyDeviceToDevice, b->stream));
+    IMSRG_TRY(launch_series_update(b, HS->d, X1->d, &F->coef, X0->d, &F->nrm));
     k_bch_next<<<1, 1, 0, b->stream>>>(F, hB);
     return cuda_status(cudaGetLastError());
   }, nullptr));
@@ -547,17 +543,14 @@ int build_batch_graph(BatchFlowGraph *f, imsrg_basis *const *bases, void *oz, cu
     for (int i = 0; i < n; i++) {
       imsrg_basis *b = bases[i];
       FlowDev *F = f->d_state + i;
-      const size_t bytes = b->nfull * sizeof(double);
       cudaGraphNode_t node;
       cudaGraph_t ib;
       IMSRG_TRY(add_if(body, mfr, hb[n + i], &node, &ib));
       IMSRG_TRY(capture(b, ib, {}, [&]() -> int {
         IMSRG_TRY(commutator_launches(b, G[i]->d, -1, X0[i]->d, hX, X1[i]->d, hRES, precision, with_e0, nullptr,
                                       kPhaseBack | kPhaseJoinE0Front));
-        if (magnus) IMSRG_TRY(launch_axpby_dev(b, DG[i]->d, 1.0, X1[i]->d, &F->cof, DG[i]->d));
-        else IMSRG_TRY(launch_axpby_dev(b, HS[i]->d, 1.0, X1[i]->d, &F->coef, HS[i]->d));
-        IMSRG_TRY(launch_norm(b, X1[i]->d, &F->nrm));
-        IMSRG_CUDA_TRY(cudaMemcpyAsync(X0[i]->d, X1[i]->d, bytes, cudaMemcpyDeviceToDevice, b->stream));
+        IMSRG_TRY(launch_series_update(b, magnus ? DG[i]->d : HS[i]->d, X1[i]->d, magnus ? &F->cof : &F->coef,
+                                       X0[i]->d, &F->nrm));
         if (magnus) k_bm_next<<<1, 1, 0, b->stream>>>(F, f->d_go + i);
         else k_bb_next<<<1, 1, 0, b->stream>>>(F, f->d_go + i);
         return cuda_status(cudaGetLastError());

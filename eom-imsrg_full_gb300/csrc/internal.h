@@ -389,6 +389,11 @@ int launch_assemble_1body(imsrg_basis *b, const double *L, int hL, const double 
 int launch_e0(imsrg_basis *b, const double *L, int hL, const double *R, int hR, double *RES, cudaStream_t st);
 int launch_axpby(imsrg_basis *b, const double *A, double ax, const double *B, double bx, double *C);
 int launch_axpby_dev(imsrg_basis *b, const double *A, double ax, const double *B, const double *bx, double *C);
+// S += *coef_dev X1, X0 = X1 (unless X0 is null), *d_norm = mat_frob_norm(X1):
+// one series term's bookkeeping in one pass over X1 (the same values as
+// launch_axpby_dev, a copy and launch_norm)
+int launch_series_update(imsrg_basis *b, double *S, const double *X1, const double *coef_dev, double *X0,
+                         double *d_norm);
 int launch_norm(imsrg_basis *b, const double *op, double *d_out);
 int launch_mbpt2(imsrg_basis *b, const double *H, int herm, double *d_out);
 int launch_white(imsrg_basis *b, const double *H, int hH, double *ETA);

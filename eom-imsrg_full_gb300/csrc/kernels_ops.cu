@@ -17,12 +17,19 @@ namespace {
 
 // C = ax A + bx B; bx_dev, when given, supplies bx from device memory (the
 // graph-captured flow), with the same arithmetic as the scalar form.
+// a ax + b bx with its roundings spelled out, shared by every kernel that
+// updates a series sum, so the host-driven and graph-captured flows agree bit
+// for bit whatever the compiler would contract
+__device__ __forceinline__ double axpby_elem(double a, double ax, double b, double bx) {
+  return __fma_rn(b, bx, __dmul_rn(a, ax));
+}
+
 __global__ void k_axpby(const double *__restrict__ A, double ax, const double *__restrict__ B, double bx,
                         const double *bx_dev, double *__restrict__ C, long n) {
   if (bx_dev) bx = *bx_dev;
   long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
   long stride = (long)gridDim.x * blockDim.x;
-  for (; i < n; i += stride) C[i] = A[i] * ax + B[i] * bx;
+  for (; i < n; i += stride) C[i] = axpby_elem(A[i], ax, B[i], bx);
 }
 
 __device__ double block_sum_ops(double v, double *sh) {
@@ -50,6 +57,33 @@ __global__ void __launch_bounds__(256) k_norm_partial(const double *__restrict__
   for (int i = threadIdx.x; i < c.len; i += blockDim.x) {
     double x = op[c.start + i];
     s = fma(x, x, s);
+  }
+  s = block_sum_ops(s, sh);
+  if (threadIdx.x == 0) partials[blockIdx.x] = s * c.weight;
+}
+
+// One Magnus or BCH series term's bookkeeping in one pass over the new term
+// B: C = A + bx B (the sum), X0 = B (the next term's operand, when X0 is set)
+// and B's mat_frob_norm partials, chunk by chunk in k_norm_partial's order
+// (so k_final_sum gives the same norm bit for bit).  E0 (index 0) lies
+// outside the norm chunks and is updated by one thread.
+__global__ void __launch_bounds__(256) k_series_update(const double *A, const double *__restrict__ B,
+                                                       const double *bx_dev, double *C, double *X0,
+                                                       const NormChunk *chunks, double *partials) {
+  __shared__ double sh[32];
+  const double bx = *bx_dev;
+  const NormChunk c = chunks[blockIdx.x];
+  double s = 0.0;
+  for (int i = threadIdx.x; i < c.len; i += blockDim.x) {
+    const long k = c.start + i;
+    const double x = B[k];
+    C[k] = axpby_elem(A[k], 1.0, x, bx);
+    if (X0) X0[k] = x;
+    s = fma(x, x, s);
+  }
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    C[0] = axpby_elem(A[0], 1.0, B[0], bx);
+    if (X0) X0[0] = B[0];
   }
   s = block_sum_ops(s, sh);
   if (threadIdx.x == 0) partials[blockIdx.x] = s * c.weight;
@@ -375,6 +409,15 @@ int launch_axpby_dev(imsrg_basis *b, const double *A, double ax, const double *B
   ProfScope ps(b, IMSRG_KERNEL_OPS);
   k_axpby<<<grid, 256, 0, b->stream>>>(A, ax, B, 0.0, bx, C, n);
   b->launches++;
+  return cuda_status(cudaGetLastError());
+}
+
+int launch_series_update(imsrg_basis *b, double *S, const double *X1, const double *coef_dev, double *X0,
+                         double *d_norm) {
+  ProfScope ps(b, IMSRG_KERNEL_OPS);
+  k_series_update<<<b->nchunks, 256, 0, b->stream>>>(S, X1, coef_dev, S, X0, b->d_chunks, b->partials);
+  k_final_sum<<<1, 256, 0, b->stream>>>(b->partials, b->nchunks, d_norm, 1);
+  b->launches += 2;
   return cuda_status(cudaGetLastError());
 }
 

@@ -745,25 +745,25 @@ __global__ void __launch_bounds__(oz_threads(S), 1) k_oz_mma(const OzProb *__res
           if (ch < nch - 1 || !row_ok) continue;
           const int k = (exps[gA] - 1022) + (exps[gB] - 1022) - 7 * LMAX;
           for (int c = 0; c < 16 && n0 + c < Np; c++) crow[(long)(n0 + c) * ldc] = oz_scale(crow[(long)(n0 + c) * ldc], k);
-          continue;
-        }
-        // WCC keeps the exact level sum as an integer (the 222_ph recoupling
-        // combines four entries of one block, which share 2^k, before its one
-        // conversion to FP64); a long contraction adds its chunks there
+        } else {
+          // WCC keeps the exact level sum as an integer (the 222_ph recoupling
+          // combines four entries of one block, which share 2^k, before its one
+          // conversion to FP64); a long contraction adds its chunks there
 #pragma unroll
-        for (int c = 0; c < 16; c++) {
-          long long v = OZ_LEVEL_SUM(c);
-          const int n = n0 + c;
-          if (row_ok && n < Np) {
-            if (ch > 0) v += irow[(long)n * ldc];
-            irow[(long)n * ldc] = v;
+          for (int c = 0; c < 16; c++) {
+            long long v = OZ_LEVEL_SUM(c);
+            const int n = n0 + c;
+            if (row_ok && n < Np) {
+              if (ch > 0) v += irow[(long)n * ldc];
+              irow[(long)n * ldc] = v;
+            }
           }
+          if (raw || ch < nch - 1 || !row_ok) continue;
+          // the last chunk of a long FP64 contraction: convert the summed integers
+          const int k = (exps[gA] - 1022) + (exps[gB] - 1022) - 7 * LMAX;
+          for (int c = 0; c < 16 && n0 + c < Np; c++)
+            crow[(long)(n0 + c) * ldc] = oz_scale((double)irow[(long)(n0 + c) * ldc], k);
         }
-        if (raw || ch < nch - 1 || !row_ok) continue;
-        // the last chunk of a long FP64 contraction: convert the summed integers
-        const int k = (exps[gA] - 1022) + (exps[gB] - 1022) - 7 * LMAX;
-        for (int c = 0; c < 16 && n0 + c < Np; c++)
-          crow[(long)(n0 + c) * ldc] = oz_scale((double)irow[(long)(n0 + c) * ldc], k);
 #undef OZ_LEVEL_SUM
       }
       if (*abort_flag) break;
