@@ -120,4 +120,22 @@ __device__ __forceinline__ double warp_sum(double v) {
   return v;
 }
 
+// Sum of v over the CTA in a fixed order (warp shuffles, then the warp totals
+// by the first warp), valid in the first warp; sh holds 32 doubles.
+__device__ __forceinline__ double block_sum_ops(double v, double *sh) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  if (lane == 0) sh[w] = v;
+  __syncthreads();
+  double r = 0.0;
+  if (threadIdx.x < 32) {
+    r = (lane < (int)(blockDim.x >> 5)) ? sh[lane] : 0.0;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) r += __shfl_xor_sync(0xffffffffu, r, o);
+  }
+  __syncthreads();
+  return r;
+}
+
 }  // namespace imsrg

@@ -23,6 +23,7 @@
 #include <cmath>
 #include <vector>
 
+#include "device.cuh"
 #include "internal.h"
 
 namespace imsrg {
@@ -118,15 +119,24 @@ __global__ void k_magnus_init(FlowDev *F, cudaGraphConditionalHandle h) {
   cudaGraphSetConditional(h, magnus_init_go(F));
 }
 
-__global__ void k_magnus_next(FlowDev *F, cudaGraphConditionalHandle h) {
-  cudaGraphSetConditional(h, magnus_next_go(F));
-}
-
 __global__ void k_bch_init(FlowDev *F, cudaGraphConditionalHandle h, double ds) {
   cudaGraphSetConditional(h, bch_init_go(F, ds));
 }
 
-__global__ void k_bch_next(FlowDev *F, cudaGraphConditionalHandle h) { cudaGraphSetConditional(h, bch_next_go(F)); }
+// A series term's norm from its partials (k_final_sum's order, so the same
+// bits) and the series' stop test in one launch.
+template <bool MAGNUS>
+__global__ void __launch_bounds__(256) k_norm_next(const double *partials, int n, FlowDev *F,
+                                                   cudaGraphConditionalHandle h) {
+  __shared__ double sh[32];
+  double s = 0.0;
+  for (int i = threadIdx.x; i < n; i += blockDim.x) s += partials[i];
+  s = block_sum_ops(s, sh);
+  if (threadIdx.x == 0) {
+    F->nrm = sqrt(s);
+    cudaGraphSetConditional(h, MAGNUS ? magnus_next_go(F) : bch_next_go(F));
+  }
+}
 
 __global__ void k_step_end(FlowDev *F, const double *HS) { F->e0 = HS[0]; }
 
@@ -207,8 +217,8 @@ int build_step_graph(imsrg_basis *b, FlowGraph *fg, imsrg_op *HS, imsrg_op *G, i
   // one Magnus term: X1 = [G, X0]; DG += cof X1; |X1|; X0 = X1
   IMSRG_TRY(capture(b, body, {}, [&]() -> int {
     IMSRG_TRY(commutator_dev(b, G->d, G->herm, X0->d, -1, X1->d, -G->herm * -1, precision, 0));
-    IMSRG_TRY(launch_series_update(b, DG->d, X1->d, &F->cof, X0->d, &F->nrm));
-    k_magnus_next<<<1, 1, 0, b->stream>>>(F, hM);
+    IMSRG_TRY(launch_series_update(b, DG->d, X1->d, &F->cof, X0->d, nullptr));
+    k_norm_next<true><<<1, 256, 0, b->stream>>>(b->partials, b->nchunks, F, hM);
     return cuda_status(cudaGetLastError());
   }, nullptr));
   // euler_step, then BCH_EXPAND set-up: HS = H0, X0 = H0
@@ -223,8 +233,8 @@ int build_step_graph(imsrg_basis *b, FlowGraph *fg, imsrg_op *HS, imsrg_op *G, i
   // one BCH term: X1 = [G, X0] (with E0); HS += X1 / n!; |X1|; X0 = X1
   IMSRG_TRY(capture(b, body, {}, [&]() -> int {
     IMSRG_TRY(commutator_dev(b, G->d, G->herm, X0->d, H0->herm, X1->d, -G->herm * H0->herm, precision, 1));
-    IMSRG_TRY(launch_series_update(b, HS->d, X1->d, &F->coef, X0->d, &F->nrm));
-    k_bch_next<<<1, 1, 0, b->stream>>>(F, hB);
+    IMSRG_TRY(launch_series_update(b, HS->d, X1->d, &F->coef, X0->d, nullptr));
+    k_norm_next<false><<<1, 256, 0, b->stream>>>(b->partials, b->nchunks, F, hB);
     return cuda_status(cudaGetLastError());
   }, nullptr));
   // next generator and the stop criterion

@@ -391,7 +391,9 @@ int launch_axpby(imsrg_basis *b, const double *A, double ax, const double *B, do
 int launch_axpby_dev(imsrg_basis *b, const double *A, double ax, const double *B, const double *bx, double *C);
 // S += *coef_dev X1, X0 = X1 (unless X0 is null), *d_norm = mat_frob_norm(X1):
 // one series term's bookkeeping in one pass over X1 (the same values as
-// launch_axpby_dev, a copy and launch_norm)
+// launch_axpby_dev, a copy and launch_norm).  d_norm null: the norm's
+// partials stay in b->partials (b->nchunks of them) for a kernel that sums
+// them with block_sum_ops in k_final_sum's order
 int launch_series_update(imsrg_basis *b, double *S, const double *X1, const double *coef_dev, double *X0,
                          double *d_norm);
 int launch_norm(imsrg_basis *b, const double *op, double *d_out);

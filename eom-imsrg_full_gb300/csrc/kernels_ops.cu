@@ -32,22 +32,6 @@ __global__ void k_axpby(const double *__restrict__ A, double ax, const double *_
   for (; i < n; i += stride) C[i] = axpby_elem(A[i], ax, B[i], bx);
 }
 
-__device__ double block_sum_ops(double v, double *sh) {
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-  int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  if (lane == 0) sh[w] = v;
-  __syncthreads();
-  double r = 0.0;
-  if (threadIdx.x < 32) {
-    r = (lane < (int)(blockDim.x >> 5)) ? sh[lane] : 0.0;
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) r += __shfl_xor_sync(0xffffffffu, r, o);
-  }
-  __syncthreads();
-  return r;
-}
-
 // sum of squares of one chunk, times its weight
 __global__ void __launch_bounds__(256) k_norm_partial(const double *__restrict__ op, const NormChunk *chunks,
                                                       double *partials) {
@@ -416,8 +400,11 @@ int launch_series_update(imsrg_basis *b, double *S, const double *X1, const doub
                          double *d_norm) {
   ProfScope ps(b, IMSRG_KERNEL_OPS);
   k_series_update<<<b->nchunks, 256, 0, b->stream>>>(S, X1, coef_dev, S, X0, b->d_chunks, b->partials);
-  k_final_sum<<<1, 256, 0, b->stream>>>(b->partials, b->nchunks, d_norm, 1);
-  b->launches += 2;
+  b->launches++;
+  if (d_norm) {
+    k_final_sum<<<1, 256, 0, b->stream>>>(b->partials, b->nchunks, d_norm, 1);
+    b->launches++;
+  }
   return cuda_status(cudaGetLastError());
 }
 
