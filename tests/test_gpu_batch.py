@@ -10,21 +10,24 @@ from conftest import make_case
 pytestmark = pytest.mark.gpu
 
 
-def _instances(gpu_lib, emaxes):
+def _instances(gpu_lib, emaxes, digits=None):
     from imsrg_gpu.synth import synth_hamiltonian, synth_omega
     out = []
     for k, emax in enumerate(emaxes):
         bas, lay = make_case(emax)
         B = gpu_lib.Basis.from_dict(bas)
+        if digits:
+            B.set_split_digits(digits)
         Hh = synth_hamiltonian(lay, 40 + k, hw=12.0 + 3.0 * k, sigma2=0.5 + 0.3 * k)
         Oh = synth_omega(lay, 40 + k)
         out.append((B, lay, Hh, Oh))
     return out
 
 
-@pytest.mark.parametrize("precision", ["ozaki", "fp64"])
-def test_batch_equals_single_commutators(gpu_lib, precision):
-    inst = _instances(gpu_lib, [2, 4, 6, 4, 2, 6])
+@pytest.mark.parametrize("precision,digits", [("ozaki", None), ("fp64", None), ("ozaki", 8)])
+def test_batch_equals_single_commutators(gpu_lib, precision, digits):
+    """digits = 8: the FP64-class split engine (chunked FP64 sums at emax = 6)."""
+    inst = _instances(gpu_lib, [2, 4, 6, 4, 2, 6], digits)
     refs = []
     for B, lay, Hh, Oh in inst:
         O, H, R = gpu_lib.Operator(B, -1, Oh), gpu_lib.Operator(B, 1, Hh), gpu_lib.Operator(B, 1)
