@@ -419,7 +419,9 @@ def commutator_host(basis: Basis, L: np.ndarray, herm_L: int, R: np.ndarray, her
 def commutator_host_packed(basis: Basis, L: np.ndarray, herm_L: int, R: np.ndarray, herm_R: int, RES: np.ndarray,
                            precision: str = "fp64", with_e0: bool = True):
     """[L, R] on host operands in the packed (vectorize) layout, neq doubles
-    each: copies in, device unpacking, commutator, device packing, copy out."""
+    each.  Page-locked arrays the device can address (e.g. pinned torch
+    tensors' numpy views) are read and written in place by the device's
+    unpack and pack kernels; other arrays are copied in and out."""
     n = basis.neq
     for a in (L, R, RES):
         if a.dtype != _F64 or not a.flags.c_contiguous or a.size != n:
